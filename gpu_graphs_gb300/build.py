@@ -1,0 +1,77 @@
+"""Build recipe of libgbfs.so (sm_103a only).
+
+Every translation unit under csrc/ is compiled in parallel with
+``nvcc -gencode arch=compute_103a,code=sm_103a`` into _build/, then linked
+into gpu_graphs_gb300/libgbfs.so next to this file (static cudart, so the
+library needs only the driver at run time).  No cmake, no torch extension
+machinery: plain nvcc, so the same command works on x86_64 and aarch64.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+CSRC = HERE / "csrc"
+BUILD = HERE / "_build"
+LIB = HERE / "libgbfs.so"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+         "--expt-relaxed-constexpr", "-diag-suppress", "177"]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and Path(cand).exists():
+            return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libgbfs.so")
+
+
+def sources() -> list[Path]:
+    return sorted(list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cpp")))
+
+
+def _stale(lib: Path, deps: list[Path]) -> bool:
+    if not lib.exists():
+        return True
+    t = lib.stat().st_mtime
+    return any(d.stat().st_mtime > t for d in deps)
+
+
+def build(verbose: bool = False, force: bool = False) -> Path:
+    """Compile csrc/ into libgbfs.so if anything changed; return its path."""
+    srcs = sources()
+    deps = srcs + list(CSRC.glob("*.cuh")) + list((HERE.parent / "include").glob("*.h")) + [Path(__file__)]
+    if not force and not _stale(LIB, deps):
+        return LIB
+    BUILD.mkdir(exist_ok=True)
+    cc = nvcc()
+
+    def compile_one(src: Path) -> Path:
+        obj = BUILD / (src.name + ".o")
+        cmd = [cc, *ARCH, *FLAGS, "-c", str(src), "-o", str(obj)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed on {src.name}:\n{r.stderr}")
+        if verbose and r.stderr.strip():
+            print(r.stderr, file=sys.stderr)
+        return obj
+
+    workers = min(len(srcs), max(1, os.cpu_count() or 1))
+    with cf.ThreadPoolExecutor(workers) as ex:
+        objs = list(ex.map(compile_one, srcs))
+    tmp = LIB.with_suffix(".so.tmp")
+    cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lpthread"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose=True, force="--force" in sys.argv))

@@ -1,0 +1,676 @@
+// api.cu -- the extern "C" entry points of libgbfs.so (see include/gbfs.h).
+#include <algorithm>
+#include <cerrno>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/gbfs.h"
+#include "graph.cuh"
+#include "scan.cuh"
+
+namespace gbfs {
+
+static thread_local std::string tl_error;
+
+void set_error(const std::string &msg) { tl_error = msg; }
+
+int fail(int code, const std::string &msg)
+{
+    tl_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    tl_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? GBFS_ERR_OOM : GBFS_ERR_CUDA;
+}
+
+bool is_device_ptr(const void *p)
+{
+    if (!p) return false;
+    cudaPointerAttributes at;
+    cudaError_t e = cudaPointerGetAttributes(&at, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+namespace {
+
+// Symmetry check on sorted rows: every (u,v) has (v,u).
+__global__ void k_check_sym(const int *__restrict__ row, const int *__restrict__ col, int n,
+                            int *flags /*[0] unsorted, [1] asymmetric*/)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += stride) {
+        const int b = row[u], e = row[u + 1];
+        for (int i = b; i < e; i++) {
+            const int v = col[i];
+            if (i > b && col[i - 1] > v) {
+                flags[0] = 1;
+                return;
+            }
+            int lo = row[v], hi = row[v + 1];
+            while (lo < hi) {
+                int mid = (lo + hi) >> 1;
+                if (col[mid] < (int)u) lo = mid + 1; else hi = mid;
+            }
+            if (lo >= row[v + 1] || col[lo] != (int)u) flags[1] = 1;
+        }
+    }
+}
+
+int check_symmetric(const DeviceCsr &c, cudaStream_t st, bool &sym)
+{
+    int *d = nullptr, h[2] = {0, 0};
+    cudaError_t e = cudaMalloc(&d, 8);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, 8, st);
+    if (e == cudaSuccess) {
+        int grid = (int)std::min<int64_t>(152 * 8, ((int64_t)c.n + 255) / 256);
+        k_check_sym<<<std::max(grid, 1), 256, 0, st>>>(c.row, c.col, c.n, d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, 8, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (d) cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(e, "symmetry check");
+    sym = h[0] == 0 && h[1] == 0;
+    return GBFS_OK;
+}
+
+}  // namespace
+
+int graph_wrap(DeviceCsr &csr, bool symmetric_known, bool symmetric, cudaStream_t st, gbfs_graph **out)
+{
+    gbfs_graph *g = new (std::nothrow) gbfs_graph();
+    if (!g) {
+        csr_free(csr);
+        if (st) cudaStreamDestroy(st);
+        return fail(GBFS_ERR_OOM, "host allocation failed");
+    }
+    g->csr = csr;
+    csr = DeviceCsr{};
+    g->stream = st;
+    cudaGetDevice(&g->device);
+    gbfs_default_params(&g->params);
+    if (symmetric_known) {
+        g->symmetric = symmetric;
+    } else {
+        bool s = false;
+        int rc = check_symmetric(g->csr, st, s);
+        if (rc != GBFS_OK) {
+            gbfs_graph_destroy(g);
+            return rc;
+        }
+        g->symmetric = s;
+    }
+    *out = g;
+    return GBFS_OK;
+}
+
+}  // namespace gbfs
+
+using namespace gbfs;
+
+// ---- status -----------------------------------------------------------------
+
+extern "C" const char *gbfs_strerror(int status)
+{
+    switch (status) {
+    case GBFS_OK: return "ok";
+    case GBFS_ERR_INVALID_ARG: return "invalid argument";
+    case GBFS_ERR_OOM: return "out of memory";
+    case GBFS_ERR_CUDA: return "CUDA error";
+    case GBFS_ERR_TIMEOUT: return "device-side wait timed out";
+    case GBFS_ERR_TOO_LARGE: return "graph too large for int32 CSR";
+    case GBFS_ERR_IO: return "file missing or malformed";
+    case GBFS_ERR_BUDGET: return "memory budget exceeded";
+    case GBFS_ERR_NOT_FOUND: return "unknown graph id or ticket";
+    case GBFS_ERR_SHUTDOWN: return "server is shutting down";
+    default: return "unknown status";
+    }
+}
+
+extern "C" const char *gbfs_last_error(void) { return tl_error.c_str(); }
+
+extern "C" const char *gbfs_version(void) { return "gbfs 0.1 (sm_103a)"; }
+
+extern "C" void gbfs_free(void *p) { free(p); }
+
+// ---- params -------------------------------------------------------------------
+
+extern "C" int gbfs_default_params(gbfs_params *p)
+{
+    if (!p) return fail(GBFS_ERR_INVALID_ARG, "params is NULL");
+    p->threads_per_block = 512;
+    p->blocks_per_sm = 2;
+    p->alpha = 14;
+    p->beta = 24;
+    p->big_degree = 256;
+    p->direction = GBFS_DIR_OPTIMIZING;
+    p->per_level_launch = 0;
+    p->timeout_ms = 2000;
+    return GBFS_OK;
+}
+
+static int validate_params(const gbfs_params *p)
+{
+    if (!p) return fail(GBFS_ERR_INVALID_ARG, "params is NULL");
+    if (p->threads_per_block != 256 && p->threads_per_block != 512 && p->threads_per_block != 1024)
+        return fail(GBFS_ERR_INVALID_ARG, "threads_per_block must be 256, 512 or 1024");
+    if (p->blocks_per_sm < 1 || p->blocks_per_sm > 32)
+        return fail(GBFS_ERR_INVALID_ARG, "blocks_per_sm must be in [1, 32]");
+    if (p->alpha < 1 || p->beta < 1) return fail(GBFS_ERR_INVALID_ARG, "alpha and beta must be >= 1");
+    if (p->big_degree < 32) return fail(GBFS_ERR_INVALID_ARG, "big_degree must be >= 32");
+    if (p->direction < 0 || p->direction > 2) return fail(GBFS_ERR_INVALID_ARG, "bad direction");
+    if (p->per_level_launch != 0 && p->per_level_launch != 1)
+        return fail(GBFS_ERR_INVALID_ARG, "per_level_launch must be 0 or 1");
+    if (p->timeout_ms < 1) return fail(GBFS_ERR_INVALID_ARG, "timeout_ms must be >= 1");
+    return GBFS_OK;
+}
+
+extern "C" int gbfs_get_params(const gbfs_graph *g, gbfs_params *p)
+{
+    if (!g || !p) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
+    *p = g->params;
+    return GBFS_OK;
+}
+
+extern "C" int gbfs_set_params(gbfs_graph *g, const gbfs_params *p)
+{
+    if (!g) return fail(GBFS_ERR_INVALID_ARG, "graph is NULL");
+    int rc = validate_params(p);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lk(g->mu);
+    g->params = *p;
+    return GBFS_OK;
+}
+
+// ---- graph construction ----------------------------------------------------
+
+static int make_stream(cudaStream_t *st)
+{
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(GBFS_ERR_CUDA, "no CUDA device available");
+    }
+    e = cudaStreamCreateWithFlags(st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamCreate");
+    return GBFS_OK;
+}
+
+// Copy `count` ints from host or device `p` into a new device buffer.
+static int to_device(const int32_t *p, int64_t count, cudaStream_t st, int **out, bool *owned)
+{
+    *owned = false;
+    if (count == 0) {
+        *out = nullptr;
+        return GBFS_OK;
+    }
+    if (is_device_ptr(p)) {
+        *out = const_cast<int *>(p);
+        return GBFS_OK;
+    }
+    cudaError_t e = cudaMalloc(out, sizeof(int) * (size_t)count);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    *owned = true;
+    e = cudaMemcpyAsync(*out, p, sizeof(int) * (size_t)count, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy H2D");
+    return GBFS_OK;
+}
+
+extern "C" int gbfs_graph_from_edges(int32_t n, int64_t m, const int32_t *src, const int32_t *dst,
+                                     uint32_t flags, gbfs_graph **out)
+{
+    if (!out) return fail(GBFS_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    if (n < 1 || n > INT32_MAX - 1) return fail(GBFS_ERR_INVALID_ARG, "n must be in [1, 2^31-2]");
+    if (m < 0 || (m > 0 && (!src || !dst))) return fail(GBFS_ERR_INVALID_ARG, "bad edge arrays");
+    if (flags & ~7u) return fail(GBFS_ERR_INVALID_ARG, "unknown flag bits");
+    if (m > (int64_t)INT32_MAX * 2) return fail(GBFS_ERR_TOO_LARGE, "too many edges");
+    cudaStream_t st = nullptr;
+    int rc = make_stream(&st);
+    if (rc) return rc;
+    int *d_src = nullptr, *d_dst = nullptr;
+    bool own_s = false, own_d = false;
+    DeviceCsr csr;
+    std::string err;
+    rc = to_device(src, m, st, &d_src, &own_s);
+    if (!rc) rc = to_device(dst, m, st, &d_dst, &own_d);
+    if (!rc) {
+        rc = csr_build_from_edges(n, m, d_src, d_dst, flags, st, csr, err);
+        if (rc) set_error(err);
+    }
+    cudaStreamSynchronize(st);
+    if (own_s) cudaFree(d_src);
+    if (own_d) cudaFree(d_dst);
+    if (rc) {
+        cudaStreamDestroy(st);
+        return rc;
+    }
+    return graph_wrap(csr, (flags & GBFS_SYMMETRIZE) != 0, true, st, out);
+}
+
+extern "C" int gbfs_graph_from_csr(int32_t n, int64_t m, const int32_t *row_offset,
+                                   const int32_t *col_idx, gbfs_graph **out)
+{
+    if (!out) return fail(GBFS_ERR_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    if (n < 1 || n > INT32_MAX - 1) return fail(GBFS_ERR_INVALID_ARG, "n must be in [1, 2^31-2]");
+    if (m < 0 || m > INT32_MAX) return fail(m < 0 ? GBFS_ERR_INVALID_ARG : GBFS_ERR_TOO_LARGE, "bad m");
+    if (!row_offset || (m > 0 && !col_idx)) return fail(GBFS_ERR_INVALID_ARG, "NULL CSR array");
+    cudaStream_t st = nullptr;
+    int rc = make_stream(&st);
+    if (rc) return rc;
+    int *d_row = nullptr, *d_col = nullptr;
+    cudaError_t e = cudaMalloc(&d_row, sizeof(int) * ((size_t)n + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&d_col, sizeof(int) * (size_t)std::max<int64_t>(m, 1));
+    const cudaMemcpyKind kr = is_device_ptr(row_offset) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    const cudaMemcpyKind kc = is_device_ptr(col_idx) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_row, row_offset, sizeof(int) * ((size_t)n + 1), kr, st);
+    if (e == cudaSuccess && m > 0) e = cudaMemcpyAsync(d_col, col_idx, sizeof(int) * (size_t)m, kc, st);
+    if (e != cudaSuccess) {
+        if (d_row) cudaFree(d_row);
+        if (d_col) cudaFree(d_col);
+        cudaStreamDestroy(st);
+        return cuda_fail(e, "CSR upload");
+    }
+    DeviceCsr csr;
+    std::string err;
+    rc = csr_adopt(n, m, d_row, d_col, st, csr, err);
+    if (rc) {
+        set_error(err);
+        cudaStreamDestroy(st);
+        return rc;
+    }
+    return graph_wrap(csr, false, false, st, out);
+}
+
+extern "C" void gbfs_graph_destroy(gbfs_graph *g)
+{
+    if (!g) return;
+    if (g->batch_set) gbfs_graphset_destroy(g->batch_set);
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    bfs_work_free(g->work);
+    ms_work_free(g->ms);
+    csr_free(g->csr);
+    if (g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+}
+
+extern "C" int gbfs_graph_get_info(const gbfs_graph *g, gbfs_graph_info *info)
+{
+    if (!g || !info) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
+    info->n = g->csr.n;
+    info->m = g->csr.m;
+    info->max_degree = g->csr.max_degree;
+    info->nonisolated = g->csr.nonisolated;
+    info->device_bytes = (int64_t)sizeof(int) * ((int64_t)g->csr.n + 1 + g->csr.m) +
+                         4 * (((int64_t)g->csr.n + 31) / 32) + g->work.bytes + g->ms.bytes;
+    return GBFS_OK;
+}
+
+extern "C" int gbfs_graph_get_csr(const gbfs_graph *g, int32_t *row_offset, int32_t *col_idx)
+{
+    if (!g || !row_offset || (g->csr.m > 0 && !col_idx)) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
+    gbfs_graph *gg = const_cast<gbfs_graph *>(g);
+    std::lock_guard<std::mutex> lk(gg->mu);
+    const cudaMemcpyKind kr = is_device_ptr(row_offset) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    const cudaMemcpyKind kc = is_device_ptr(col_idx) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    cudaError_t e = cudaMemcpyAsync(row_offset, g->csr.row, sizeof(int) * ((size_t)g->csr.n + 1), kr, g->stream);
+    if (e == cudaSuccess && g->csr.m > 0)
+        e = cudaMemcpyAsync(col_idx, g->csr.col, sizeof(int) * (size_t)g->csr.m, kc, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "CSR download");
+    return GBFS_OK;
+}
+
+// ---- traversal ------------------------------------------------------------------
+
+static void fill_stats(gbfs_stats *s, const BfsResult &r, int64_t nsources)
+{
+    if (!s) return;
+    s->ms = r.ms;
+    s->levels = r.levels;
+    s->td_levels = r.td_levels;
+    s->bu_levels = r.bu_levels;
+    s->launches = r.launches;
+    s->vertices_reached = r.reached;
+    s->edges_in_component = r.edges_c;
+    s->edges_traversed = r.reached - nsources;
+}
+
+static gbfs_params effective_params(const gbfs_graph *g)
+{
+    gbfs_params p = g->params;
+    if (!g->symmetric) p.direction = GBFS_DIR_TOPDOWN;
+    return p;
+}
+
+// Runs a BFS into the graph's workspace or the caller's device buffer, then
+// copies to the caller's host buffer if needed.  Caller holds g->mu.
+static int run_bfs_locked(gbfs_graph *g, const int *d_roots, int k, int single_root, int32_t *levels_out,
+                          BfsResult &res)
+{
+    std::string err;
+    int rc = bfs_work_alloc(g->work, g->csr.n, err);
+    if (rc) return fail(rc, err);
+    const bool dev_out = is_device_ptr(levels_out);
+    int *d_level = dev_out ? levels_out : g->work.level;
+    gbfs_params p = effective_params(g);
+    rc = bfs_run(g->csr, p, g->work, d_roots, k, single_root, d_level, g->stream, res, err);
+    if (rc) return fail(rc, err);
+    if (!dev_out) {
+        cudaError_t e = cudaMemcpyAsync(levels_out, d_level, sizeof(int) * (size_t)g->csr.n,
+                                        cudaMemcpyDeviceToHost, g->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "levels D2H");
+    }
+    return GBFS_OK;
+}
+
+extern "C" int gbfs_bfs(gbfs_graph *g, int32_t source, int32_t *levels_out, gbfs_stats *stats)
+{
+    if (!g || !levels_out) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
+    if (source < 0 || source >= g->csr.n) return fail(GBFS_ERR_INVALID_ARG, "source outside [0, n)");
+    std::lock_guard<std::mutex> lk(g->mu);
+    BfsResult res;
+    int rc = run_bfs_locked(g, nullptr, 1, source, levels_out, res);
+    if (rc) return rc;
+    fill_stats(stats, res, 1);
+    return GBFS_OK;
+}
+
+extern "C" int gbfs_bfs_many(gbfs_graph *g, const int32_t *sources, int32_t k, int32_t *levels_out,
+                             gbfs_stats *stats)
+{
+    if (!g || !sources || k < 1) return fail(GBFS_ERR_INVALID_ARG, "bad argument");
+    std::vector<int32_t> hsrc((size_t)k);
+    if (is_device_ptr(sources)) {
+        cudaError_t e = cudaMemcpy(hsrc.data(), sources, sizeof(int32_t) * (size_t)k, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(e, "sources D2H");
+    } else {
+        std::copy(sources, sources + k, hsrc.begin());
+    }
+    for (int32_t i = 0; i < k; i++)
+        if (hsrc[i] < 0 || hsrc[i] >= g->csr.n) return fail(GBFS_ERR_INVALID_ARG, "source outside [0, n)");
+    std::lock_guard<std::mutex> lk(g->mu);
+    std::string err;
+    int rc = bfs_work_alloc(g->work, g->csr.n, err);
+    if (!rc) rc = bfs_work_reserve_many(g->work, k, err);
+    if (rc) return fail(rc, err);
+    BfsWork &w = g->work;
+    const size_t n = (size_t)g->csr.n;
+    const bool dev_out = levels_out && is_device_ptr(levels_out);
+    const gbfs_params p = effective_params(g);
+    cudaError_t e = cudaSuccess;
+    for (int32_t i = 0; i < k && e == cudaSuccess; i++) {
+        int *d_level = dev_out ? levels_out + n * i : w.level;
+        e = cudaEventRecord(w.evs[i], g->stream);
+        if (e == cudaSuccess) e = bfs_enqueue(g->csr, p, w, nullptr, 1, hsrc[i], d_level, w.d_outs + i, g->stream);
+        if (e == cudaSuccess && levels_out && !dev_out)
+            e = cudaMemcpyAsync(levels_out + n * i, d_level, sizeof(int) * n, cudaMemcpyDeviceToHost, g->stream);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(w.evs[k], g->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(w.h_outs, w.d_outs, sizeof(BfsOut) * (size_t)k, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(w.h_ctrl, w.ctrl, sizeof(BfsCtrl), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "BFS launches");
+    if (w.h_ctrl->status != DEV_OK) {
+        cudaMemsetAsync(w.ctrl, 0, sizeof(BfsCtrl), g->stream);
+        cudaStreamSynchronize(g->stream);
+        return fail(GBFS_ERR_TIMEOUT, "a device-side wait ran out (grid barrier)");
+    }
+    if (stats)
+        for (int32_t i = 0; i < k; i++) {
+            BfsResult r;
+            cudaEventElapsedTime(&r.ms, w.evs[i], w.evs[i + 1]);
+            const BfsOut &o = w.h_outs[i];
+            r.levels = o.levels;
+            r.td_levels = o.td_levels;
+            r.bu_levels = o.bu_levels;
+            r.launches = 1;
+            r.reached = (int64_t)o.reached;
+            r.edges_c = (int64_t)o.edges_c;
+            fill_stats(&stats[i], r, 1);
+        }
+    return GBFS_OK;
+}
+
+extern "C" void *gbfs_graph_stream(const gbfs_graph *g) { return g ? (void *)g->stream : nullptr; }
+
+extern "C" int gbfs_bfs_multiroot(gbfs_graph *g, const int32_t *sources, int32_t k, int32_t *levels_out,
+                                  gbfs_stats *stats)
+{
+    if (!g || !levels_out || !sources || k < 1) return fail(GBFS_ERR_INVALID_ARG, "bad argument");
+    if (k > g->csr.n) return fail(GBFS_ERR_INVALID_ARG, "more roots than vertices");
+    const bool dev_src = is_device_ptr(sources);
+    if (!dev_src)
+        for (int32_t i = 0; i < k; i++)
+            if (sources[i] < 0 || sources[i] >= g->csr.n) return fail(GBFS_ERR_INVALID_ARG, "root outside [0, n)");
+    std::lock_guard<std::mutex> lk(g->mu);
+    std::string err;
+    int rc = bfs_work_alloc(g->work, g->csr.n, err);
+    if (rc) return fail(rc, err);
+    cudaError_t e = cudaMemcpyAsync(g->work.roots, sources, sizeof(int) * (size_t)k,
+                                    dev_src ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, g->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "roots upload");
+    BfsResult res;
+    rc = run_bfs_locked(g, g->work.roots, k, -1, levels_out, res);
+    if (rc) return rc;
+    fill_stats(stats, res, res.roots);
+    return GBFS_OK;
+}
+
+extern "C" int gbfs_bfs_multi(gbfs_graph *g, const int32_t *sources, int32_t k, int32_t *levels_out,
+                              gbfs_stats *stats)
+{
+    if (!g || !levels_out || !sources || k < 1) return fail(GBFS_ERR_INVALID_ARG, "bad argument");
+    const bool dev_src = is_device_ptr(sources);
+    std::vector<int32_t> hsrc;
+    if (dev_src) {
+        hsrc.resize(k);
+        cudaError_t e = cudaMemcpy(hsrc.data(), sources, sizeof(int) * (size_t)k, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(e, "sources D2H");
+    } else {
+        hsrc.assign(sources, sources + k);
+    }
+    for (int32_t i = 0; i < k; i++)
+        if (hsrc[i] < 0 || hsrc[i] >= g->csr.n) return fail(GBFS_ERR_INVALID_ARG, "source outside [0, n)");
+    std::lock_guard<std::mutex> lk(g->mu);
+    std::string err;
+    int rc = ms_work_alloc(g->ms, g->csr.n, err);
+    if (rc) return fail(rc, err);
+    const bool dev_out = is_device_ptr(levels_out);
+    const size_t n = (size_t)g->csr.n;
+    gbfs_params p = g->params;
+    MsResult tot;
+    for (int32_t b0 = 0; b0 < k; b0 += MS_LANES) {
+        const int kk = std::min<int>(MS_LANES, k - b0);
+        cudaError_t e = cudaMemcpyAsync(g->ms.src, hsrc.data() + b0, sizeof(int) * kk, cudaMemcpyHostToDevice,
+                                        g->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "sources H2D");
+        int *d_out = dev_out ? levels_out + (size_t)b0 * n : g->ms.out;
+        MsResult r;
+        rc = msbfs_run(g->csr, p, g->symmetric, g->ms, g->ms.src, kk, d_out, g->stream, r, err);
+        if (rc) return fail(rc, err);
+        if (!dev_out) {
+            e = cudaMemcpyAsync(levels_out + (size_t)b0 * n, d_out, sizeof(int) * n * kk, cudaMemcpyDeviceToHost,
+                                g->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+            if (e != cudaSuccess) return cuda_fail(e, "levels D2H");
+        }
+        tot.ms += r.ms;
+        tot.levels = std::max(tot.levels, r.levels);
+        tot.push_levels += r.push_levels;
+        tot.pull_levels += r.pull_levels;
+        tot.reached += r.reached;
+        tot.edges_c += r.edges_c;
+    }
+    if (stats) {
+        stats->ms = tot.ms;
+        stats->levels = tot.levels;
+        stats->td_levels = tot.push_levels;
+        stats->bu_levels = tot.pull_levels;
+        stats->launches = (k + MS_LANES - 1) / MS_LANES;
+        stats->vertices_reached = tot.reached;
+        stats->edges_in_component = tot.edges_c;
+        stats->edges_traversed = tot.reached - k;
+    }
+    return GBFS_OK;
+}
+
+// ---- scan primitive --------------------------------------------------------------
+
+namespace {
+struct ScanPool {
+    std::mutex mu;
+    void *mem = nullptr;
+    int64_t tiles = 0;
+    ScanScratch s;
+    int device = -1;
+};
+ScanPool g_scan_pool[64];
+}  // namespace
+
+extern "C" int gbfs_exclusive_scan_i32(const int32_t *d_in, int64_t *d_out, int64_t n, void *stream)
+{
+    if (n < 0 || (n > 0 && (!d_in || !d_out))) return fail(GBFS_ERR_INVALID_ARG, "bad argument");
+    if (n == 0) return GBFS_OK;
+    if (!is_device_ptr(d_in) || !is_device_ptr(d_out))
+        return fail(GBFS_ERR_INVALID_ARG, "d_in and d_out must be device pointers");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    ScanPool &pool = g_scan_pool[dev & 63];
+    std::lock_guard<std::mutex> lk(pool.mu);
+    const int64_t tiles = scan_tiles(n);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (pool.tiles < tiles) {
+        if (pool.mem) {
+            cudaDeviceSynchronize();
+            cudaFree(pool.mem);
+            pool.mem = nullptr;
+        }
+        const int64_t want = std::max<int64_t>(tiles, 1024);
+        e = cudaMalloc(&pool.mem, scan_scratch_bytes(want));
+        if (e != cudaSuccess) {
+            pool.tiles = 0;
+            return cuda_fail(e, "scan scratch");
+        }
+        e = cudaMemset(pool.mem, 0, scan_scratch_bytes(want));
+        if (e != cudaSuccess) return cuda_fail(e, "scan scratch");
+        scan_scratch_carve(pool.mem, want, pool.s);
+        pool.tiles = want;
+        pool.s.epoch = 0;
+    }
+    e = scan_exclusive_i32_i64(d_in, (long long *)d_out, n, nullptr, pool.s, st);
+    if (e != cudaSuccess) return cuda_fail(e, "scan launch");
+    unsigned status = 0;
+    e = cudaMemcpyAsync(&status, pool.s.ctl + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "scan");
+    if (status != 0) {
+        unsigned zero = 0;
+        cudaMemcpy(pool.s.ctl + 2, &zero, sizeof(unsigned), cudaMemcpyHostToDevice);
+        return fail(GBFS_ERR_TIMEOUT, "scan look-back wait ran out");
+    }
+    return GBFS_OK;
+}
+
+// ---- file format ------------------------------------------------------------------
+
+extern "C" int gbfs_read_edge_list(const char *path, int32_t one_based, int32_t *n, int64_t *m, int32_t **src,
+                                   int32_t **dst)
+{
+    if (!path || !n || !m || !src || !dst) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
+    *src = *dst = nullptr;
+    FILE *f = fopen(path, "rb");
+    if (!f) return fail(GBFS_ERR_IO, std::string("Unable to open file ") + path);
+    long long hn = 0, hm = 0;
+    if (fscanf(f, "%lld %lld", &hn, &hm) != 2 || hn < 1 || hn > INT32_MAX - 1 || hm < 0) {
+        fclose(f);
+        return fail(GBFS_ERR_IO, "bad header (expected vertex and edge counts)");
+    }
+    std::vector<int32_t> s, d;
+    s.reserve((size_t)std::min<long long>(hm, 1LL << 26));
+    d.reserve(s.capacity());
+    long long a, b;
+    const long long off = one_based ? 1 : 0;
+    // Pairs until end of file, like `while (infile >> from >> to)`.
+    while (fscanf(f, "%lld %lld", &a, &b) == 2) {
+        a -= off;
+        b -= off;
+        if (a < 0 || a >= hn || b < 0 || b >= hn) {
+            fclose(f);
+            return fail(GBFS_ERR_IO, "edge endpoint outside the declared vertex range");
+        }
+        s.push_back((int32_t)a);
+        d.push_back((int32_t)b);
+    }
+    fclose(f);
+    const size_t cnt = s.size();
+    *src = (int32_t *)malloc(sizeof(int32_t) * std::max<size_t>(cnt, 1));
+    *dst = (int32_t *)malloc(sizeof(int32_t) * std::max<size_t>(cnt, 1));
+    if (!*src || !*dst) {
+        free(*src);
+        free(*dst);
+        *src = *dst = nullptr;
+        return fail(GBFS_ERR_OOM, "host allocation failed");
+    }
+    if (cnt) {
+        memcpy(*src, s.data(), sizeof(int32_t) * cnt);
+        memcpy(*dst, d.data(), sizeof(int32_t) * cnt);
+    }
+    *n = (int32_t)hn;
+    *m = (int64_t)cnt;
+    return GBFS_OK;
+}
+
+extern "C" int gbfs_graph_save(const gbfs_graph *g, const char *path)
+{
+    if (!g || !path) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
+    std::vector<int32_t> row((size_t)g->csr.n + 1), col((size_t)std::max<int64_t>(g->csr.m, 1));
+    int rc = gbfs_graph_get_csr(g, row.data(), col.data());
+    if (rc) return rc;
+    FILE *f = fopen(path, "wb");
+    if (!f) return fail(GBFS_ERR_IO, std::string("cannot write ") + path);
+    int32_t n = g->csr.n;
+    int64_t m = g->csr.m;
+    bool ok = fwrite(&n, 4, 1, f) == 1 && fwrite(&m, 8, 1, f) == 1 &&
+              fwrite(row.data(), 4, row.size(), f) == row.size() &&
+              (m == 0 || fwrite(col.data(), 4, (size_t)m, f) == (size_t)m);
+    ok = (fclose(f) == 0) && ok;
+    return ok ? GBFS_OK : fail(GBFS_ERR_IO, "short write");
+}
+
+extern "C" int gbfs_graph_load(const char *path, gbfs_graph **out)
+{
+    if (!path || !out) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
+    *out = nullptr;
+    FILE *f = fopen(path, "rb");
+    if (!f) return fail(GBFS_ERR_IO, std::string("cannot open ") + path);
+    int32_t n = 0;
+    int64_t m = 0;
+    if (fread(&n, 4, 1, f) != 1 || fread(&m, 8, 1, f) != 1 || n < 1 || m < 0 || m > INT32_MAX) {
+        fclose(f);
+        return fail(GBFS_ERR_IO, "bad CSR header");
+    }
+    std::vector<int32_t> row((size_t)n + 1), col((size_t)std::max<int64_t>(m, 1));
+    bool ok = fread(row.data(), 4, row.size(), f) == row.size() &&
+              (m == 0 || fread(col.data(), 4, (size_t)m, f) == (size_t)m);
+    fclose(f);
+    if (!ok) return fail(GBFS_ERR_IO, "truncated CSR file");
+    return gbfs_graph_from_csr(n, m, row.data(), col.data(), out);
+}

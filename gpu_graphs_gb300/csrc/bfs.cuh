@@ -1,0 +1,79 @@
+// bfs.cuh -- single-GPU direction-optimising BFS (host side of bfs.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "common.cuh"
+#include "csr_build.cuh"
+
+namespace gbfs {
+
+// Device control block of one traversal context.  Zeroed at allocation; the
+// kernel leaves it zeroed on success (the host re-zeroes it after an error).
+// Results of one traversal, written by the kernel's thread 0.
+struct BfsOut {
+    int levels, td_levels, bu_levels, roots;   // roots: distinct vertices at level 0
+    unsigned long long reached, edges_c;
+};
+
+struct BfsCtrl {
+    GridBarrier bar;
+    int status;
+    int pad0;
+    unsigned long long cnt[3];   // frontier vertex counts, rotating by level
+    unsigned long long deg[3];   // frontier out-degree sums, rotating by level
+    unsigned big[3];             // top-down rows deferred to the grid pass
+    unsigned pad1;
+    unsigned long long fill;     // bitmap -> queue conversion slots
+    BfsOut out;                  // results of the last traversal (default slot)
+};
+
+// Per-graph traversal workspace (allocated on first use, reused).
+struct BfsWork {
+    int32_t n = 0;
+    int *level = nullptr;        // n (used when the caller's buffer is on the host)
+    unsigned *visited = nullptr; // W
+    unsigned *fb0 = nullptr;     // W frontier bitmaps
+    unsigned *fb1 = nullptr;
+    int *q0 = nullptr;           // n frontier queues
+    int *q1 = nullptr;
+    int *big = nullptr;          // n deferred rows
+    int *roots = nullptr;        // root staging (n)
+    BfsCtrl *ctrl = nullptr;
+    BfsCtrl *h_ctrl = nullptr;   // pinned mirror for results
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // back-to-back launches: per-launch result slots and events
+    BfsOut *d_outs = nullptr;
+    BfsOut *h_outs = nullptr;
+    int outs_cap = 0;
+    cudaEvent_t *evs = nullptr;
+    int evs_cap = 0;
+    int64_t bytes = 0;
+};
+
+int bfs_work_alloc(BfsWork &w, int32_t n, std::string &err);
+void bfs_work_free(BfsWork &w);
+
+struct BfsResult {
+    float ms = 0;
+    int levels = 0, td_levels = 0, bu_levels = 0, launches = 0, roots = 0;
+    int64_t reached = 0, edges_c = 0;
+};
+
+// Enqueues one (multi-root) BFS of `g` writing levels to d_level (device, n
+// int32) and its results to *slot (device).  d_roots: device array of k
+// roots, or single_root >= 0.  Does not synchronise.
+cudaError_t bfs_enqueue(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_roots, int k,
+                        int single_root, int *d_level, BfsOut *slot, cudaStream_t st);
+
+// bfs_enqueue + events + result read-back; synchronises `st`.
+int bfs_run(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_roots, int k,
+            int single_root, int *d_level, cudaStream_t st, BfsResult &res, std::string &err);
+
+// Grow the per-launch slots / events of `w` to at least `k`.
+int bfs_work_reserve_many(BfsWork &w, int k, std::string &err);
+
+}  // namespace gbfs

@@ -1,0 +1,605 @@
+// csr_build.cu -- on-device edge list -> CSR (sm_103a).
+//
+// The reference builds CSR on the host: vector<vector<int>> adjacency lists
+// filled line by line, then flattened (1D Partition/src/csr.cpp:25-65,
+// 2D Partition/src/csc.cpp:18-89), with no dedup, no self-loop removal and
+// no symmetrisation.  Here the same CSR (rows sorted, which does not change
+// BFS levels) is built in HBM:
+//   1. k_count   degree histogram (warp-aggregated atomics: match_any groups
+//                lanes with the same source so hubs take one atomic)
+//   2. scan      decoupled look-back exclusive scan -> row offsets
+//   3. k_scatter each edge to its row (aggregated atomic cursors)
+//   4. k_bin + k_sort_small / k_sort_medium / k_sort_large
+//                per-row sort: rows <= 32 in registers (warp bitonic), rows
+//                <= 4096 in shared memory (CTA bitonic), longer rows with a
+//                CTA-wide stable LSD radix sort; each row also counts (and
+//                packs to its front) its distinct values when deduplicating
+//   5. scan + k_compact   packed rows -> final col_idx (dedup only)
+//   6. k_finalize zero-degree bitmap, max degree, non-isolated count
+#include <algorithm>
+#include <climits>
+#include <cstdio>
+
+#include "common.cuh"
+#include "csr_build.cuh"
+#include "scan.cuh"
+
+namespace gbfs {
+
+namespace {
+
+constexpr int MED_MAX = 4096;     // rows up to this length sort in shared memory
+constexpr int MED_THREADS = 512;
+constexpr int LARGE_THREADS = 1024;
+constexpr int BIN_THREADS = 1024;
+
+#define CK(call)                                                                 \
+    do {                                                                         \
+        cudaError_t e_ = (call);                                                 \
+        if (e_ != cudaSuccess) {                                                 \
+            err = std::string(#call) + ": " + cudaGetErrorString(e_);            \
+            rc = (e_ == cudaErrorMemoryAllocation) ? GBFS_ERR_OOM : GBFS_ERR_CUDA; \
+            goto done;                                                           \
+        }                                                                        \
+    } while (0)
+
+// All 32 lanes call; key < 0 means "no increment".  Returns the old value of
+// arr[key] plus this lane's rank among lanes with the same key.
+__device__ __forceinline__ int agg_atomic_add(int *arr, int key)
+{
+    unsigned peers = __match_any_sync(FULL, key);
+    int leader = __ffs(peers) - 1;
+    int old = 0;
+    if (key >= 0 && (int)lane_id() == leader) old = atomicAdd(&arr[key], __popc(peers));
+    old = __shfl_sync(FULL, old, leader);
+    return old + __popc(peers & lanemask_lt());
+}
+
+template <typename T>
+__device__ __forceinline__ T block_sum(T x, T *s_red)
+{
+    x = warp_sum(x);
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) s_red[warp] = x;
+    __syncthreads();
+    T t = 0;
+    if (warp == 0) {
+        t = lane < (blockDim.x >> 5) ? s_red[lane] : 0;
+        t = warp_sum(t);
+    }
+    return t;  // valid in thread 0
+}
+
+// Exclusive block scan (blockDim.x <= 1024); returns the prefix, *total set.
+__device__ __forceinline__ int block_excl_scan(int x, int *s_warp, int *total)
+{
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int incl = warp_incl_scan(x);
+    __syncthreads();
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < nw ? s_warp[lane] : 0;
+        int wi = warp_incl_scan(w);
+        if (lane < nw) s_warp[lane] = wi - w;
+        if (lane == nw - 1) s_warp[32] = wi;
+    }
+    __syncthreads();
+    *total = s_warp[32];
+    return s_warp[warp] + incl - x;
+}
+
+__global__ void k_count(const int *__restrict__ src, const int *__restrict__ dst, int64_t m,
+                        int n, unsigned flags, int *deg, unsigned long long *total, int *status)
+{
+    __shared__ unsigned long long s_red[32];
+    const bool sym = flags & GBFS_SYMMETRIZE, noself = flags & GBFS_DROP_SELF_LOOPS;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    unsigned long long mine = 0;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < m;
+         base += stride) {
+        int64_t i = base + lane_id();
+        int u = -1, v = -1;
+        if (i < m) {
+            u = src[i];
+            v = dst[i];
+            if ((unsigned)u >= (unsigned)n || (unsigned)v >= (unsigned)n) {
+                atomicExch(status, DEV_BAD_ID);
+                u = v = -1;
+            } else if (noself && u == v) {
+                u = v = -1;
+            }
+        }
+        agg_atomic_add(deg, u);
+        mine += u >= 0;
+        if (sym) {
+            agg_atomic_add(deg, v);
+            mine += v >= 0;
+        }
+    }
+    unsigned long long t = block_sum(mine, s_red);
+    if (threadIdx.x == 0 && t) atomicAdd(total, t);
+}
+
+__global__ void k_scatter(const int *__restrict__ src, const int *__restrict__ dst, int64_t m,
+                          int n, unsigned flags, int *cursor, int *tmp)
+{
+    const bool sym = flags & GBFS_SYMMETRIZE, noself = flags & GBFS_DROP_SELF_LOOPS;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < m;
+         base += stride) {
+        int64_t i = base + lane_id();
+        int u = -1, v = -1;
+        if (i < m) {
+            u = src[i];
+            v = dst[i];
+            if ((unsigned)u >= (unsigned)n || (unsigned)v >= (unsigned)n || (noself && u == v))
+                u = v = -1;
+        }
+        int p = agg_atomic_add(cursor, u);
+        if (u >= 0) tmp[p] = v;
+        if (sym) {
+            int q = agg_atomic_add(cursor, v);
+            if (v >= 0) tmp[q] = u;
+        }
+    }
+}
+
+// Rows longer than 32 go to the medium (<= MED_MAX) or large list.
+__global__ void k_bin(const int *__restrict__ row, int n, int *med, int *large, unsigned *cnt)
+{
+    __shared__ int s_warp[33];
+    __shared__ int s_base[2];
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n;
+         base += (int64_t)gridDim.x * blockDim.x) {
+        int64_t r = base + threadIdx.x;
+        int d = r < n ? row[r + 1] - row[r] : 0;
+        int is_med = d > 32 && d <= MED_MAX, is_large = d > MED_MAX;
+        int tm, tl;
+        int om = block_excl_scan(is_med, s_warp, &tm);
+        int ol = block_excl_scan(is_large, s_warp, &tl);
+        if (threadIdx.x == 0) {
+            s_base[0] = tm ? (int)atomicAdd(&cnt[0], (unsigned)tm) : 0;
+            s_base[1] = tl ? (int)atomicAdd(&cnt[1], (unsigned)tl) : 0;
+        }
+        __syncthreads();
+        if (is_med) med[s_base[0] + om] = (int)r;
+        if (is_large) large[s_base[1] + ol] = (int)r;
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ int warp_bitonic_sort(int x)
+{
+    const unsigned lane = lane_id();
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            int y = __shfl_xor_sync(FULL, x, j);
+            bool up = (lane & k) == 0;
+            bool lower = (lane & j) == 0;
+            x = (lower == up) ? min(x, y) : max(x, y);
+        }
+    }
+    return x;
+}
+
+// One warp per row of length <= 32: sort in registers, pack distinct values.
+__global__ void k_sort_small(const int *__restrict__ row, int n, int *tmp, int dedup, int *ucnt)
+{
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const unsigned lane = lane_id();
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
+        const int b = row[r], d = row[r + 1] - b;
+        if (d > 32) continue;
+        if (d <= 1) {
+            if (lane == 0) ucnt[r] = d;
+            continue;
+        }
+        int x = (int)lane < d ? tmp[b + lane] : INT_MAX;
+        x = warp_bitonic_sort(x);
+        if (dedup) {
+            int prev = __shfl_up_sync(FULL, x, 1);
+            bool uniq = (int)lane < d && (lane == 0 || x != prev);
+            unsigned mask = __ballot_sync(FULL, uniq);
+            if (uniq) tmp[b + __popc(mask & lanemask_lt())] = x;
+            if (lane == 0) ucnt[r] = __popc(mask);
+        } else {
+            if ((int)lane < d) tmp[b + lane] = x;
+            if (lane == 0) ucnt[r] = d;
+        }
+    }
+}
+
+// One CTA per row of length 33..MED_MAX: bitonic sort in shared memory.
+__global__ void __launch_bounds__(MED_THREADS)
+k_sort_medium(const int *__restrict__ row, const int *__restrict__ list, const unsigned *cnt,
+              int *tmp, int dedup, int *ucnt)
+{
+    __shared__ int s[MED_MAX];
+    __shared__ int s_warp[33];
+    const int count = (int)cnt[0];
+    for (int li = blockIdx.x; li < count; li += gridDim.x) {
+        const int r = list[li];
+        const int b = row[r], d = row[r + 1] - b;
+        int P = 64;
+        while (P < d) P <<= 1;
+        for (int i = threadIdx.x; i < P; i += blockDim.x) s[i] = i < d ? tmp[b + i] : INT_MAX;
+        __syncthreads();
+        for (int k = 2; k <= P; k <<= 1) {
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = threadIdx.x; i < P; i += blockDim.x) {
+                    int ixj = i ^ j;
+                    if (ixj > i) {
+                        int a = s[i], c = s[ixj];
+                        bool up = (i & k) == 0;
+                        if ((a > c) == up) {
+                            s[i] = c;
+                            s[ixj] = a;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        // Each thread owns a contiguous run of ceil(P/blockDim) slots.
+        const int per = (P + blockDim.x - 1) / blockDim.x;
+        const int lo = threadIdx.x * per, hi = min(lo + per, d);
+        int c = 0;
+        for (int i = lo; i < hi; i++) c += !dedup || i == 0 || s[i] != s[i - 1];
+        int total;
+        int off = block_excl_scan(c, s_warp, &total);
+        int vals[8];
+        int nv = 0;
+        for (int i = lo; i < hi; i++)
+            if (!dedup || i == 0 || s[i] != s[i - 1]) vals[nv++] = s[i];
+        __syncthreads();
+        for (int k = 0; k < nv; k++) tmp[b + off + k] = vals[k];
+        if (threadIdx.x == 0) ucnt[r] = total;
+        __syncthreads();
+    }
+}
+
+// One CTA per row longer than MED_MAX: stable LSD radix sort (8-bit digits)
+// ping-ponging between tmp and tmp2 over the row's own range, then packing
+// distinct values into tmp.  Stability within a 1024-element tile comes
+// from match_any ranks inside each warp and per-digit prefixes across warps
+// in warp order.
+__global__ void __launch_bounds__(LARGE_THREADS)
+k_sort_large(const int *__restrict__ row, const int *__restrict__ list, const unsigned *cnt,
+             int *tmp, int *tmp2, int key_bits, int dedup, int *ucnt)
+{
+    __shared__ int s_hist[256];
+    __shared__ int s_base[256];
+    __shared__ int s_tile[256];
+    __shared__ unsigned short s_wcnt[LARGE_THREADS / 32][256];
+    __shared__ int s_warp[33];
+    const int count = (int)cnt[1];
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+    for (int li = blockIdx.x; li < count; li += gridDim.x) {
+        const int r = list[li];
+        const int b = row[r], d = row[r + 1] - b;
+        int *from = tmp + b, *to = tmp2 + b;
+        for (int shift = 0; shift < key_bits; shift += 8) {
+            for (int i = threadIdx.x; i < 256; i += blockDim.x) s_hist[i] = 0;
+            __syncthreads();
+            for (int i = threadIdx.x; i < d; i += blockDim.x)
+                atomicAdd(&s_hist[((unsigned)from[i] >> shift) & 255u], 1);
+            __syncthreads();
+            if (warp == 0) {  // exclusive scan of 256 bins, 8 per lane
+                int v[8], t = 0;
+                for (int k = 0; k < 8; k++) { v[k] = s_hist[lane * 8 + k]; t += v[k]; }
+                int incl = warp_incl_scan(t);
+                int run = incl - t;
+                for (int k = 0; k < 8; k++) { s_base[lane * 8 + k] = run; run += v[k]; }
+            }
+            __syncthreads();
+            for (int t0 = 0; t0 < d; t0 += blockDim.x) {
+                const int i = t0 + threadIdx.x;
+                const bool ok = i < d;
+                const int x = ok ? from[i] : 0;
+                const int dig = ok ? (int)(((unsigned)x >> shift) & 255u) : 256;
+                for (int k = threadIdx.x; k < nwarps * 256; k += blockDim.x)
+                    s_wcnt[k >> 8][k & 255] = 0;
+                __syncthreads();
+                unsigned peers = __match_any_sync(FULL, dig);
+                int rank = __popc(peers & lanemask_lt());
+                if (ok && (int)lane == __ffs(peers) - 1) s_wcnt[warp][dig] = (unsigned short)__popc(peers);
+                __syncthreads();
+                for (int k = threadIdx.x; k < 256; k += blockDim.x) {
+                    int run = 0;
+                    for (int w = 0; w < nwarps; w++) {
+                        int c = s_wcnt[w][k];
+                        s_wcnt[w][k] = (unsigned short)run;
+                        run += c;
+                    }
+                    s_tile[k] = run;
+                }
+                __syncthreads();
+                if (ok) to[s_base[dig] + s_wcnt[warp][dig] + rank] = x;
+                __syncthreads();
+                for (int k = threadIdx.x; k < 256; k += blockDim.x) s_base[k] += s_tile[k];
+                __syncthreads();
+            }
+            int *t = from; from = to; to = t;
+        }
+        // Sorted values are in `from`; pack (distinct) values into tmp.
+        if (from == tmp + b) {
+            for (int i = threadIdx.x; i < d; i += blockDim.x) tmp2[b + i] = from[i];
+            __syncthreads();
+            from = tmp2 + b;
+        }
+        int written = 0;
+        for (int t0 = 0; t0 < d; t0 += blockDim.x) {
+            const int i = t0 + threadIdx.x;
+            const int x = i < d ? from[i] : 0;
+            const int keep = i < d && (!dedup || i == 0 || x != from[i - 1]);
+            int total;
+            int off = block_excl_scan(keep, s_warp, &total);
+            if (keep) tmp[b + written + off] = x;
+            written += total;
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) ucnt[r] = written;
+        __syncthreads();
+    }
+}
+
+// One warp per row: copy the packed distinct prefix of each row.
+__global__ void k_compact(const int *__restrict__ row, const int *__restrict__ row2, int n,
+                          const int *__restrict__ tmp, int *col)
+{
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
+        const int b = row[r], o = row2[r], c = row2[r + 1] - o;
+        for (int i = lane_id(); i < c; i += 32) col[o + i] = tmp[b + i];
+    }
+}
+
+__global__ void k_finalize(const int *__restrict__ row, int n, unsigned *zmask, int *maxdeg,
+                           unsigned long long *nonisolated)
+{
+    __shared__ unsigned long long s_red[32];
+    __shared__ int s_max[32];
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    unsigned long long mine = 0;
+    int mx = 0;
+    const int W = (n + 31) >> 5;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < (int64_t)W * 32;
+         base += stride) {
+        int64_t v = base + lane_id();
+        int d = v < n ? row[v + 1] - row[v] : 0;
+        unsigned z = __ballot_sync(FULL, d == 0);  // out-of-range bits count as zero-degree
+        if (lane_id() == 0) zmask[v >> 5] = z;
+        mine += d > 0;
+        mx = max(mx, d);
+    }
+    unsigned long long t = block_sum(mine, s_red);
+    if (threadIdx.x == 0 && t) atomicAdd(nonisolated, t);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(FULL, mx, o));
+    __syncthreads();
+    if (lane_id() == 0) s_max[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (unsigned w = 1; w < (blockDim.x >> 5); w++) mx = max(mx, s_max[w]);
+        atomicMax(maxdeg, mx);
+    }
+}
+
+__global__ void k_validate_csr(const int *__restrict__ row, const int *__restrict__ col, int n,
+                               int64_t m, int *status)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m || i < n; i += stride) {
+        if (i < n && row[i + 1] < row[i]) atomicExch(status, DEV_BAD_ID);
+        if (i < m && (unsigned)col[i] >= (unsigned)n) atomicExch(status, DEV_BAD_ID);
+    }
+}
+
+int grid_for(int64_t work, int threads, int cap = 152 * 16)
+{
+    int64_t g = (work + threads - 1) / threads;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(g, cap));
+}
+
+struct Scratch {
+    void *p = nullptr;
+    ~Scratch() { if (p) cudaFree(p); }
+};
+
+int finalize(DeviceCsr &out, cudaStream_t st, std::string &err)
+{
+    int rc = GBFS_OK;
+    struct Res { unsigned long long nonisolated; int maxdeg; int pad; } h{};
+    Res *d_res = nullptr;
+    const int W = (out.n + 31) / 32;
+    CK(cudaMalloc(&out.zmask, sizeof(unsigned) * (size_t)W));
+    CK(cudaMalloc(&d_res, sizeof(Res)));
+    CK(cudaMemsetAsync(d_res, 0, sizeof(Res), st));
+    k_finalize<<<grid_for((int64_t)W * 32, 256), 256, 0, st>>>(out.row, out.n, out.zmask,
+                                                                &d_res->maxdeg, &d_res->nonisolated);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(&h, d_res, sizeof(Res), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    out.max_degree = h.maxdeg;
+    out.nonisolated = (int64_t)h.nonisolated;
+done:
+    if (d_res) cudaFree(d_res);
+    return rc;
+}
+
+}  // namespace
+
+void csr_free(DeviceCsr &c)
+{
+    if (c.row) cudaFree(c.row);
+    if (c.col) cudaFree(c.col);
+    if (c.zmask) cudaFree(c.zmask);
+    c = DeviceCsr{};
+}
+
+int csr_build_from_edges(int32_t n, int64_t m, const int *d_src, const int *d_dst, unsigned flags,
+                         cudaStream_t st, DeviceCsr &out, std::string &err)
+{
+    int rc = GBFS_OK;
+    const bool sym = flags & GBFS_SYMMETRIZE, dedup = flags & GBFS_DEDUP;
+    int *deg = nullptr, *cursor = nullptr, *tmp = nullptr, *tmp2 = nullptr, *ucnt = nullptr;
+    int *med = nullptr, *large = nullptr, *row2 = nullptr;
+    unsigned *lcnt = nullptr;
+    int *status = nullptr;
+    unsigned long long *total = nullptr;
+    void *scan_mem = nullptr;
+    ScanScratch ss;
+    unsigned long long h_total = 0;
+    int h_status = 0;
+    int64_t md = 0;
+    int key_bits = 1;
+    const int thr = 256;
+    out = DeviceCsr{};
+    out.n = n;
+
+    // Scratch for both scans (n+1 elements at most).
+    const int64_t tiles = scan_tiles((int64_t)n + 1);
+    CK(cudaMalloc(&scan_mem, scan_scratch_bytes(tiles)));
+    CK(cudaMemsetAsync(scan_mem, 0, scan_scratch_bytes(tiles), st));
+    scan_scratch_carve(scan_mem, tiles, ss);
+
+    CK(cudaMalloc(&deg, sizeof(int) * ((size_t)n + 1)));
+    CK(cudaMalloc(&status, 64));
+    total = (unsigned long long *)(status + 2);
+    lcnt = (unsigned *)(status + 4);
+    CK(cudaMemsetAsync(deg, 0, sizeof(int) * ((size_t)n + 1), st));
+    CK(cudaMemsetAsync(status, 0, 64, st));
+    if (m > 0) {
+        k_count<<<grid_for(m, thr), thr, 0, st>>>(d_src, d_dst, m, n, flags, deg, total, status);
+        CK(cudaGetLastError());
+    }
+    CK(cudaMemcpyAsync(&h_total, total, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&h_status, status, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (h_status != DEV_OK) {
+        err = "edge endpoint outside [0, n)";
+        rc = GBFS_ERR_INVALID_ARG;
+        goto done;
+    }
+    if (h_total > (unsigned long long)INT32_MAX) {
+        err = "more than 2^31-1 directed edges";
+        rc = GBFS_ERR_TOO_LARGE;
+        goto done;
+    }
+    md = (int64_t)h_total;
+
+    CK(cudaMalloc(&out.row, sizeof(int) * ((size_t)n + 1)));
+    CK(scan_exclusive_i32_i32(deg, out.row, n, out.row + n, ss, st));
+    CK(cudaMalloc(&cursor, sizeof(int) * ((size_t)n + 1)));
+    CK(cudaMemcpyAsync(cursor, out.row, sizeof(int) * ((size_t)n + 1), cudaMemcpyDeviceToDevice, st));
+    CK(cudaMalloc(&tmp, sizeof(int) * (size_t)std::max<int64_t>(md, 1)));
+    if (m > 0) {
+        k_scatter<<<grid_for(m, thr), thr, 0, st>>>(d_src, d_dst, m, n, flags, cursor, tmp);
+        CK(cudaGetLastError());
+    }
+    cudaFree(cursor);
+    cursor = nullptr;
+    cudaFree(deg);
+    deg = nullptr;
+
+    // Per-row sort (+ distinct count).
+    CK(cudaMalloc(&ucnt, sizeof(int) * ((size_t)n + 1)));
+    CK(cudaMalloc(&med, sizeof(int) * (size_t)n));
+    CK(cudaMalloc(&large, sizeof(int) * (size_t)n));
+    k_bin<<<grid_for(n, BIN_THREADS, 152 * 4), BIN_THREADS, 0, st>>>(out.row, n, med, large, lcnt);
+    CK(cudaGetLastError());
+    k_sort_small<<<grid_for((int64_t)n * 32, thr), thr, 0, st>>>(out.row, n, tmp, dedup, ucnt);
+    CK(cudaGetLastError());
+    k_sort_medium<<<152 * 4, MED_THREADS, 0, st>>>(out.row, med, lcnt, tmp, dedup, ucnt);
+    CK(cudaGetLastError());
+    while (key_bits < 31 && (1LL << key_bits) < (int64_t)n) key_bits++;
+    CK(cudaMalloc(&tmp2, sizeof(int) * (size_t)std::max<int64_t>(md, 1)));
+    k_sort_large<<<152 * 2, LARGE_THREADS, 0, st>>>(out.row, large, lcnt, tmp, tmp2, key_bits, dedup,
+                                                    ucnt);
+    CK(cudaGetLastError());
+
+    if (dedup) {
+        int h_m2 = 0;
+        CK(cudaMalloc(&row2, sizeof(int) * ((size_t)n + 1)));
+        CK(scan_exclusive_i32_i32(ucnt, row2, n, row2 + n, ss, st));
+        CK(cudaMemcpyAsync(&h_m2, row2 + n, 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        CK(cudaMalloc(&out.col, sizeof(int) * (size_t)std::max(h_m2, 1)));
+        k_compact<<<grid_for((int64_t)n * 32, thr), thr, 0, st>>>(out.row, row2, n, tmp, out.col);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(st));
+        cudaFree(out.row);
+        out.row = row2;
+        row2 = nullptr;
+        out.m = h_m2;
+    } else {
+        out.col = tmp;
+        tmp = nullptr;
+        out.m = md;
+    }
+    {
+        unsigned h_scan_status[3] = {0, 0, 0};
+        CK(cudaMemcpyAsync(h_scan_status, ss.ctl, 12, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (h_scan_status[2] != 0) {
+            err = "scan look-back timed out";
+            rc = GBFS_ERR_TIMEOUT;
+            goto done;
+        }
+    }
+    rc = finalize(out, st, err);
+
+done:
+    if (deg) cudaFree(deg);
+    if (cursor) cudaFree(cursor);
+    if (tmp) cudaFree(tmp);
+    if (tmp2) cudaFree(tmp2);
+    if (ucnt) cudaFree(ucnt);
+    if (med) cudaFree(med);
+    if (large) cudaFree(large);
+    if (row2) cudaFree(row2);
+    if (status) cudaFree(status);
+    if (scan_mem) cudaFree(scan_mem);
+    if (rc != GBFS_OK) csr_free(out);
+    return rc;
+}
+
+int csr_adopt(int32_t n, int64_t m, int *d_row, int *d_col, cudaStream_t st, DeviceCsr &out,
+              std::string &err)
+{
+    int rc = GBFS_OK;
+    int *status = nullptr;
+    int h[2] = {0, 0};
+    int h_status = 0;
+    out = DeviceCsr{};
+    out.n = n;
+    out.m = m;
+    out.row = d_row;
+    out.col = d_col;
+    CK(cudaMalloc(&status, sizeof(int)));
+    CK(cudaMemsetAsync(status, 0, sizeof(int), st));
+    k_validate_csr<<<grid_for(std::max<int64_t>(m, n), 256), 256, 0, st>>>(d_row, d_col, n, m, status);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(&h[0], d_row, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&h[1], d_row + n, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&h_status, status, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (h[0] != 0 || (int64_t)h[1] != m || h_status != DEV_OK) {
+        err = "CSR is not well formed (row_offset[0]==0, non-decreasing, row_offset[n]==m, "
+              "col ids in [0, n))";
+        rc = GBFS_ERR_INVALID_ARG;
+        goto done;
+    }
+    rc = finalize(out, st, err);
+done:
+    if (status) cudaFree(status);
+    if (rc != GBFS_OK) csr_free(out);
+    return rc;
+}
+
+}  // namespace gbfs

@@ -1,0 +1,36 @@
+// csr_build.cuh -- on-device edge list -> CSR builder.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+namespace gbfs {
+
+// A CSR resident in HBM.  Rows of graphs built from edges are sorted
+// ascending.  zmask bit v is set when out-degree(v) == 0.
+struct DeviceCsr {
+    int32_t n = 0;
+    int64_t m = 0;
+    int *row = nullptr;        // n+1
+    int *col = nullptr;        // m
+    unsigned *zmask = nullptr; // (n+31)/32
+    int32_t max_degree = 0;
+    int64_t nonisolated = 0;
+};
+
+// Build from device edge arrays (m entries each).  Returns a GBFS_* status;
+// on failure `err` says why.  All work is ordered on `st`; the call
+// synchronises `st` before returning.
+int csr_build_from_edges(int32_t n, int64_t m, const int *d_src, const int *d_dst,
+                         unsigned flags, cudaStream_t st, DeviceCsr &out, std::string &err);
+
+// Take an existing device CSR (row n+1, col m; ownership moves to `out`),
+// validate it and compute zmask / max_degree / nonisolated.
+int csr_adopt(int32_t n, int64_t m, int *d_row, int *d_col, cudaStream_t st, DeviceCsr &out,
+              std::string &err);
+
+void csr_free(DeviceCsr &c);
+
+}  // namespace gbfs

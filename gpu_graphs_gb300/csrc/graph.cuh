@@ -1,0 +1,50 @@
+// graph.cuh -- the opaque handle types behind the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "bfs.cuh"
+#include "csr_build.cuh"
+#include "msbfs.cuh"
+
+struct gbfs_graphset;
+
+struct gbfs_graph {
+    gbfs::DeviceCsr csr;
+    gbfs_params params{};
+    gbfs::BfsWork work;
+    gbfs::MsWork ms;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    bool symmetric = false;      // in-edges == out-edges (bottom-up allowed)
+    std::mutex mu;
+    // graph set cached by gbfs_bfs_batch_graphs (keyed by the handle list)
+    std::vector<const gbfs_graph *> batch_key;
+    gbfs_graphset *batch_set = nullptr;
+};
+
+struct gbfs_graphset {
+    gbfs_graph *g = nullptr;           // the disjoint union
+    std::vector<int64_t> offsets;      // count+1 vertex offsets
+    std::vector<int32_t> sizes;        // n of each member
+};
+
+namespace gbfs {
+
+// thread-local error detail
+void set_error(const std::string &msg);
+int fail(int code, const std::string &msg);
+bool is_device_ptr(const void *p);
+int cuda_fail(cudaError_t e, const char *what);
+
+// Make a handle around a built CSR (takes ownership of csr).
+int graph_wrap(DeviceCsr &csr, bool symmetric_known, bool symmetric, cudaStream_t st,
+               gbfs_graph **out);
+
+}  // namespace gbfs

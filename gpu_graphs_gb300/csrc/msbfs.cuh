@@ -1,0 +1,53 @@
+// msbfs.cuh -- 64-lane multi-source BFS (host side of msbfs.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "common.cuh"
+#include "csr_build.cuh"
+
+namespace gbfs {
+
+constexpr int MS_LANES = 64;
+
+struct MsCtrl {
+    GridBarrier bar;
+    int status;
+    int pad0;
+    unsigned long long cnt[3];   // vertices that gained a lane, rotating by level
+    int levels, push_levels, pull_levels, pad1;
+    unsigned long long reached, edges_c;
+};
+
+struct MsWork {
+    int32_t n = 0;
+    unsigned long long *vis = nullptr;   // n lane masks: lanes that reached v
+    unsigned long long *cur = nullptr;   // n lane masks: v in the lane's frontier
+    unsigned long long *nxt = nullptr;   // n lane masks: next frontier
+    int *out = nullptr;                  // MS_LANES * n levels (host-bound results)
+    int *src = nullptr;                  // MS_LANES sources
+    MsCtrl *ctrl = nullptr;
+    MsCtrl *h_ctrl = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int64_t bytes = 0;
+};
+
+int ms_work_alloc(MsWork &w, int32_t n, std::string &err);
+void ms_work_free(MsWork &w);
+
+struct MsResult {
+    float ms = 0;
+    int levels = 0, push_levels = 0, pull_levels = 0;
+    int64_t reached = 0, edges_c = 0;
+};
+
+// k <= 64 sources (device array d_src); d_out: k*n int32, row i = levels of
+// source i.  pull_allowed: the graph is symmetric.  Synchronises `st`.
+int msbfs_run(const DeviceCsr &g, const gbfs_params &p, bool pull_allowed, MsWork &w,
+              const int *d_src, int k, int *d_out, cudaStream_t st, MsResult &res,
+              std::string &err);
+
+}  // namespace gbfs

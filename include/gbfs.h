@@ -1,0 +1,270 @@
+/*
+ * gbfs.h -- C ABI of the GB300-native BFS engine (libgbfs.so).
+ *
+ * The engine keeps the reference's graphBFS host path -- edge list in, CSR
+ * build, BFS from a source, per-vertex int32 level array out (-1 =
+ * unreachable) -- on one GPU, behind plain C entry points: pointers, sizes
+ * and status codes, no C++ or torch types.  Every call returns GBFS_OK (0)
+ * or a negative status; the library never exits the process.
+ *
+ * Reference interfaces replaced (paths relative to the YKMorsy/GPU_Graphs
+ * project root):
+ *   csr::csr(const char*)          1D Partition/include/csr.h:9-23,
+ *                                  1D Partition/src/csr.cpp:3-67
+ *   csc::csc(const char*, R, C)    2D Partition/include/csc.h:12-25,
+ *                                  2D Partition/src/csc.cpp:3-94
+ *   gpuBFS::gpuBFS(csr&, int)      1D Partition/include/gpuBFS.cuh:9-54,
+ *                                  1D Partition/src/gpuBFS.cu:13-116
+ *   gpuBFS::gpuBFS(csc&, int,R,C)  2D Partition/include/gpuBFS.cuh:12-63,
+ *                                  2D Partition/src/gpuBFS.cu:189-345
+ *   PrefixSum::sum_scan_blelloch   2D Partition/include/prefixSum.cuh:4-10
+ *
+ * Pointers marked "host or device" are classified with
+ * cudaPointerGetAttributes; device pointers must be on the current device.
+ * Thread safety: calls on one graph handle are serialised by a per-graph
+ * lock; different handles may be used from different threads at once.
+ */
+#ifndef GBFS_H
+#define GBFS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define GBFS_OK                0
+#define GBFS_ERR_INVALID_ARG  -1  /* bad pointer, size, id or source        */
+#define GBFS_ERR_OOM          -2  /* device or host allocation failed       */
+#define GBFS_ERR_CUDA         -3  /* a CUDA runtime call failed / no device */
+#define GBFS_ERR_TIMEOUT      -4  /* a bounded device-side wait ran out     */
+#define GBFS_ERR_TOO_LARGE    -5  /* graph exceeds the int32 CSR limits     */
+#define GBFS_ERR_IO           -6  /* file missing or malformed              */
+#define GBFS_ERR_BUDGET       -7  /* serving: memory budget refuses it      */
+#define GBFS_ERR_NOT_FOUND    -8  /* serving: unknown graph id or ticket    */
+#define GBFS_ERR_SHUTDOWN     -9  /* serving: server is shutting down       */
+
+/* Text for a status code (static storage). */
+const char *gbfs_strerror(int status);
+/* Detail message of the last failing call on this thread ("" if none). */
+const char *gbfs_last_error(void);
+/* Library version string. */
+const char *gbfs_version(void);
+
+/* ---- graph construction ---------------------------------------------- */
+/* Build flags.  With 0 the CSR keeps the edges as stored, like the
+ * reference loaders (directed, duplicates and self-loops kept). */
+#define GBFS_SYMMETRIZE       1u  /* add (v,u) for every (u,v)              */
+#define GBFS_DEDUP            2u  /* drop repeated (u,v)                     */
+#define GBFS_DROP_SELF_LOOPS  4u  /* drop (u,u)                              */
+#define GBFS_UNDIRECTED (GBFS_SYMMETRIZE | GBFS_DEDUP | GBFS_DROP_SELF_LOOPS)
+
+typedef struct gbfs_graph gbfs_graph;
+
+/*
+ * Edge list -> device CSR, built on the GPU (degree count, look-back scan,
+ * scatter, per-row sort, dedup, compaction).  Rows come out sorted
+ * ascending.  src/dst: m int32 vertex ids in [0, n), host or device.
+ * Replaces csr::csr / csc::csc (which parse a file into host CSR; the file
+ * parser is gbfs_read_edge_list below).  Limits: n <= 2^31-2, stored
+ * directed edges <= 2^31-1 (GBFS_ERR_TOO_LARGE otherwise).
+ */
+int gbfs_graph_from_edges(int32_t n, int64_t m, const int32_t *src,
+                          const int32_t *dst, uint32_t flags,
+                          gbfs_graph **out);
+
+/*
+ * Existing CSR -> device graph, taken as is (rows need not be sorted).
+ * row_offset: n+1 int32 (row_offset[0]==0, non-decreasing, [n]==m);
+ * col_idx: m int32 in [0, n).  Host or device.  Mirrors the public
+ * int* row_offset / int* col_idx of csr (1D Partition/include/csr.h:15-16).
+ */
+int gbfs_graph_from_csr(int32_t n, int64_t m, const int32_t *row_offset,
+                        const int32_t *col_idx, gbfs_graph **out);
+
+void gbfs_graph_destroy(gbfs_graph *g);
+
+typedef struct gbfs_graph_info {
+    int32_t n;                  /* vertices                                  */
+    int32_t max_degree;
+    int64_t m;                  /* stored directed edges                     */
+    int64_t nonisolated;        /* vertices with out-degree > 0              */
+    int64_t device_bytes;       /* CSR + per-graph search workspace          */
+} gbfs_graph_info;
+
+int gbfs_graph_get_info(const gbfs_graph *g, gbfs_graph_info *info);
+
+/* Copy the device CSR out: row_offset n+1, col_idx m (host or device). */
+int gbfs_graph_get_csr(const gbfs_graph *g, int32_t *row_offset,
+                       int32_t *col_idx);
+
+/* ---- traversal parameters (autotuned) --------------------------------- */
+#define GBFS_DIR_OPTIMIZING   0   /* Beamer top-down / bottom-up switching  */
+#define GBFS_DIR_TOPDOWN      1
+#define GBFS_DIR_BOTTOMUP     2
+
+typedef struct gbfs_params {
+    int32_t threads_per_block;  /* 256, 512 or 1024                         */
+    int32_t blocks_per_sm;      /* persistent CTAs per SM (capped by occupancy) */
+    int32_t alpha;              /* TD->BU when frontier edges > unexplored/alpha */
+    int32_t beta;               /* BU->TD when frontier vertices < n/beta    */
+    int32_t big_degree;         /* TD rows >= this are split across the grid */
+    int32_t direction;          /* GBFS_DIR_*                               */
+    int32_t per_level_launch;   /* 1: one launch per level with a host loop
+                                   (the reference's shape), 0: persistent   */
+    int32_t timeout_ms;         /* bound on every device-side wait          */
+} gbfs_params;
+
+/* Built-in defaults (before any autotuning). */
+int gbfs_default_params(gbfs_params *p);
+int gbfs_get_params(const gbfs_graph *g, gbfs_params *p);
+int gbfs_set_params(gbfs_graph *g, const gbfs_params *p);
+
+/*
+ * Autotuner: times a grid of candidate parameters (block size, CTAs per SM,
+ * alpha, beta, big_degree) on `nsources` sources of this graph, keeps the
+ * fastest whose levels equal the default's, stores it in the graph and
+ * returns it in *best (nullable).  A process-wide cache keyed by the
+ * graph's size/degree signature makes repeated calls cheap.
+ */
+int gbfs_autotune(gbfs_graph *g, const int32_t *sources, int32_t nsources,
+                  gbfs_params *best);
+
+/* ---- single-source BFS ------------------------------------------------ */
+typedef struct gbfs_stats {
+    float   ms;                 /* device time of the traversal (events)    */
+    int32_t levels;             /* number of BFS levels (max level + 1)     */
+    int32_t td_levels;          /* levels expanded top-down                 */
+    int32_t bu_levels;          /* levels expanded bottom-up                */
+    int32_t launches;           /* kernel launches this call made           */
+    int64_t vertices_reached;   /* vertices with level >= 0 (all sources)   */
+    int64_t edges_in_component; /* out-edges of reached vertices (E_c)      */
+    int64_t edges_traversed;    /* reference convention: discovered vertices
+                                   (2D Partition/src/cpuBFS.cpp:59)         */
+} gbfs_stats;
+
+/*
+ * BFS from `source`; levels_out receives n int32 (host or device), -1 for
+ * unreachable.  Replaces gpuBFS::gpuBFS(csr&, int) and its host_distance /
+ * exec_time / total_edges_traversed / iteration members.  stats nullable.
+ */
+int gbfs_bfs(gbfs_graph *g, int32_t source, int32_t *levels_out,
+             gbfs_stats *stats);
+
+/*
+ * k single-source searches run back to back, one launch each, queued on the
+ * graph's stream with no host round trip in between (the plain
+ * one-query-per-launch BFS).  levels_out: k*n int32 (host or device; row i
+ * for sources[i]) or NULL to discard the levels.  stats: k entries
+ * (nullable); stats[i].ms spans launch i (and its D2H copy when levels_out
+ * is on the host).
+ */
+int gbfs_bfs_many(gbfs_graph *g, const int32_t *sources, int32_t k,
+                  int32_t *levels_out, gbfs_stats *stats);
+
+/* The CUDA stream (cudaStream_t) the graph's work is ordered on, for
+ * callers that record their own events around it. */
+void *gbfs_graph_stream(const gbfs_graph *g);
+
+/*
+ * Multi-root BFS: every vertex in sources[0..k) starts at level 0 and a
+ * vertex's level is its distance to the nearest root.  levels_out: n int32.
+ */
+int gbfs_bfs_multiroot(gbfs_graph *g, const int32_t *sources, int32_t k,
+                       int32_t *levels_out, gbfs_stats *stats);
+
+/*
+ * Multi-source BFS: k independent searches on one graph, 64 per launch in
+ * uint64 per-vertex lane masks.  levels_out: k*n int32, row i = the level
+ * array of sources[i].  stats (nullable) sums over all searches.
+ */
+int gbfs_bfs_multi(gbfs_graph *g, const int32_t *sources, int32_t k,
+                   int32_t *levels_out, gbfs_stats *stats);
+
+/* ---- many small graphs, one fused launch ------------------------------ */
+typedef struct gbfs_graphset gbfs_graphset;
+
+/*
+ * `count` edge lists -> one device graph set (the disjoint union in one CSR
+ * plus a per-graph vertex offset table).  n[i], m[i], src[i], dst[i] as in
+ * gbfs_graph_from_edges; ids are local to each graph.
+ */
+int gbfs_graphset_from_edges(int32_t count, const int32_t *n,
+                             const int64_t *m, const int32_t *const *src,
+                             const int32_t *const *dst, uint32_t flags,
+                             gbfs_graphset **out);
+/* Same, from graphs already on the device (their CSRs are copied). */
+int gbfs_graphset_from_graphs(int32_t count, gbfs_graph *const *graphs,
+                              gbfs_graphset **out);
+void gbfs_graphset_destroy(gbfs_graphset *s);
+int gbfs_graphset_vertex_offsets(const gbfs_graphset *s, int64_t *offsets);
+
+/*
+ * One BFS per graph (sources[i] local to graph i), all in one persistent
+ * launch.  levels_out[i]: n[i] int32 (host or device).
+ */
+int gbfs_bfs_batch(gbfs_graphset *s, const int32_t *sources,
+                   int32_t *const *levels_out, gbfs_stats *stats);
+
+/* Convenience over separate handles: builds (and caches on the first
+ * handle) a graph set, then runs gbfs_bfs_batch. */
+int gbfs_bfs_batch_graphs(gbfs_graph *const *graphs, const int32_t *sources,
+                          int32_t count, int32_t *const *levels_out,
+                          gbfs_stats *stats);
+
+/* ---- scan primitive ---------------------------------------------------- */
+/*
+ * Exclusive prefix sum of n int32 on the device (single-pass decoupled
+ * look-back), 64-bit output.  d_in, d_out device pointers; stream may be
+ * NULL (legacy default stream).  Replaces PrefixSum::sum_scan_blelloch
+ * (2D Partition/src/prefixSum.cu:136-224), which allocates and frees its
+ * scratch on every call; this one keeps a per-device scratch pool.
+ */
+int gbfs_exclusive_scan_i32(const int32_t *d_in, int64_t *d_out, int64_t n,
+                            void *stream);
+
+/* ---- file format and workload generators ------------------------------ */
+/*
+ * Read the reference's text format: "n", "m", then whitespace-separated
+ * "from to" pairs until end of file (1D Partition/src/csr.cpp:14-29,
+ * 2D Partition/src/csc.cpp:14-25).  one_based=1 subtracts 1 from every id
+ * like csc.cpp:24.  *src / *dst are malloc'd; free with gbfs_free.
+ * Ids outside [0, n) are an error (the reference writes out of bounds).
+ */
+int gbfs_read_edge_list(const char *path, int32_t one_based, int32_t *n,
+                        int64_t *m, int32_t **src, int32_t **dst);
+void gbfs_free(void *p);
+
+/* Binary CSR cache: int32 n, int64 m, int32 row_offset[n+1], int32 col[m]. */
+int gbfs_graph_save(const gbfs_graph *g, const char *path);
+int gbfs_graph_load(const char *path, gbfs_graph **out);
+
+/*
+ * Seeded, thread-count-independent workload generators (host).  Each
+ * returns the number of edges written, or a negative status if `cap` is too
+ * small.  Edges are undirected pairs, to be built with GBFS_UNDIRECTED.
+ *   er:   `pairs` uniform (u,v) pairs over n vertices
+ *   rmat: 2^scale vertices, edge_factor*2^scale edges, quadrant
+ *         probabilities a,b,c (d = 1-a-b-c), ids permuted by the seed
+ *   grid: side x side 4-neighbour grid (row-major ids), each edge dropped
+ *         with probability drop, plus round(extra * 2*side*(side-1)) edges
+ *         from a uniform vertex to a uniform vertex within Manhattan radius
+ *         `radius` (a draw that finds no in-grid target in 64 tries becomes
+ *         a self-loop, removed by GBFS_DROP_SELF_LOOPS)
+ */
+int64_t gbfs_gen_er(int32_t n, int64_t pairs, uint64_t seed, int32_t *src,
+                    int32_t *dst, int64_t cap);
+int64_t gbfs_gen_rmat(int32_t scale, int32_t edge_factor, double a, double b,
+                      double c, uint64_t seed, int32_t *src, int32_t *dst,
+                      int64_t cap);
+int64_t gbfs_gen_grid(int32_t side, double drop, double extra, int32_t radius,
+                      uint64_t seed, int32_t *src, int32_t *dst, int64_t cap);
+/* Upper bound of gbfs_gen_grid's edge count for the same arguments. */
+int64_t gbfs_gen_grid_capacity(int32_t side, double extra);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBFS_H */

@@ -1,0 +1,111 @@
+"""C-ABI surface and host-side logic of libgbfs.so (CPU only: no kernel runs)."""
+from __future__ import annotations
+
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, load_golden
+
+HEADERS = sorted((ROOT / "include").glob("*.h"))
+
+
+def declared_functions() -> set[str]:
+    names = set()
+    for h in HEADERS:
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w\s\*]*?\b(gbfs_\w+)\s*\(", text, flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_function(gb):
+    lib = C.CDLL(gb.library_path())
+    names = declared_functions()
+    assert len(names) > 20
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, f"declared in include/*.h but not exported: {missing}"
+
+
+def test_status_strings(gb):
+    lib = gb._lib.lib
+    for code in range(0, -10, -1):
+        s = lib.gbfs_strerror(code).decode()
+        assert s and s != "unknown status"
+    assert lib.gbfs_strerror(-999).decode() == "unknown status"
+    assert b"sm_103a" in lib.gbfs_version()
+
+
+def test_params_validation(gb):
+    p = gb.default_params()
+    assert p.threads_per_block in (256, 512, 1024) and p.alpha >= 1 and p.beta >= 1
+    lib = gb._lib.lib
+    assert lib.gbfs_set_params(None, C.byref(p)) == gb._lib.ERR_INVALID_ARG
+    assert lib.gbfs_default_params(None) == gb._lib.ERR_INVALID_ARG
+
+
+def test_null_and_range_arguments(gb):
+    lib = gb._lib.lib
+    h = C.c_void_p()
+    assert lib.gbfs_graph_from_edges(0, 0, None, None, 0, C.byref(h)) == gb._lib.ERR_INVALID_ARG
+    assert lib.gbfs_graph_from_edges(5, 3, None, None, 0, C.byref(h)) == gb._lib.ERR_INVALID_ARG
+    assert lib.gbfs_graph_from_edges(5, 0, None, None, 8, C.byref(h)) == gb._lib.ERR_INVALID_ARG
+    assert lib.gbfs_bfs(None, 0, None, None) == gb._lib.ERR_INVALID_ARG
+    assert lib.gbfs_graph_get_info(None, None) == gb._lib.ERR_INVALID_ARG
+    assert lib.gbfs_exclusive_scan_i32(None, None, -1, None) == gb._lib.ERR_INVALID_ARG
+
+
+def test_generators_are_deterministic(gb):
+    a = gb.gen_rmat(12, 16, seed=9)
+    b = gb.gen_rmat(12, 16, seed=9)
+    c = gb.gen_rmat(12, 16, seed=10)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert not np.array_equal(a[0], c[0])
+    assert len(a[0]) == 16 << 12 and a[0].max() < 4096 and a[0].min() >= 0
+    s, d = gb.gen_er(1000, 5000, 3)
+    assert len(s) == 5000 and s.max() < 1000 and d.max() < 1000
+    s, d = gb.gen_grid(50, 0.1, 0.001, 8, 4)
+    cap = 2 * 50 * 49 + round(0.001 * 2 * 50 * 49)
+    assert len(s) <= cap and s.max() < 2500
+    # grid edges join 4-neighbours; extra edges stay within Manhattan radius 8
+    r, c = np.divmod(s, 50)
+    r2, c2 = np.divmod(d, 50)
+    dist = np.abs(r - r2) + np.abs(c - c2)
+    assert (dist <= 8).all()
+    assert (dist == 1).mean() > 0.95
+
+
+def test_rmat_skew(gb):
+    s, d = gb.gen_rmat(14, 16, seed=1)
+    deg = np.bincount(np.concatenate([s, d]), minlength=1 << 14)
+    # a power-law-ish degree distribution: hubs far above the mean, many isolated
+    assert deg.max() > 40 * deg.mean()
+    assert (deg == 0).mean() > 0.1
+
+
+def test_read_edge_list(gb, tmp_path):
+    d = load_golden("ref_tree")
+    p = tmp_path / "tree.txt"
+    lines = [str(int(d["n"])), str(len(d["src"]))] + [f"{a + 1}   {b + 1}" for a, b in zip(d["src"], d["dst"])]
+    p.write_text("\n".join(lines))
+    n, s, t = gb.read_edge_list(str(p))
+    assert n == int(d["n"]) and np.array_equal(s, d["src"]) and np.array_equal(t, d["dst"])
+    n0, s0, _ = gb.read_edge_list(str(p), one_based=False)
+    assert np.array_equal(s0, d["src"] + 1)
+    with pytest.raises(gb.GbfsError) as e:
+        gb.read_edge_list(str(tmp_path / "missing.txt"))
+    assert e.value.code == gb._lib.ERR_IO
+    bad = tmp_path / "bad.txt"
+    bad.write_text("3\n1\n1 9\n")
+    with pytest.raises(gb.GbfsError) as e:
+        gb.read_edge_list(str(bad))
+    assert e.value.code == gb._lib.ERR_IO
+
+
+def test_csr_mirror_reports_missing_file(gb, tmp_path, capsys):
+    with pytest.raises(gb.GbfsError):
+        gb.csr(str(tmp_path / "nope.txt"))
+    assert "Error: Unable to open file" in capsys.readouterr().err

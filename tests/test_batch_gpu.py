@@ -1,0 +1,103 @@
+"""GPU parity: 64-lane multi-source BFS, fused many-graph launches, scan."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("k", [1, 5, 64, 100])
+def test_multi_source_matches_single(gb, orc, k):
+    n = 1 << 16
+    src, dst = gb.gen_rmat(16, 16, seed=12)
+    o = orc.csr_build(n, src, dst, orc.UNDIRECTED)
+    g = gb.Graph.from_edges(n, src, dst)
+    deg = np.diff(o.row_offset)
+    rng = np.random.default_rng(k)
+    sources = rng.choice(np.flatnonzero(deg > 0), k, replace=True)
+    sources[0] = 0 if deg[0] == 0 else sources[0]  # an isolated source when vertex 0 is one
+    got, st = g.bfs_multi(sources, stats=True)
+    reached = 0
+    for i, s in enumerate(sources):
+        want = orc.bfs_queue(o, int(s))
+        assert np.array_equal(got[i], want), (i, int(s))
+        reached += int((want >= 0).sum())
+    assert st.vertices_reached == reached
+    assert st.launches == (k + 63) // 64
+
+
+@pytest.mark.parametrize("direction", [0, 1, 2])
+def test_multi_source_directions_and_directed(gb, orc, direction):
+    n = 20000
+    src, dst = gb.gen_er(n, 60000, seed=13)
+    for flags in (gb.UNDIRECTED, 0):
+        o = orc.csr_build(n, src, dst, flags)
+        g = gb.Graph.from_edges(n, src, dst, flags)
+        g.set_params(direction=direction)
+        sources = list(range(0, 64 * 7, 7))
+        got = g.bfs_multi(sources)
+        for i, s in enumerate(sources):
+            assert np.array_equal(got[i], orc.bfs_queue(o, s))
+
+
+def test_multi_source_grid(gb, orc):
+    side = 200
+    src, dst = gb.gen_grid(side, 0.1, 0.001, 8, seed=14)
+    n = side * side
+    o = orc.csr_build(n, src, dst, orc.UNDIRECTED)
+    g = gb.Graph.from_edges(n, src, dst)
+    sources = [0, n - 1, n // 2, 12345] * 8
+    got = g.bfs_multi(sources)
+    for i, s in enumerate(sources):
+        assert np.array_equal(got[i], orc.bfs_queue(o, s))
+
+
+def _small_graphs(gb, count, seed):
+    rng = np.random.default_rng(seed)
+    graphs = []
+    for i in range(count):
+        n = int(np.exp(rng.uniform(np.log(8), np.log(4096))))
+        s, d = gb.gen_er(n, 4 * n, seed * 1000 + i)
+        graphs.append((n, s, d))
+    return graphs
+
+
+def test_graph_set_fused_launch(gb, orc):
+    graphs = _small_graphs(gb, 60, 1)
+    gs = gb.GraphSet.from_edges(graphs)
+    rng = np.random.default_rng(2)
+    sources = [int(rng.integers(0, n)) for n, _, _ in graphs]
+    outs, st = gs.bfs(sources, stats=True)
+    assert st.launches == 1
+    for (n, s, d), src, got in zip(graphs, sources, outs):
+        o = orc.csr_build(n, s, d, orc.UNDIRECTED)
+        assert np.array_equal(got, orc.bfs_queue(o, src))
+
+
+def test_batch_over_handles(gb, orc):
+    graphs = _small_graphs(gb, 12, 3)
+    handles = [gb.Graph.from_edges(n, s, d) for n, s, d in graphs]
+    sources = [0] * len(graphs)
+    from gpu_graphs_gb300 import bfs_batch_graphs
+    for _ in range(2):  # second call reuses the cached union
+        outs = bfs_batch_graphs(handles, sources)
+        for (n, s, d), got in zip(graphs, outs):
+            o = orc.csr_build(n, s, d, orc.UNDIRECTED)
+            assert np.array_equal(got, orc.bfs_queue(o, 0))
+    gs = gb.GraphSet.from_graphs(handles)
+    outs = gs.bfs(sources)
+    for (n, s, d), got in zip(graphs, outs):
+        o = orc.csr_build(n, s, d, orc.UNDIRECTED)
+        assert np.array_equal(got, orc.bfs_queue(o, 0))
+
+
+@pytest.mark.parametrize("n", [1, 2047, 2048, 2049, 1000003, 20000000])
+def test_exclusive_scan(gb, orc, n):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(n)
+    x = rng.integers(-1000, 100000, size=n, dtype=np.int32)
+    got = gb.exclusive_scan(torch.from_numpy(x).cuda()).cpu().numpy()
+    assert np.array_equal(got, orc.exclusive_scan(x))
+    got2 = gb.exclusive_scan(torch.from_numpy(x).cuda()).cpu().numpy()  # scratch reuse
+    assert np.array_equal(got2, got)

@@ -1,0 +1,202 @@
+"""GPU parity: CSR build and single-source / multi-root BFS against the oracle.
+
+Every level array must equal the oracle's (which is pinned to the
+reference's own CPU BFS by tests/test_oracle.py) bit for bit, including -1
+for unreachable and isolated vertices.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden, synthetic_edges
+
+pytestmark = pytest.mark.gpu
+
+MODES = {"opt": 0, "td": 1, "bu": 2}
+
+
+def sorted_rows_equal(row_a, col_a, row_b, col_b) -> bool:
+    if not np.array_equal(np.asarray(row_a, np.int64), np.asarray(row_b, np.int64)):
+        return False
+    for r in range(len(row_a) - 1):
+        a = np.sort(col_a[row_a[r]:row_a[r + 1]])
+        b = np.sort(col_b[row_b[r]:row_b[r + 1]])
+        if not np.array_equal(a, b):
+            return False
+    return True
+
+
+@pytest.mark.parametrize("name", golden_names("ref_"))
+def test_reference_fixtures(gb, orc, name):
+    d = load_golden(name)
+    n = int(d["n"])
+    g = gb.Graph.from_edges(n, d["src"], d["dst"], 0)   # directed, as stored
+    row, col = g.csr()
+    o = orc.csr_build(n, d["src"], d["dst"], 0)
+    assert sorted_rows_equal(row, col, o.row_offset, o.col_idx)
+    for s, want in zip(d["sources"], d["levels"]):
+        got = g.bfs(int(s))
+        assert np.array_equal(got, want), (name, int(s))
+    if "ref_row" in d:  # the reference's own (unsorted) CSR through from_csr
+        g2 = gb.Graph.from_csr(d["ref_row"], d["ref_col"])
+        for s, want in zip(d["sources"], d["levels"]):
+            assert np.array_equal(g2.bfs(int(s)), want)
+
+
+@pytest.mark.parametrize("name", golden_names("syn_"))
+@pytest.mark.parametrize("mode", list(MODES))
+def test_synthetic_golden(gb, orc, name, mode):
+    d = load_golden(name)
+    n, src, dst = synthetic_edges(d)
+    g = gb.Graph.from_edges(n, src, dst, gb.UNDIRECTED)
+    o = orc.csr_build(n, src, dst, orc.UNDIRECTED)
+    row, col = g.csr()
+    assert np.array_equal(row, o.row_offset) and np.array_equal(col, o.col_idx)
+    g.set_params(direction=MODES[mode])
+    for s, want in zip(d["sources"], d["levels"]):
+        got, st = g.bfs(int(s), stats=True)
+        assert np.array_equal(got, want)
+        assert st.vertices_reached == int((want >= 0).sum())
+        assert st.edges_in_component == orc.component_edges(o, want)
+        assert st.levels == int(want.max()) + 1
+
+
+def _check_against_oracle(gb, orc, n, src, dst, sources, flags=None, params=None):
+    flags = gb.UNDIRECTED if flags is None else flags
+    g = gb.Graph.from_edges(n, src, dst, flags)
+    o = orc.csr_build(n, src, dst, flags)
+    row, col = g.csr()
+    if flags & gb.DEDUP:
+        assert np.array_equal(row, o.row_offset) and np.array_equal(col, o.col_idx)
+    if params:
+        g.set_params(**params)
+    for s in sources:
+        want = orc.bfs_queue(o, int(s))
+        got = g.bfs(int(s))
+        assert np.array_equal(got, want), int(s)
+    return g, o
+
+
+@pytest.mark.parametrize("params", [
+    {}, {"threads_per_block": 256, "blocks_per_sm": 4}, {"threads_per_block": 1024, "blocks_per_sm": 1},
+    {"alpha": 2, "beta": 4}, {"alpha": 96, "beta": 96}, {"big_degree": 32}, {"big_degree": 4096},
+    {"direction": 1}, {"direction": 2},
+])
+def test_rmat18_param_grid(gb, orc, params):
+    src, dst = gb.gen_rmat(18, 16, seed=2)
+    deg = np.bincount(np.concatenate([src, dst]), minlength=1 << 18)
+    rng = np.random.default_rng(0)
+    sources = rng.choice(np.flatnonzero(deg > 0), 3, replace=False)
+    _check_against_oracle(gb, orc, 1 << 18, src, dst, list(sources) + [int(np.argmax(deg))], params=params)
+
+
+def test_grid_high_diameter(gb, orc):
+    side = 400
+    src, dst = gb.gen_grid(side, 0.1, 0.001, 8, seed=3)
+    g, o = _check_against_oracle(gb, orc, side * side, src, dst, [0, side * side // 2 + 7])
+    _, st = g.bfs(0, stats=True)
+    assert st.levels > side  # hundreds of levels in one persistent launch
+    assert st.launches == 1
+
+
+def test_er_and_directed(gb, orc):
+    src, dst = gb.gen_er(200000, 800000, seed=4)
+    _check_against_oracle(gb, orc, 200000, src, dst, [0, 5, 199999])
+    # directed as stored: bottom-up must not be used (no reverse edges)
+    src, dst = gb.gen_er(50000, 150000, seed=5)
+    g, _ = _check_against_oracle(gb, orc, 50000, src, dst, [0, 1, 2], flags=0)
+    g.set_params(direction=2)
+    o = orc.csr_build(50000, src, dst, 0)
+    assert np.array_equal(g.bfs(3), orc.bfs_queue(o, 3))
+
+
+def test_edge_cases(gb, orc):
+    # single vertex, no edges
+    g = gb.Graph.from_edges(1, np.array([], np.int32), np.array([], np.int32))
+    assert g.bfs(0).tolist() == [0]
+    # isolated source and isolated vertices
+    g = gb.Graph.from_edges(6, [1, 2], [2, 3])
+    assert g.bfs(0).tolist() == [0, -1, -1, -1, -1, -1]
+    assert g.bfs(1).tolist() == [-1, 0, 1, 2, -1, -1]
+    # self-loops and duplicates only
+    g = gb.Graph.from_edges(3, [0, 0, 1, 1], [0, 1, 0, 1], 0)
+    assert g.bfs(0).tolist() == [0, 1, -1]
+    g = gb.Graph.from_edges(3, [0, 0, 1, 1], [0, 1, 0, 1], gb.UNDIRECTED)
+    assert g.m == 2 and g.bfs(1).tolist() == [1, 0, -1]
+    # n not a multiple of 32, last vertex reached
+    n = 33
+    g = gb.Graph.from_edges(n, np.arange(n - 1), np.arange(1, n))
+    assert g.bfs(0).tolist() == list(range(n))
+    assert g.bfs(n - 1).tolist() == list(range(n - 1, -1, -1))
+    # errors
+    with pytest.raises(gb.GbfsError) as e:
+        g.bfs(n)
+    assert e.value.code == gb._lib.ERR_INVALID_ARG
+    with pytest.raises(gb.GbfsError) as e:
+        g.bfs(-1)
+    with pytest.raises(gb.GbfsError) as e:
+        gb.Graph.from_edges(4, [0, 5], [1, 2])
+    assert e.value.code == gb._lib.ERR_INVALID_ARG
+    with pytest.raises(gb.GbfsError):
+        gb.Graph.from_csr(np.array([0, 2, 1], np.int32), np.array([1, 0], np.int32))
+    with pytest.raises(gb.GbfsError):
+        gb.Graph.from_csr(np.array([0, 1, 2], np.int32), np.array([1, 7], np.int32))
+
+
+def test_device_output_and_input(gb, orc):
+    torch = pytest.importorskip("torch")
+    src, dst = gb.gen_rmat(14, 16, seed=6)
+    o = orc.csr_build(1 << 14, src, dst, orc.UNDIRECTED)
+    g = gb.Graph.from_edges(1 << 14, torch.from_numpy(src).cuda(), torch.from_numpy(dst).cuda())
+    out = torch.empty(1 << 14, dtype=torch.int32, device="cuda")
+    s = int(np.argmax(np.diff(o.row_offset)))
+    g.bfs(s, out=out)
+    assert np.array_equal(out.cpu().numpy(), orc.bfs_queue(o, s))
+    row, col = g.csr()
+    g2 = gb.Graph.from_csr(torch.from_numpy(row).cuda(), torch.from_numpy(col).cuda())
+    assert np.array_equal(g2.bfs(s), orc.bfs_queue(o, s))
+
+
+def test_multiroot(gb, orc):
+    src, dst = gb.gen_rmat(15, 16, seed=8)
+    n = 1 << 15
+    o = orc.csr_build(n, src, dst, orc.UNDIRECTED)
+    g = gb.Graph.from_edges(n, src, dst)
+    roots = [3, 77, 77, 1000, 30000]
+    want = None
+    for r in roots:
+        lv = orc.bfs_queue(o, r)
+        lv = np.where(lv < 0, np.iinfo(np.int32).max, lv)
+        want = lv if want is None else np.minimum(want, lv)
+    want = np.where(want == np.iinfo(np.int32).max, -1, want).astype(np.int32)
+    got, st = g.bfs_multiroot(roots, stats=True)
+    assert np.array_equal(got, want)
+    assert st.vertices_reached == int((want >= 0).sum())
+
+
+def test_save_load_roundtrip(gb, orc, tmp_path):
+    src, dst = gb.gen_er(5000, 20000, seed=9)
+    g = gb.Graph.from_edges(5000, src, dst)
+    p = tmp_path / "g.csr"
+    g.save(str(p))
+    g2 = gb.Graph.load(str(p))
+    r1, c1 = g.csr()
+    r2, c2 = g2.csr()
+    assert np.array_equal(r1, r2) and np.array_equal(c1, c2)
+    assert np.array_equal(g.bfs(0), g2.bfs(0))
+
+
+def test_reference_interface_mirror(gb, orc, tmp_path):
+    d = load_golden("ref_test2")
+    p = tmp_path / "test2.txt"
+    p.write_text("\n".join([str(int(d["n"])), str(len(d["src"]))] +
+                           [f"{a + 1} {b + 1}" for a, b in zip(d["src"], d["dst"])]))
+    graph = gb.csr(str(p))
+    assert graph.num_nodes == int(d["n"]) and graph.num_edges == len(d["src"])
+    for s, want in zip(d["sources"], d["levels"]):
+        b = gb.gpuBFS(graph, int(s))
+        assert np.array_equal(b.host_distance, want)
+        assert b.iteration == int(want.max()) + 1
+        assert b.total_edges_traversed == int((want >= 0).sum()) - 1
+        assert b.exec_time > 0
