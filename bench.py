@@ -59,6 +59,8 @@ def parse_args():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--autotune", action="store_true", help="autotune parameters before timing")
     ap.add_argument("--params", type=str, default="", help="k=v,... overrides of the traversal parameters")
+    ap.add_argument("--layout", choices=["hub-first", "sorted"], default="hub-first",
+                    help="CSR row order: sorted ids, or highest-degree neighbour first")
     return ap.parse_args()
 
 
@@ -244,7 +246,7 @@ def main():
     import gpu_graphs_gb300 as gb
 
     n, src, dst = workload(args.scale)
-    g = gb.Graph.from_edges(n, src, dst, gb.UNDIRECTED)
+    g = gb.Graph.from_edges(n, src, dst, gb.UNDIRECTED | (gb.HUB_FIRST if args.layout == "hub-first" else 0))
     del src, dst
     row, col = g.csr()
     deg = np.diff(row)
@@ -336,7 +338,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic", "config": config_block(args, n, g.m) | {"parallelism": f"replicas{world}",
-                                                                            "params": params},
+                                                                            "layout": args.layout, "params": params},
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
             "clocks": clk.summary(), "parity_spot_check": parity,
             "per_source_gteps": {"min": round(min(gteps_each), 2), "median": round(statistics.median(gteps_each), 2),

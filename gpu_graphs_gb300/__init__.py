@@ -21,13 +21,13 @@ from typing import Iterable, Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import (DEDUP, DIR_BOTTOMUP, DIR_OPTIMIZING, DIR_TOPDOWN, DROP_SELF_LOOPS, SYMMETRIZE,
+from ._lib import (DEDUP, DIR_BOTTOMUP, DIR_OPTIMIZING, DIR_TOPDOWN, DROP_SELF_LOOPS, HUB_FIRST, SYMMETRIZE,
                    UNDIRECTED, GbfsError, Params, Stats, check, lib)
 
 __all__ = [
     "Graph", "GraphSet", "Server", "GbfsError", "Params", "Stats", "csr", "gpuBFS",
     "read_edge_list", "gen_er", "gen_rmat", "gen_grid", "exclusive_scan", "default_params",
-    "SYMMETRIZE", "DEDUP", "DROP_SELF_LOOPS", "UNDIRECTED", "DIR_OPTIMIZING", "DIR_TOPDOWN",
+    "SYMMETRIZE", "DEDUP", "DROP_SELF_LOOPS", "UNDIRECTED", "HUB_FIRST", "DIR_OPTIMIZING", "DIR_TOPDOWN",
     "DIR_BOTTOMUP", "library_path",
 ]
 
@@ -177,6 +177,17 @@ class Graph:
         check(lib.gbfs_bfs_many(self._h, C.c_void_p(s.ctypes.data), k, po, C.cast(sts, C.c_void_p)),
               "gbfs_bfs_many")
         return out, list(sts)
+
+    def last_trace(self) -> list[dict]:
+        """Per-level trace of the last traversal: level, direction, frontier
+        size and edges, and the step's end time in us after initialisation."""
+        rows = (_lib.LevelTrace * 1024)()
+        k = lib.gbfs_last_trace(self._h, C.cast(rows, C.c_void_p), 1024)
+        if k < 0:
+            raise GbfsError(k, "gbfs_last_trace")
+        dirs = {-2: "end", -1: "init", 0: "td", 1: "bu", 2: "td+split"}
+        return [{"level": r.level, "dir": dirs.get(r.direction, str(r.direction)), "frontier": r.frontier_vertices,
+                 "edges": r.frontier_edges, "t_us": round(r.t_us, 2)} for r in rows[:k]]
 
     @property
     def stream(self) -> int:

@@ -25,6 +25,7 @@ SYMMETRIZE = 1
 DEDUP = 2
 DROP_SELF_LOOPS = 4
 UNDIRECTED = SYMMETRIZE | DEDUP | DROP_SELF_LOOPS
+HUB_FIRST = 8
 
 DIR_OPTIMIZING = 0
 DIR_TOPDOWN = 1
@@ -70,6 +71,16 @@ class GraphInfo(C.Structure):
         ("m", C.c_int64),
         ("nonisolated", C.c_int64),
         ("device_bytes", C.c_int64),
+    ]
+
+
+class LevelTrace(C.Structure):
+    _fields_ = [
+        ("level", C.c_int32),
+        ("direction", C.c_int32),
+        ("frontier_vertices", C.c_int64),
+        ("frontier_edges", C.c_int64),
+        ("t_us", C.c_double),
     ]
 
 
@@ -134,6 +145,7 @@ SIGNATURES = {
     "gbfs_bfs_multiroot": (C.c_int, [P, P, I32, P, C.POINTER(Stats)]),
     "gbfs_bfs_many": (C.c_int, [P, P, I32, P, P]),
     "gbfs_graph_stream": (C.c_void_p, [P]),
+    "gbfs_last_trace": (C.c_int, [P, P, I32]),
     "gbfs_bfs_multi": (C.c_int, [P, P, I32, P, C.POINTER(Stats)]),
     "gbfs_graphset_from_edges": (C.c_int, [I32, P, P, P, P, C.c_uint32, C.POINTER(P)]),
     "gbfs_graphset_from_graphs": (C.c_int, [I32, P, C.POINTER(P)]),

@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <cerrno>
 #include <cstdio>
+#include <cstddef>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
@@ -43,51 +44,6 @@ bool is_device_ptr(const void *p)
     return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
 }
 
-namespace {
-
-// Symmetry check on sorted rows: every (u,v) has (v,u).
-__global__ void k_check_sym(const int *__restrict__ row, const int *__restrict__ col, int n,
-                            int *flags /*[0] unsorted, [1] asymmetric*/)
-{
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += stride) {
-        const int b = row[u], e = row[u + 1];
-        for (int i = b; i < e; i++) {
-            const int v = col[i];
-            if (i > b && col[i - 1] > v) {
-                flags[0] = 1;
-                return;
-            }
-            int lo = row[v], hi = row[v + 1];
-            while (lo < hi) {
-                int mid = (lo + hi) >> 1;
-                if (col[mid] < (int)u) lo = mid + 1; else hi = mid;
-            }
-            if (lo >= row[v + 1] || col[lo] != (int)u) flags[1] = 1;
-        }
-    }
-}
-
-int check_symmetric(const DeviceCsr &c, cudaStream_t st, bool &sym)
-{
-    int *d = nullptr, h[2] = {0, 0};
-    cudaError_t e = cudaMalloc(&d, 8);
-    if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, 8, st);
-    if (e == cudaSuccess) {
-        int grid = (int)std::min<int64_t>(152 * 8, ((int64_t)c.n + 255) / 256);
-        k_check_sym<<<std::max(grid, 1), 256, 0, st>>>(c.row, c.col, c.n, d);
-        e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, 8, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (d) cudaFree(d);
-    if (e != cudaSuccess) return cuda_fail(e, "symmetry check");
-    sym = h[0] == 0 && h[1] == 0;
-    return GBFS_OK;
-}
-
-}  // namespace
-
 int graph_wrap(DeviceCsr &csr, bool symmetric_known, bool symmetric, cudaStream_t st, gbfs_graph **out)
 {
     gbfs_graph *g = new (std::nothrow) gbfs_graph();
@@ -105,10 +61,11 @@ int graph_wrap(DeviceCsr &csr, bool symmetric_known, bool symmetric, cudaStream_
         g->symmetric = symmetric;
     } else {
         bool s = false;
-        int rc = check_symmetric(g->csr, st, s);
+        std::string err;
+        int rc = csr_check_symmetric(g->csr, st, s, err);
         if (rc != GBFS_OK) {
             gbfs_graph_destroy(g);
-            return rc;
+            return fail(rc, err);
         }
         g->symmetric = s;
     }
@@ -236,7 +193,7 @@ extern "C" int gbfs_graph_from_edges(int32_t n, int64_t m, const int32_t *src, c
     *out = nullptr;
     if (n < 1 || n > INT32_MAX - 1) return fail(GBFS_ERR_INVALID_ARG, "n must be in [1, 2^31-2]");
     if (m < 0 || (m > 0 && (!src || !dst))) return fail(GBFS_ERR_INVALID_ARG, "bad edge arrays");
-    if (flags & ~7u) return fail(GBFS_ERR_INVALID_ARG, "unknown flag bits");
+    if (flags & ~15u) return fail(GBFS_ERR_INVALID_ARG, "unknown flag bits");
     if (m > (int64_t)INT32_MAX * 2) return fail(GBFS_ERR_TOO_LARGE, "too many edges");
     cudaStream_t st = nullptr;
     int rc = make_stream(&st);
@@ -248,7 +205,8 @@ extern "C" int gbfs_graph_from_edges(int32_t n, int64_t m, const int32_t *src, c
     rc = to_device(src, m, st, &d_src, &own_s);
     if (!rc) rc = to_device(dst, m, st, &d_dst, &own_d);
     if (!rc) {
-        rc = csr_build_from_edges(n, m, d_src, d_dst, flags, st, csr, err);
+        rc = csr_build_from_edges(n, m, d_src, d_dst, flags & 7u, st, csr, err);
+        if (!rc && (flags & GBFS_HUB_FIRST)) rc = csr_hub_first(csr, st, err);
         if (rc) set_error(err);
     }
     cudaStreamSynchronize(st);
@@ -368,7 +326,7 @@ static int run_bfs_locked(gbfs_graph *g, const int *d_roots, int k, int single_r
     const bool dev_out = is_device_ptr(levels_out);
     int *d_level = dev_out ? levels_out : g->work.level;
     gbfs_params p = effective_params(g);
-    rc = bfs_run(g->csr, p, g->work, d_roots, k, single_root, d_level, g->stream, res, err);
+    rc = bfs_run(g->csr, p, g->work, d_roots, k, single_root, d_level, g->stream, res, err, g->symmetric);
     if (rc) return fail(rc, err);
     if (!dev_out) {
         cudaError_t e = cudaMemcpyAsync(levels_out, d_level, sizeof(int) * (size_t)g->csr.n,
@@ -417,14 +375,16 @@ extern "C" int gbfs_bfs_many(gbfs_graph *g, const int32_t *sources, int32_t k, i
     for (int32_t i = 0; i < k && e == cudaSuccess; i++) {
         int *d_level = dev_out ? levels_out + n * i : w.level;
         e = cudaEventRecord(w.evs[i], g->stream);
-        if (e == cudaSuccess) e = bfs_enqueue(g->csr, p, w, nullptr, 1, hsrc[i], d_level, w.d_outs + i, g->stream);
+        if (e == cudaSuccess)
+            e = bfs_enqueue(g->csr, p, w, nullptr, 1, hsrc[i], d_level, w.d_outs + i, g->stream, g->symmetric);
         if (e == cudaSuccess && levels_out && !dev_out)
             e = cudaMemcpyAsync(levels_out + n * i, d_level, sizeof(int) * n, cudaMemcpyDeviceToHost, g->stream);
     }
     if (e == cudaSuccess) e = cudaEventRecord(w.evs[k], g->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(w.h_outs, w.d_outs, sizeof(BfsOut) * (size_t)k, cudaMemcpyDeviceToHost, g->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(w.h_ctrl, w.ctrl, sizeof(BfsCtrl), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(w.h_ctrl, w.ctrl, offsetof(BfsCtrl, t_entry), cudaMemcpyDeviceToHost, g->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     if (e != cudaSuccess) return cuda_fail(e, "BFS launches");
     if (w.h_ctrl->status != DEV_OK) {
@@ -446,6 +406,42 @@ extern "C" int gbfs_bfs_many(gbfs_graph *g, const int32_t *sources, int32_t k, i
             fill_stats(&stats[i], r, 1);
         }
     return GBFS_OK;
+}
+
+extern "C" int gbfs_last_trace(gbfs_graph *g, gbfs_level_trace *rows, int32_t cap)
+{
+    if (!g || (cap > 0 && !rows) || cap < 0) return fail(GBFS_ERR_INVALID_ARG, "bad argument");
+    std::lock_guard<std::mutex> lk(g->mu);
+    if (!g->work.ctrl) return 0;
+    BfsCtrl *h = g->work.h_ctrl;
+    cudaError_t e = cudaMemcpyAsync(&h->t_entry, &g->work.ctrl->t_entry,
+                                    sizeof(BfsCtrl) - offsetof(BfsCtrl, t_entry), cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "trace D2H");
+    const int len = std::min<int>(std::min<int>(h->trace_len, TRACE_CAP), cap - 2);
+    if (len < 0) return 0;
+    // row 0: initialisation (level -1), from CTA 0's entry to the end of init
+    rows[0].level = -1;
+    rows[0].direction = -1;
+    rows[0].frontier_vertices = 0;
+    rows[0].frontier_edges = 0;
+    rows[0].t_us = -(double)(h->t_start - h->t_entry) / 1000.0;
+    rows++;
+    for (int i = 0; i < len; i++) {
+        const LevelTrace &t = h->trace[i];
+        rows[i].level = t.level;
+        rows[i].direction = t.dir;
+        rows[i].frontier_vertices = (int64_t)t.frontier;
+        rows[i].frontier_edges = (int64_t)t.edges;
+        rows[i].t_us = (double)(t.t_ns - h->t_start) / 1000.0;
+    }
+    // last row: the end of the level loop (the termination check included)
+    rows[len].level = -2;
+    rows[len].direction = -2;
+    rows[len].frontier_vertices = 0;
+    rows[len].frontier_edges = 0;
+    rows[len].t_us = (double)(h->t_end - h->t_start) / 1000.0;
+    return len + 2;
 }
 
 extern "C" void *gbfs_graph_stream(const gbfs_graph *g) { return g ? (void *)g->stream : nullptr; }

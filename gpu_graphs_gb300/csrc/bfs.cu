@@ -33,6 +33,7 @@
 // Bottom-up needs in-edges == out-edges, so it is used on symmetric graphs
 // only; other graphs run top-down at every level.
 #include <algorithm>
+#include <cstddef>
 #include <cstring>
 
 #include "bfs.cuh"
@@ -42,7 +43,10 @@ namespace gbfs {
 namespace {
 
 constexpr int QCAP = 256;    // per-warp staging queue entries
-constexpr int CHUNK = 512;   // edges per grid-wide chunk of a deferred row
+constexpr int SEG = 2048;    // frontier rows expanded edge-balanced per pass
+constexpr int ILP = 4;       // edges in flight per lane in top-down passes
+constexpr int PROBE = 8;     // neighbours probed per step in bottom-up
+constexpr int FIRST_PROBE = 2;  // neighbours probed by the first bottom-up step
 
 struct BfsArgs {
     int n;
@@ -50,11 +54,12 @@ struct BfsArgs {
     long long m;
     const int *row;
     const int *col;
-    const unsigned *zmask;
+    const unsigned *zmask;   // out-degree-0 bitmap, or NULL (directed graphs:
+                             // a sink still has in-edges, so it stays claimable)
     int *level;
     unsigned *visited;
-    unsigned *fb0, *fb1;
-    int *q0, *q1;
+    unsigned *fb[3];         // frontier bitmaps, rotating by level
+    int *q0, *q1;            // frontier queues
     int *bigl;
     BfsCtrl *ctrl;
     BfsOut *out;
@@ -92,14 +97,28 @@ __device__ __forceinline__ void wq_push(WarpQ &q, bool has, int v, unsigned long
     q.n += c;
 }
 
-__device__ __forceinline__ bool td_claim(int w, unsigned *visited, int *level, int nl)
+// Flush every warp queue of the block with one global atomic (all threads call).
+__device__ __forceinline__ void block_flush(WarpQ &q, unsigned long long *cnt, int *out, int *s_wq,
+                                            unsigned long long *s_base)
 {
-    const unsigned bit = 1u << (w & 31);
-    unsigned *p = visited + (w >> 5);
-    if (__ldcg(p) & bit) return false;
-    if (atomicOr(p, bit) & bit) return false;
-    level[w] = nl;
-    return true;
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __syncwarp();
+    if (lane_id() == 0) s_wq[w] = q.n;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int tot = 0;
+        for (int i = 0; i < nw; i++) {
+            const int c = s_wq[i];
+            s_wq[i] = tot;
+            tot += c;
+        }
+        *s_base = tot ? atomicAdd(cnt, (unsigned long long)tot) : 0ull;
+    }
+    __syncthreads();
+    const unsigned long long base = *s_base + (unsigned long long)s_wq[w];
+    for (int i = lane_id(); i < q.n; i += 32) out[base + i] = q.buf[i];
+    q.n = 0;
+    __syncthreads();
 }
 
 template <typename T>
@@ -135,67 +154,147 @@ __device__ __forceinline__ int block_excl_scan_int(int x, int *s_warp, int *tota
     return s_warp[warp] + incl - x;
 }
 
-// Claim every neighbour in col[s, e) with the whole warp (int4 body).
-__device__ __forceinline__ void warp_claim_range(int s, int e, const BfsArgs &a, int nl, WarpQ &q,
-                                                 unsigned long long *cnt, int *qn,
-                                                 unsigned long long &my_deg)
+// Top-down claim of ILP neighbours per lane, all loads and atomics issued
+// before any result is used.  w[j] < 0 means "no edge".  A vertex is won by
+// the atomicOr that sets its visited bit; the winner writes its level,
+// adds its out-degree to my_deg and appends it to the warp queue.
+__device__ __forceinline__ void claim_batch(const int (&w)[ILP], const BfsArgs &a, int nl, WarpQ &q,
+                                            unsigned long long *cnt, int *qn, unsigned long long &my_deg)
 {
-    const int lane = (int)lane_id();
-    const int al = min(e, (s + 3) & ~3);
-    {
-        int k = s + lane;
-        bool got = false;
-        int w = 0;
-        if (k < al) {
-            w = __ldg(a.col + k);
-            got = td_claim(w, a.visited, a.level, nl);
-        }
-        if (got) my_deg += __ldg(a.row + w + 1) - __ldg(a.row + w);
-        wq_push(q, got, w, cnt, qn);
+    unsigned word[ILP];
+#pragma unroll
+    for (int j = 0; j < ILP; j++) word[j] = w[j] >= 0 ? a.visited[w[j] >> 5] : FULL;
+    unsigned old[ILP];
+#pragma unroll
+    for (int j = 0; j < ILP; j++) {
+        const unsigned bit = 1u << (w[j] & 31);
+        old[j] = FULL;
+        if (!(word[j] & bit)) old[j] = atomicOr(&a.visited[w[j] >> 5], bit);
     }
-    const int z = al + ((e - al) & ~3);
-    for (int base = al; base < z; base += 128) {
-        const int k = base + lane * 4;
-        int4 x = make_int4(0, 0, 0, 0);
-        const bool ok = k < z;
-        if (ok) x = ld_stream_v4(a.col + k);
-        bool g0 = ok && td_claim(x.x, a.visited, a.level, nl);
-        bool g1 = ok && td_claim(x.y, a.visited, a.level, nl);
-        bool g2 = ok && td_claim(x.z, a.visited, a.level, nl);
-        bool g3 = ok && td_claim(x.w, a.visited, a.level, nl);
-        if (g0) my_deg += __ldg(a.row + x.x + 1) - __ldg(a.row + x.x);
-        if (g1) my_deg += __ldg(a.row + x.y + 1) - __ldg(a.row + x.y);
-        if (g2) my_deg += __ldg(a.row + x.z + 1) - __ldg(a.row + x.z);
-        if (g3) my_deg += __ldg(a.row + x.w + 1) - __ldg(a.row + x.w);
-        wq_push(q, g0, x.x, cnt, qn);
-        wq_push(q, g1, x.y, cnt, qn);
-        wq_push(q, g2, x.z, cnt, qn);
-        wq_push(q, g3, x.w, cnt, qn);
-    }
-    {
-        int k = z + lane;
-        bool got = false;
-        int w = 0;
-        if (k < e) {
-            w = __ldg(a.col + k);
-            got = td_claim(w, a.visited, a.level, nl);
+    bool won[ILP];
+    int d0[ILP], d1[ILP];
+#pragma unroll
+    for (int j = 0; j < ILP; j++) {
+        won[j] = !((old[j] >> (w[j] & 31)) & 1u);
+        d0[j] = d1[j] = 0;
+        if (won[j]) {
+            a.level[w[j]] = nl;
+            d0[j] = __ldg(a.row + w[j]);
+            d1[j] = __ldg(a.row + w[j] + 1);
         }
-        if (got) my_deg += __ldg(a.row + w + 1) - __ldg(a.row + w);
-        wq_push(q, got, w, cnt, qn);
+    }
+#pragma unroll
+    for (int j = 0; j < ILP; j++) {
+        my_deg += (unsigned long long)(d1[j] - d0[j]);
+        wq_push(q, won[j], w[j], cnt, qn);
     }
 }
 
+// Expand the rows of list[0, cnt) with every warp of the grid, the edges
+// split evenly: each CTA builds the degree prefix of a SEG-row segment in
+// shared memory and warp g takes edges [E*g/W, E*(g+1)/W) of it.
 template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) k_bfs(BfsArgs a)
+__device__ void grid_expand_list(const int *list, int cnt, const BfsArgs &a, int nl, WarpQ &q,
+                                 unsigned long long *cnt_next, int *qn, unsigned long long &my_deg, int *s_pre,
+                                 int *s_beg, int *s_warp)
+{
+    constexpr int PER = SEG / BLOCK;
+    const int lane = (int)lane_id();
+    const long long gwarp = ((long long)blockIdx.x * BLOCK + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * BLOCK) >> 5;
+    for (int seg = 0; seg < cnt; seg += SEG) {
+        const int segn = min(SEG, cnt - seg);
+        int d[PER];
+        int sum = 0;
+#pragma unroll
+        for (int t = 0; t < PER; t++) {
+            const int j = threadIdx.x * PER + t;
+            d[t] = 0;
+            if (j < segn) {
+                const int v = __ldcg(list + seg + j);
+                const int b = __ldg(a.row + v);
+                s_beg[j] = b;
+                d[t] = __ldg(a.row + v + 1) - b;
+            }
+            sum += d[t];
+        }
+        int total;
+        int run = block_excl_scan_int(sum, s_warp, &total);
+#pragma unroll
+        for (int t = 0; t < PER; t++) {
+            const int j = threadIdx.x * PER + t;
+            if (j < segn) s_pre[j] = run;
+            run += d[t];
+        }
+        __syncthreads();
+        const long long lo = (long long)total * gwarp / nwarps;
+        const long long hi = (long long)total * (gwarp + 1) / nwarps;
+        for (long long base = lo; base < hi; base += 32 * ILP) {
+            int w[ILP];
+#pragma unroll
+            for (int j = 0; j < ILP; j++) {
+                const long long e = base + j * 32 + lane;
+                w[j] = -1;
+                if (e < hi) {
+                    int l = 0, h = segn - 1;  // max r with s_pre[r] <= e
+                    while (l < h) {
+                        const int mid = (l + h + 1) >> 1;
+                        if (s_pre[mid] <= e) l = mid; else h = mid - 1;
+                    }
+                    w[j] = __ldg(a.col + s_beg[l] + (int)(e - s_pre[l]));
+                }
+            }
+            claim_batch(w, a, nl, q, cnt_next, qn, my_deg);
+        }
+        __syncthreads();
+    }
+}
+
+// Bits of a bitmap word set through a tile of BLOCK words per CTA pass:
+// appends the vertices whose bit is set in (want ? bits : ~bits & valid)
+// to out, one global atomic per CTA tile.
+template <int BLOCK>
+__device__ void bitmap_to_list(const unsigned *bm, bool complement, int n, int W, int *out,
+                               unsigned long long *cnt, int *s_warp, unsigned long long *s_base)
+{
+    for (long long t0 = (long long)blockIdx.x * BLOCK; t0 < W; t0 += (long long)gridDim.x * BLOCK) {
+        const long long w = t0 + threadIdx.x;
+        unsigned bits = 0;
+        if (w < W) {
+            bits = __ldcg(bm + w);
+            if (complement) {
+                const unsigned valid = (w == W - 1 && (n & 31)) ? ((1u << (n & 31)) - 1u) : FULL;
+                bits = ~bits & valid;
+            }
+        }
+        int total;
+        const int off = block_excl_scan_int(__popc(bits), s_warp, &total);
+        if (threadIdx.x == 0) *s_base = total ? atomicAdd(cnt, (unsigned long long)total) : 0ull;
+        __syncthreads();
+        unsigned long long pos = *s_base + (unsigned long long)off;
+        while (bits) {
+            const int b = __ffs(bits) - 1;
+            out[pos++] = (int)(w * 32 + b);
+            bits &= bits - 1u;
+        }
+        __syncthreads();
+    }
+}
+
+// MINB (CTAs per SM the register budget is sized for) only shapes register
+// allocation; the launch decides the actual grid.
+template <int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
 {
     extern __shared__ int smem[];
     __shared__ unsigned long long s_red[32];
+    __shared__ unsigned long long s_base;
     __shared__ int s_warp[33];
+    __shared__ int s_wq[33];
     constexpr int NW = BLOCK / 32;
-    int *s_q = smem;                       // NW * QCAP
-    int *s_cs = smem + NW * QCAP;          // BLOCK + 1 chunk prefix
-    int *s_b = s_cs + BLOCK + 1;           // BLOCK row begins
-    int *s_e = s_b + BLOCK;                // BLOCK row ends
+    int *s_q = smem;                           // NW * QCAP warp queues
+    int *s_pre = s_q + NW * QCAP;              // SEG degree prefix
+    int *s_beg = s_pre + SEG;                  // SEG row begins
 
     const int n = a.n;
     const int W = (n + 31) >> 5;
@@ -206,6 +305,8 @@ __global__ void __launch_bounds__(BLOCK) k_bfs(BfsArgs a)
     const long long nwarps = gthreads >> 5;
     BfsCtrl *ctrl = a.ctrl;
     WarpQ q{s_q + (threadIdx.x >> 5) * QCAP, 0};
+    unsigned epoch = 0;
+    if (gtid == 0) ctrl->t_entry = globaltimer_ns();
 
     // ---- init ----------------------------------------------------------
     {
@@ -219,17 +320,18 @@ __global__ void __launch_bounds__(BLOCK) k_bfs(BfsArgs a)
             for (long long i = gtid; i < n; i += gthreads) a.level[i] = -1;
         }
         for (long long w = gtid; w < W; w += gthreads) {
-            unsigned z = a.zmask[w];
+            unsigned z = a.zmask ? a.zmask[w] : 0u;
             if (root >= 0 && w == (root >> 5)) z |= 1u << (root & 31);
             a.visited[w] = z;
-            a.fb0[w] = 0;
+            a.fb[0][w] = 0;
+            a.fb[1][w] = 0;
         }
         if (root >= 0 && gtid == 0) {
             a.q0[0] = root;
             ctrl->cnt[0] = 1;
             ctrl->deg[0] = (unsigned long long)(__ldg(a.row + root + 1) - __ldg(a.row + root));
         }
-        if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns)) return;
+        if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
         if (root >= 0) {
             if (gtid == 0) a.level[root] = 0;
         } else {
@@ -245,11 +347,14 @@ __global__ void __launch_bounds__(BLOCK) k_bfs(BfsArgs a)
                     }
                 }
             }
-            if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns)) return;
+            if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
         }
     }
+    if (gtid == 0) ctrl->t_start = globaltimer_ns();
 
     // ---- level loop ------------------------------------------------------
+    // Frontier L lives in queue q[L&1] after a top-down step and in bitmap
+    // fb[L%3] after a bottom-up step; switches convert.
     long long m_u = a.m;                 // out-edges of not-yet-reached vertices
     unsigned long long prev_nf = 0, reached = 0, edges_c = 0, roots = 0;
     int L = 0, td_levels = 0, bu_levels = 0;
@@ -271,12 +376,14 @@ __global__ void __launch_bounds__(BLOCK) k_bfs(BfsArgs a)
 
         int *qc = (L & 1) ? a.q1 : a.q0;
         int *qn = (L & 1) ? a.q0 : a.q1;
-        unsigned *fc = (L & 1) ? a.fb1 : a.fb0;
-        unsigned *fn = (L & 1) ? a.fb0 : a.fb1;
+        unsigned *fc = a.fb[L % 3];
+        unsigned *fn = a.fb[(L + 1) % 3];
+        unsigned *fz = a.fb[(L + 2) % 3];   // zeroed now: the next level's fn
         unsigned long long *cnt_next = &ctrl->cnt[(L + 1) % 3];
         unsigned long long *deg_next = &ctrl->deg[(L + 1) % 3];
         const int nl = L + 1;
 
+        bool traced_big = false;
         if (gtid == 0) {
             ctrl->cnt[(L + 2) % 3] = 0;
             ctrl->deg[(L + 2) % 3] = 0;
@@ -284,176 +391,213 @@ __global__ void __launch_bounds__(BLOCK) k_bfs(BfsArgs a)
         }
 
         if (bu && td) {
-            // queue -> bitmap (fc was zeroed by the previous top-down step or init)
+            // queue -> bitmap (fc is zero: fb[L%3] was cleared two levels
+            // ago and top-down steps do not write it)
             for (long long i = gtid; i < (long long)nf; i += gthreads) {
                 const int v = __ldcg(qc + i);
                 atomicOr(&fc[v >> 5], 1u << (v & 31));
             }
-            if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns)) return;
+            if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
         } else if (!bu && !td) {
-            // bitmap -> queue (slots from the fill counter, reset by the next
-            // top-down step, which is behind the barrier below)
-            for (long long w0 = gwarp * 32; w0 < W; w0 += nwarps * 32) {
-                const long long w = w0 + lane;
-                unsigned bits = w < W ? __ldcg(fc + w) : 0u;
-                const int c = __popc(bits);
-                const int incl = warp_incl_scan(c);
-                const int tot = __shfl_sync(FULL, incl, 31);
-                unsigned long long base = 0;
-                if (lane == 31 && tot) base = atomicAdd(&ctrl->fill, (unsigned long long)tot);
-                base = __shfl_sync(FULL, base, 31);
-                unsigned long long pos = base + (unsigned long long)(incl - c);
-                while (bits) {
-                    const int bpos = __ffs(bits) - 1;
-                    qc[pos++] = (int)(w * 32 + bpos);
-                    bits &= bits - 1u;
-                }
-            }
-            if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns)) return;
+            // bitmap -> queue
+            bitmap_to_list<BLOCK>(fc, false, n, W, qc, &ctrl->fill, s_warp, &s_base);
+            if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
         }
         td = !bu;
 
+        for (long long w = gtid; w < W; w += gthreads) fz[w] = 0;
         if (td) {
             ++td_levels;
             if (gtid == 0) ctrl->fill = 0;
-            // zero the bitmap the next level would convert into
-            for (long long w = gtid; w < W; w += gthreads) fn[w] = 0;
             unsigned long long my_deg = 0;
-            for (long long base = gwarp * 32; base < (long long)nf; base += nwarps * 32) {
-                const long long i = base + lane;
-                int v = 0, b = 0, d = 0;
-                if (i < (long long)nf) {
-                    v = __ldcg(qc + i);
-                    b = __ldg(a.row + v);
-                    d = __ldg(a.row + v + 1) - b;
-                }
-                const bool isbig = d >= a.big_degree;
-                const unsigned bm = __ballot_sync(FULL, isbig);
-                if (bm) {
-                    unsigned pos = 0;
-                    const int leader = __ffs(bm) - 1;
-                    if ((int)lane == leader) pos = atomicAdd(&ctrl->big[L % 3], (unsigned)__popc(bm));
-                    pos = __shfl_sync(FULL, pos, leader);
-                    if (isbig) a.bigl[pos + __popc(bm & lanemask_lt())] = v;
-                    if (isbig) d = 0;
-                }
-                const int incl = warp_incl_scan(d);
-                const int excl = incl - d;
-                const int T = __shfl_sync(FULL, incl, 31);
-                for (int e0 = 0; e0 < T; e0 += 32) {
-                    const int k = e0 + (int)lane;
-                    const int kk = min(k, T - 1);
-                    int lo = 0;
+            if (nf <= (unsigned long long)SEG) {
+                // small frontier: every edge of it balanced over the whole grid
+                grid_expand_list<BLOCK>(qc, (int)nf, a, nl, q, cnt_next, qn, my_deg, s_pre, s_beg, s_warp);
+            } else {
+                // large frontier: 32 rows per warp as one concatenated edge
+                // range, rows of degree >= big_degree deferred to a grid pass
+                for (long long base = gwarp * 32; base < (long long)nf; base += nwarps * 32) {
+                    const long long i = base + lane;
+                    int v = 0, b = 0, d = 0;
+                    if (i < (long long)nf) {
+                        v = __ldcg(qc + i);
+                        b = __ldg(a.row + v);
+                        d = __ldg(a.row + v + 1) - b;
+                    }
+                    const bool isbig = d >= a.big_degree;
+                    const unsigned bm = __ballot_sync(FULL, isbig);
+                    if (bm) {
+                        unsigned pos = 0;
+                        const int leader = __ffs(bm) - 1;
+                        if ((int)lane == leader) pos = atomicAdd(&ctrl->big[L % 3], (unsigned)__popc(bm));
+                        pos = __shfl_sync(FULL, pos, leader);
+                        if (isbig) a.bigl[pos + __popc(bm & lanemask_lt())] = v;
+                        if (isbig) d = 0;
+                    }
+                    const int incl = warp_incl_scan(d);
+                    const int excl = incl - d;
+                    const int T = __shfl_sync(FULL, incl, 31);
+                    for (int e0 = 0; e0 < T; e0 += 32 * ILP) {
+                        int w[ILP];
 #pragma unroll
-                    for (int s = 16; s > 0; s >>= 1) {
-                        const int c = lo + s;
-                        if (__shfl_sync(FULL, excl, c) <= kk) lo = c;
+                        for (int j = 0; j < ILP; j++) {
+                            const int k = e0 + j * 32 + (int)lane;
+                            const int kk = min(k, T - 1);
+                            int lo = 0;
+#pragma unroll
+                            for (int s = 16; s > 0; s >>= 1) {
+                                const int c = lo + s;
+                                if (__shfl_sync(FULL, excl, c) <= kk) lo = c;
+                            }
+                            const int ob = __shfl_sync(FULL, b, lo);
+                            const int oe = __shfl_sync(FULL, excl, lo);
+                            w[j] = k < T ? __ldg(a.col + ob + (kk - oe)) : -1;
+                        }
+                        claim_batch(w, a, nl, q, cnt_next, qn, my_deg);
                     }
-                    const int ob = __shfl_sync(FULL, b, lo);
-                    const int oe = __shfl_sync(FULL, excl, lo);
-                    bool got = false;
-                    int w = 0;
-                    if (k < T) {
-                        w = __ldg(a.col + ob + (kk - oe));
-                        got = td_claim(w, a.visited, a.level, nl);
-                    }
-                    if (got) my_deg += __ldg(a.row + w + 1) - __ldg(a.row + w);
-                    wq_push(q, got, w, cnt_next, qn);
                 }
             }
-            wq_flush(q, cnt_next, qn);
+            block_flush(q, cnt_next, qn, s_wq, &s_base);
             {
                 const unsigned long long bd = block_reduce_sum(my_deg, s_red);
                 if (threadIdx.x == 0 && bd) atomicAdd(deg_next, bd);
             }
-            if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns)) return;
+            if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
 
-            // rows deferred as too long for one warp: split over the whole grid
-            const int nb = (int)__ldcg(&ctrl->big[L % 3]);
+            const int nb = nf > (unsigned long long)SEG ? (int)__ldcg(&ctrl->big[L % 3]) : 0;
+            traced_big = nb > 0;
             if (nb > 0) {
                 my_deg = 0;
-                for (int seg = 0; seg < nb; seg += BLOCK) {
-                    const int segn = min(BLOCK, nb - seg);
-                    int chunks = 0;
-                    if ((int)threadIdx.x < segn) {
-                        const int v = __ldcg(a.bigl + seg + threadIdx.x);
-                        const int b = __ldg(a.row + v), e = __ldg(a.row + v + 1);
-                        s_b[threadIdx.x] = b;
-                        s_e[threadIdx.x] = e;
-                        chunks = (e - b + CHUNK - 1) / CHUNK;
-                    }
-                    int total;
-                    const int ex = block_excl_scan_int(chunks, s_warp, &total);
-                    s_cs[threadIdx.x] = ex;
-                    __syncthreads();
-                    for (long long c = gwarp; c < total; c += nwarps) {
-                        int lo = 0, hi = segn - 1;  // max j with s_cs[j] <= c
-                        while (lo < hi) {
-                            const int mid = (lo + hi + 1) >> 1;
-                            if (s_cs[mid] <= c) lo = mid; else hi = mid - 1;
-                        }
-                        const int s = s_b[lo] + (int)(c - s_cs[lo]) * CHUNK;
-                        const int e = min(s + CHUNK, s_e[lo]);
-                        warp_claim_range(s, e, a, nl, q, cnt_next, qn, my_deg);
-                    }
-                    __syncthreads();
-                }
-                wq_flush(q, cnt_next, qn);
+                grid_expand_list<BLOCK>(a.bigl, nb, a, nl, q, cnt_next, qn, my_deg, s_pre, s_beg, s_warp);
+                block_flush(q, cnt_next, qn, s_wq, &s_base);
                 const unsigned long long bd = block_reduce_sum(my_deg, s_red);
                 if (threadIdx.x == 0 && bd) atomicAdd(deg_next, bd);
-                if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns)) return;
+                if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
             }
         } else {
             ++bu_levels;
             unsigned long long my_cnt = 0, my_deg = 0;
-            for (long long w = gwarp; w < W; w += nwarps) {
-                const unsigned vis = __ldcg(a.visited + w);
-                const unsigned valid = (w == W - 1 && (n & 31)) ? ((1u << (n & 31)) - 1u) : FULL;
-                const unsigned unv = ~vis & valid;
-                if (unv == 0) {
-                    if (lane == 0) fn[w] = 0;
-                    continue;
+            // cw bitmap words per warp iteration, cw chosen so a chunk holds
+            // about 64 unvisited vertices (dense levels: small chunks keep
+            // every warp busy; sparse levels: large chunks avoid empty round
+            // trips).  A chunk's unvisited vertices are dealt two per lane
+            // and probed in interleaved steps; the warp owns the chunk's
+            // words, so fn / visited words are written without atomics.
+            long long unv_est = (long long)a.n_active - (long long)reached;
+            if (unv_est < 1) unv_est = 1;
+            int cw = 2;
+            while (cw < 32 && (long long)cw * 32 * unv_est < 64LL * n) cw <<= 1;
+            unsigned *my_found = (unsigned *)(s_beg) + (threadIdx.x >> 5) * 32;  // s_beg is free here
+            my_found[lane] = 0;
+            __syncwarp();
+            for (long long w0 = gwarp * cw; w0 < W; w0 += nwarps * cw) {
+                const long long wl = w0 + lane;
+                unsigned vis = FULL, valid = 0;
+                if ((int)lane < cw && wl < W) {
+                    vis = __ldcg(a.visited + wl);
+                    valid = (wl == W - 1 && (n & 31)) ? ((1u << (n & 31)) - 1u) : FULL;
                 }
-                const int v = (int)(w * 32 + lane);
-                bool found = false;
-                int d = 0;
-                if ((unv >> lane) & 1u) {
-                    const int b = __ldg(a.row + v), e = __ldg(a.row + v + 1);
-                    d = e - b;
-                    for (int i = b; i < e; i += 4) {
-                        const int u0 = __ldg(a.col + i);
-                        const int u1 = i + 1 < e ? __ldg(a.col + i + 1) : u0;
-                        const int u2 = i + 2 < e ? __ldg(a.col + i + 2) : u0;
-                        const int u3 = i + 3 < e ? __ldg(a.col + i + 3) : u0;
-                        const unsigned f = (__ldcg(fc + (u0 >> 5)) >> (u0 & 31)) |
-                                           (__ldcg(fc + (u1 >> 5)) >> (u1 & 31)) |
-                                           (__ldcg(fc + (u2 >> 5)) >> (u2 & 31)) |
-                                           (__ldcg(fc + (u3 >> 5)) >> (u3 & 31));
-                        if (f & 1u) {
-                            found = true;
-                            break;
+                const unsigned unv = ~vis & valid;
+                const int c = __popc(unv);
+                const int incl = warp_incl_scan(c);
+                const int excl = incl - c;
+                const int U = __shfl_sync(FULL, incl, 31);
+                for (int r0 = 0; r0 < U; r0 += 64) {
+                    int vv[2];
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        const int slot = r0 + (int)lane + 32 * h;
+                        const int jj = min(slot, U - 1);
+                        int owner = 0;
+#pragma unroll
+                        for (int s = 16; s > 0; s >>= 1) {
+                            const int cand = owner + s;
+                            if (__shfl_sync(FULL, excl, cand) <= jj) owner = cand;
                         }
+                        unsigned um = __shfl_sync(FULL, unv, owner);
+                        int k = jj - __shfl_sync(FULL, excl, owner);
+                        int pos = 0;  // position of the k-th set bit of um
+#pragma unroll
+                        for (int s = 16; s > 0; s >>= 1) {
+                            const int lowc = __popc(um & ((1u << s) - 1u));
+                            if (k >= lowc) {
+                                k -= lowc;
+                                um >>= s;
+                                pos += s;
+                            }
+                        }
+                        vv[h] = slot < U ? (int)((w0 + owner) * 32 + pos) : -1;
+                    }
+                    const int va = vv[0], vb = vv[1];
+                    int ia = 0, ea = 0, ib = 0, eb = 0;
+                    if (va >= 0) { ia = __ldg(a.row + va); ea = __ldg(a.row + va + 1); }
+                    if (vb >= 0) { ib = __ldg(a.row + vb); eb = __ldg(a.row + vb + 1); }
+                    const int da = ea - ia, db = eb - ib;
+                    bool fa = false, fb = false;
+                    // First step: FIRST_PROBE neighbours (most vertices find their
+                    // parent there); later steps PROBE wide.  Narrow first steps
+                    // keep the frontier-bitmap sector reads near one per vertex.
+                    int width = FIRST_PROBE;
+                    while ((ia < ea && !fa) || (ib < eb && !fb)) {
+                        int ua[PROBE], ub[PROBE];
+#pragma unroll
+                        for (int t = 0; t < PROBE; t++) {
+                            ua[t] = (t < width && !fa && ia + t < ea) ? __ldg(a.col + ia + t) : -1;
+                            ub[t] = (t < width && !fb && ib + t < eb) ? __ldg(a.col + ib + t) : -1;
+                        }
+                        unsigned ga = 0, gb = 0;
+#pragma unroll
+                        for (int t = 0; t < PROBE; t++) {
+                            if (ua[t] >= 0) ga |= __ldcg(fc + (ua[t] >> 5)) >> (ua[t] & 31);
+                            if (ub[t] >= 0) gb |= __ldcg(fc + (ub[t] >> 5)) >> (ub[t] & 31);
+                        }
+                        if (!fa && ia < ea) { if (ga & 1u) fa = true; else ia += width; }
+                        if (!fb && ib < eb) { if (gb & 1u) fb = true; else ib += width; }
+                        width = PROBE;
+                    }
+                    if (fa) {
+                        a.level[va] = nl;
+                        atomicOr(&my_found[(va >> 5) - w0], 1u << (va & 31));
+                        ++my_cnt;
+                        my_deg += (unsigned long long)da;
+                    }
+                    if (fb) {
+                        a.level[vb] = nl;
+                        atomicOr(&my_found[(vb >> 5) - w0], 1u << (vb & 31));
+                        ++my_cnt;
+                        my_deg += (unsigned long long)db;
                     }
                 }
-                const unsigned nbm = __ballot_sync(FULL, found);
-                if (found) a.level[v] = nl;
-                if (lane == 0) {
-                    fn[w] = nbm;
-                    if (nbm) a.visited[w] = vis | nbm;
+                __syncwarp();
+                if ((int)lane < cw && wl < W) {
+                    const unsigned fw = my_found[lane];
+                    fn[wl] = fw;
+                    if (fw) a.visited[wl] = vis | fw;
+                    my_found[lane] = 0;
                 }
-                my_cnt += found;
-                my_deg += found ? (unsigned long long)d : 0ull;
+                __syncwarp();
             }
             const unsigned long long bc = block_reduce_sum(my_cnt, s_red);
             if (threadIdx.x == 0 && bc) atomicAdd(cnt_next, bc);
             const unsigned long long bd = block_reduce_sum(my_deg, s_red);
             if (threadIdx.x == 0 && bd) atomicAdd(deg_next, bd);
-            if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns)) return;
+            if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
+        }
+        if (gtid == 0) {
+            LevelTrace t;
+            t.level = L;
+            t.dir = (td ? 0 : 1) + (td && traced_big ? 2 : 0);
+            t.frontier = nf;
+            t.edges = mf;
+            t.t_ns = globaltimer_ns();
+            ctrl->trace[L < TRACE_CAP - 1 ? L : TRACE_CAP - 1] = t;
         }
         ++L;
     }
 
     if (gtid == 0) {
+        ctrl->t_end = globaltimer_ns();
+        ctrl->trace_len = L < TRACE_CAP ? L : TRACE_CAP;
         BfsOut o;
         o.levels = L;
         o.td_levels = td_levels;
@@ -469,38 +613,52 @@ __global__ void __launch_bounds__(BLOCK) k_bfs(BfsArgs a)
         }
         ctrl->fill = 0;
     }
+    grid_exit(&ctrl->bar);
 }
 
 template <int BLOCK>
 size_t bfs_smem_bytes()
 {
-    return sizeof(int) * ((size_t)(BLOCK / 32) * QCAP + 3 * (size_t)BLOCK + 1);
+    return sizeof(int) * ((size_t)(BLOCK / 32) * QCAP + 2 * (size_t)SEG);
 }
 
-template <int BLOCK>
-cudaError_t bfs_launch(BfsArgs &args, int blocks_per_sm, cudaStream_t st, int &grid_out)
+template <int BLOCK, int MINB>
+cudaError_t bfs_launch(BfsArgs &args, int blocks_per_sm, cudaStream_t st)
 {
     static int sms = 0;
+    static bool attr_set = false;
     const size_t smem = bfs_smem_bytes<BLOCK>();
     cudaError_t e;
-    if (smem > 48 * 1024) {
-        e = cudaFuncSetAttribute(k_bfs<BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (!attr_set) {
+        e = cudaFuncSetAttribute(k_bfs<BLOCK, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
+        attr_set = true;
     }
-    int dev = 0;
-    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-    if (!sms && (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
-        return e;
+    if (!sms) {
+        int dev = 0;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    }
     int occ = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bfs<BLOCK>, BLOCK, smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bfs<BLOCK, MINB>, BLOCK, smem);
     if (e != cudaSuccess) return e;
     if (occ < 1) return cudaErrorInvalidConfiguration;
     const int per = std::max(1, std::min(blocks_per_sm, occ));
-    const int grid = sms * per;
-    grid_out = grid;
     void *kargs[] = {&args};
-    return cudaLaunchCooperativeKernel((const void *)k_bfs<BLOCK>, dim3(grid), dim3(BLOCK), kargs,
+    return cudaLaunchCooperativeKernel((const void *)k_bfs<BLOCK, MINB>, dim3(sms * per), dim3(BLOCK), kargs,
                                        smem, st);
+}
+
+cudaError_t bfs_launch_any(BfsArgs &a, int threads, int bps, cudaStream_t st)
+{
+    switch (threads) {
+    case 256: return bps <= 4 ? bfs_launch<256, 4>(a, bps, st) : bfs_launch<256, 8>(a, bps, st);
+    case 1024: return bps <= 1 ? bfs_launch<1024, 1>(a, bps, st) : bfs_launch<1024, 2>(a, bps, st);
+    default:
+        if (bps <= 2) return bfs_launch<512, 2>(a, bps, st);
+        if (bps == 3) return bfs_launch<512, 3>(a, bps, st);
+        return bfs_launch<512, 4>(a, bps, st);
+    }
 }
 
 }  // namespace
@@ -522,7 +680,7 @@ int bfs_work_alloc(BfsWork &w, int32_t n, std::string &err)
     };
     w.bytes = 0;
     if (!al((void **)&w.level, bytes_int) || !al((void **)&w.visited, W * 4) ||
-        !al((void **)&w.fb0, W * 4) || !al((void **)&w.fb1, W * 4) ||
+        !al((void **)&w.fb0, W * 4) || !al((void **)&w.fb1, W * 4) || !al((void **)&w.fb2, W * 4) ||
         !al((void **)&w.q0, bytes_int) || !al((void **)&w.q1, bytes_int) ||
         !al((void **)&w.big, bytes_int) || !al((void **)&w.roots, bytes_int) ||
         !al((void **)&w.ctrl, sizeof(BfsCtrl))) {
@@ -542,7 +700,7 @@ int bfs_work_alloc(BfsWork &w, int32_t n, std::string &err)
 
 void bfs_work_free(BfsWork &w)
 {
-    void *ps[] = {w.level, w.visited, w.fb0, w.fb1, w.q0, w.q1, w.big, w.roots, w.ctrl, w.d_outs};
+    void *ps[] = {w.level, w.visited, w.fb0, w.fb1, w.fb2, w.q0, w.q1, w.big, w.roots, w.ctrl, w.d_outs};
     for (void *p : ps)
         if (p) cudaFree(p);
     if (w.h_outs) cudaFreeHost(w.h_outs);
@@ -557,7 +715,7 @@ void bfs_work_free(BfsWork &w)
 }
 
 cudaError_t bfs_enqueue(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_roots, int k,
-                        int single_root, int *d_level, BfsOut *slot, cudaStream_t st)
+                        int single_root, int *d_level, BfsOut *slot, cudaStream_t st, bool symmetric)
 {
     BfsArgs a;
     a.n = g.n;
@@ -565,11 +723,12 @@ cudaError_t bfs_enqueue(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, co
     a.m = g.m;
     a.row = g.row;
     a.col = g.col;
-    a.zmask = g.zmask;
+    a.zmask = symmetric ? g.zmask : nullptr;
     a.level = d_level;
     a.visited = w.visited;
-    a.fb0 = w.fb0;
-    a.fb1 = w.fb1;
+    a.fb[0] = w.fb0;
+    a.fb[1] = w.fb1;
+    a.fb[2] = w.fb2;
     a.q0 = w.q0;
     a.q1 = w.q1;
     a.bigl = w.big;
@@ -583,12 +742,7 @@ cudaError_t bfs_enqueue(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, co
     a.big_degree = std::max(32, p.big_degree);
     a.direction = p.direction;
     a.timeout_ns = (unsigned long long)std::max(1, p.timeout_ms) * 1000000ull;
-    int grid = 0;
-    switch (p.threads_per_block) {
-    case 256: return bfs_launch<256>(a, p.blocks_per_sm, st, grid);
-    case 1024: return bfs_launch<1024>(a, p.blocks_per_sm, st, grid);
-    default: return bfs_launch<512>(a, p.blocks_per_sm, st, grid);
-    }
+    return bfs_launch_any(a, p.threads_per_block, p.blocks_per_sm, st);
 }
 
 int bfs_work_reserve_many(BfsWork &w, int k, std::string &err)
@@ -621,13 +775,13 @@ int bfs_work_reserve_many(BfsWork &w, int k, std::string &err)
 }
 
 int bfs_run(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_roots, int k,
-            int single_root, int *d_level, cudaStream_t st, BfsResult &res, std::string &err)
+            int single_root, int *d_level, cudaStream_t st, BfsResult &res, std::string &err, bool symmetric)
 {
     cudaError_t e = cudaEventRecord(w.ev0, st);
-    if (e == cudaSuccess) e = bfs_enqueue(g, p, w, d_roots, k, single_root, d_level, &w.ctrl->out, st);
+    if (e == cudaSuccess) e = bfs_enqueue(g, p, w, d_roots, k, single_root, d_level, &w.ctrl->out, st, symmetric);
     if (e == cudaSuccess) e = cudaEventRecord(w.ev1, st);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(w.h_ctrl, w.ctrl, sizeof(BfsCtrl), cudaMemcpyDeviceToHost, st);
+        e = cudaMemcpyAsync(w.h_ctrl, w.ctrl, offsetof(BfsCtrl, t_entry), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
         err = std::string("BFS launch: ") + cudaGetErrorString(e);

@@ -13,6 +13,16 @@ namespace gbfs {
 
 // Device control block of one traversal context.  Zeroed at allocation; the
 // kernel leaves it zeroed on success (the host re-zeroes it after an error).
+// One row of the per-level trace (thread 0 writes it after the level's barrier).
+struct LevelTrace {
+    int level;                   // frontier index L expanded by this step
+    int dir;                     // 0 top-down, 1 bottom-up, +2 if a grid-split pass ran
+    unsigned long long frontier; // vertices in frontier L
+    unsigned long long edges;    // their out-edges
+    unsigned long long t_ns;     // %globaltimer when the step's last barrier completed
+};
+constexpr int TRACE_CAP = 1024;  // levels kept (the first TRACE_CAP - 1, then the last)
+
 // Results of one traversal, written by the kernel's thread 0.
 struct BfsOut {
     int levels, td_levels, bu_levels, roots;   // roots: distinct vertices at level 0
@@ -29,6 +39,12 @@ struct BfsCtrl {
     unsigned pad1;
     unsigned long long fill;     // bitmap -> queue conversion slots
     BfsOut out;                  // results of the last traversal (default slot)
+    unsigned long long t_entry;  // %globaltimer when CTA 0 started
+    unsigned long long t_start;  // %globaltimer after initialisation
+    unsigned long long t_end;    // %globaltimer when CTA 0 left the level loop
+    int trace_len;
+    int pad3;
+    LevelTrace trace[TRACE_CAP];
 };
 
 // Per-graph traversal workspace (allocated on first use, reused).
@@ -36,8 +52,9 @@ struct BfsWork {
     int32_t n = 0;
     int *level = nullptr;        // n (used when the caller's buffer is on the host)
     unsigned *visited = nullptr; // W
-    unsigned *fb0 = nullptr;     // W frontier bitmaps
+    unsigned *fb0 = nullptr;     // W frontier bitmaps (three, rotating)
     unsigned *fb1 = nullptr;
+    unsigned *fb2 = nullptr;
     int *q0 = nullptr;           // n frontier queues
     int *q1 = nullptr;
     int *big = nullptr;          // n deferred rows
@@ -65,13 +82,15 @@ struct BfsResult {
 
 // Enqueues one (multi-root) BFS of `g` writing levels to d_level (device, n
 // int32) and its results to *slot (device).  d_roots: device array of k
-// roots, or single_root >= 0.  Does not synchronise.
+// roots, or single_root >= 0.  symmetric: in-edges == out-edges (enables the
+// zero-degree shortcut; bottom-up must already be off in `p` otherwise).
+// Does not synchronise.
 cudaError_t bfs_enqueue(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_roots, int k,
-                        int single_root, int *d_level, BfsOut *slot, cudaStream_t st);
+                        int single_root, int *d_level, BfsOut *slot, cudaStream_t st, bool symmetric);
 
 // bfs_enqueue + events + result read-back; synchronises `st`.
 int bfs_run(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_roots, int k,
-            int single_root, int *d_level, cudaStream_t st, BfsResult &res, std::string &err);
+            int single_root, int *d_level, cudaStream_t st, BfsResult &res, std::string &err, bool symmetric);
 
 // Grow the per-launch slots / events of `w` to at least `k`.
 int bfs_work_reserve_many(BfsWork &w, int k, std::string &err);

@@ -111,50 +111,70 @@ enum DevStatus : int {
 
 // ---- bounded grid barrier ---------------------------------------------------
 // Used only by cooperative launches (all CTAs co-resident), so every wait
-// ends once the other CTAs arrive.  Each wait is still bounded by
+// ends once the other CTAs arrive.  Arrival is a one-way release reduction
+// on a counter that only grows during a launch; CTA thread 0 then spins
+// with acquire loads until the counter reaches epoch * gridDim.x (epoch =
+// barriers passed so far, identical in every CTA).  Each wait is bounded by
 // `timeout_ns` of %globaltimer: when it runs out the CTA records
 // DEV_TIMEOUT in *status and returns false; a CTA that sees a non-zero
 // status while waiting also returns false, so every CTA leaves the kernel
-// shortly after the first one gives up.
+// shortly after the first one gives up.  grid_exit() (called once by every
+// CTA at the end of a successful launch) lets the last CTA out reset the
+// counters for the next launch.
 struct GridBarrier {
     unsigned count;
-    unsigned gen;
+    unsigned exit;
 };
 
-__device__ __forceinline__ bool grid_sync(GridBarrier *bar, int *status,
-                                          unsigned long long timeout_ns)
+__device__ __forceinline__ void red_release_add(unsigned *p, unsigned v)
+{
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ bool grid_sync(GridBarrier *bar, int *status, unsigned long long timeout_ns,
+                                          unsigned &epoch)
 {
     __shared__ int s_ok;
     __syncthreads();
+    ++epoch;
     if (threadIdx.x == 0) {
+        const unsigned target = epoch * gridDim.x;
+        red_release_add(&bar->count, 1u);
         int ok = 1;
-        unsigned g = ld_acquire_gpu(&bar->gen);
-        __threadfence();
-        unsigned t = atomicAdd(&bar->count, 1u);
-        if (t == gridDim.x - 1) {
-            bar->count = 0;
-            __threadfence();
-            st_release_gpu(&bar->gen, g + 1);
-        } else {
-            unsigned long long t0 = globaltimer_ns();
-            unsigned spins = 0;
-            while (ld_acquire_gpu(&bar->gen) == g) {
-                if ((++spins & 63u) == 0) {
-                    if (ld_relaxed_i32(status) != DEV_OK) { ok = 0; break; }
-                    if (globaltimer_ns() - t0 > timeout_ns) {
-                        atomicCAS(status, DEV_OK, DEV_TIMEOUT);
-                        ok = 0;
-                        break;
-                    }
+        unsigned long long t0 = 0;
+        unsigned spins = 0;
+        while ((int)(ld_acquire_gpu(&bar->count) - target) < 0) {
+            if ((++spins & 31u) == 0) {
+                if (ld_relaxed_i32(status) != DEV_OK) {
+                    ok = 0;
+                    break;
+                }
+                const unsigned long long now = globaltimer_ns();
+                if (t0 == 0) {
+                    t0 = now;
+                } else if (now - t0 > timeout_ns) {
+                    atomicCAS(status, DEV_OK, DEV_TIMEOUT);
+                    ok = 0;
+                    break;
                 }
             }
         }
-        __threadfence();
-        if (ok && ld_relaxed_i32(status) != DEV_OK) ok = 0;
         s_ok = ok;
     }
     __syncthreads();
     return s_ok != 0;
+}
+
+__device__ __forceinline__ void grid_exit(GridBarrier *bar)
+{
+    if (threadIdx.x == 0) {
+        const unsigned old = atomicAdd(&bar->exit, 1u);
+        if (old == gridDim.x - 1) {
+            bar->count = 0;
+            bar->exit = 0;
+            __threadfence();
+        }
+    }
 }
 
 }  // namespace gbfs

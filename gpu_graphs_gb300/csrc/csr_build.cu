@@ -400,6 +400,108 @@ __global__ void k_validate_csr(const int *__restrict__ row, const int *__restric
     }
 }
 
+// Symmetry check on sorted rows: every (u,v) has (v,u).
+__global__ void k_check_sym(const int *__restrict__ row, const int *__restrict__ col, int n, int *flags)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += stride) {
+        const int b = row[u], e = row[u + 1];
+        for (int i = b; i < e; i++) {
+            const int v = col[i];
+            int lo = row[v], hi = row[v + 1];
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (col[mid] < (int)u) lo = mid + 1; else hi = mid;
+            }
+            if (lo >= row[v + 1] || col[lo] != (int)u) {
+                flags[1] = 1;
+                break;
+            }
+        }
+    }
+}
+
+__global__ void k_check_sorted(const int *__restrict__ row, const int *__restrict__ col, int n, int *flags)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += stride) {
+        const int b = row[u], e = row[u + 1];
+        for (int i = b + 1; i < e; i++)
+            if (col[i - 1] > col[i]) {
+                flags[0] = 1;
+                break;
+            }
+    }
+}
+
+// Hub-first order: each row's highest-degree neighbour (lowest id among
+// ties) is swapped to the row's front, the neighbour a bottom-up step
+// probes first.  One warp per row below HUB_CTA_ROW, one CTA above.
+constexpr int HUB_CTA_ROW = 4096;
+
+__device__ __forceinline__ unsigned long long hub_key(const int *row, int v, int pos)
+{
+    const unsigned d = (unsigned)(row[v + 1] - row[v]);
+    return ((unsigned long long)d << 32) | (unsigned)(0x7fffffff - pos);
+}
+
+__global__ void k_hub_first_warp(const int *__restrict__ row, int n, int *col)
+{
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
+        const int b = row[r], d = row[r + 1] - b;
+        if (d < 2 || d >= HUB_CTA_ROW) continue;
+        unsigned long long best = 0;
+        for (int i = lane_id(); i < d; i += 32) {
+            const unsigned long long k = hub_key(row, col[b + i], i);
+            best = k > best ? k : best;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long y = __shfl_xor_sync(FULL, best, o);
+            best = y > best ? y : best;
+        }
+        const int pos = 0x7fffffff - (int)(best & 0xffffffffu);
+        __syncwarp();
+        if (lane_id() == 0 && pos > 0) {
+            const int t = col[b];
+            col[b] = col[b + pos];
+            col[b + pos] = t;
+        }
+    }
+}
+
+__global__ void k_hub_first_cta(const int *__restrict__ row, int n, int *col)
+{
+    __shared__ unsigned long long s_best[32];
+    for (int64_t r = blockIdx.x; r < n; r += gridDim.x) {
+        const int b = row[r], d = row[r + 1] - b;
+        if (d < HUB_CTA_ROW) continue;
+        unsigned long long best = 0;
+        for (int i = threadIdx.x; i < d; i += blockDim.x) {
+            const unsigned long long k = hub_key(row, col[b + i], i);
+            best = k > best ? k : best;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long y = __shfl_xor_sync(FULL, best, o);
+            best = y > best ? y : best;
+        }
+        if (lane_id() == 0) s_best[threadIdx.x >> 5] = best;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (unsigned w = 1; w < (blockDim.x >> 5); w++) best = s_best[w] > best ? s_best[w] : best;
+            const int pos = 0x7fffffff - (int)(best & 0xffffffffu);
+            if (pos > 0) {
+                const int t = col[b];
+                col[b] = col[b + pos];
+                col[b + pos] = t;
+            }
+        }
+        __syncthreads();
+    }
+}
+
 int grid_for(int64_t work, int threads, int cap = 152 * 16)
 {
     int64_t g = (work + threads - 1) / threads;
@@ -432,7 +534,86 @@ done:
     return rc;
 }
 
+// Sort every row of (row, col) in place (no dedup).  Scratch is allocated
+// and freed here.  Synchronises st.
+int sort_rows_inplace(const int *row, int *col, int32_t n, int64_t m, cudaStream_t st, std::string &err)
+{
+    int rc = GBFS_OK;
+    int *ucnt = nullptr, *med = nullptr, *large = nullptr, *tmp2 = nullptr;
+    unsigned *lcnt = nullptr;
+    int key_bits = 1;
+    const int thr = 256;
+    CK(cudaMalloc(&ucnt, sizeof(int) * ((size_t)n + 1)));
+    CK(cudaMalloc(&med, sizeof(int) * (size_t)n));
+    CK(cudaMalloc(&large, sizeof(int) * (size_t)n));
+    CK(cudaMalloc(&lcnt, 16));
+    CK(cudaMalloc(&tmp2, sizeof(int) * (size_t)std::max<int64_t>(m, 1)));
+    CK(cudaMemsetAsync(lcnt, 0, 16, st));
+    k_bin<<<grid_for(n, BIN_THREADS, 152 * 4), BIN_THREADS, 0, st>>>(row, n, med, large, lcnt);
+    CK(cudaGetLastError());
+    k_sort_small<<<grid_for((int64_t)n * 32, thr), thr, 0, st>>>(row, n, col, 0, ucnt);
+    CK(cudaGetLastError());
+    k_sort_medium<<<152 * 4, MED_THREADS, 0, st>>>(row, med, lcnt, col, 0, ucnt);
+    CK(cudaGetLastError());
+    while (key_bits < 31 && (1LL << key_bits) < (int64_t)n) key_bits++;
+    k_sort_large<<<152 * 2, LARGE_THREADS, 0, st>>>(row, large, lcnt, col, tmp2, key_bits, 0, ucnt);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+done:
+    if (ucnt) cudaFree(ucnt);
+    if (med) cudaFree(med);
+    if (large) cudaFree(large);
+    if (lcnt) cudaFree(lcnt);
+    if (tmp2) cudaFree(tmp2);
+    return rc;
+}
+
 }  // namespace
+
+int csr_check_symmetric(const DeviceCsr &c, cudaStream_t st, bool &sym, std::string &err)
+{
+    int rc = GBFS_OK;
+    int *flags = nullptr, *copy = nullptr;
+    int h[2] = {0, 0};
+    const int grid = grid_for(c.n, 256, 152 * 8);
+    CK(cudaMalloc(&flags, 8));
+    CK(cudaMemsetAsync(flags, 0, 8, st));
+    k_check_sorted<<<grid, 256, 0, st>>>(c.row, c.col, c.n, flags);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h, flags, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    {
+        const int *col = c.col;
+        if (h[0]) {  // unsorted rows: check a sorted copy
+            CK(cudaMalloc(&copy, sizeof(int) * (size_t)std::max<int64_t>(c.m, 1)));
+            CK(cudaMemcpyAsync(copy, c.col, sizeof(int) * (size_t)c.m, cudaMemcpyDeviceToDevice, st));
+            rc = sort_rows_inplace(c.row, copy, c.n, c.m, st, err);
+            if (rc) goto done;
+            col = copy;
+        }
+        k_check_sym<<<grid, 256, 0, st>>>(c.row, col, c.n, flags);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(h, flags, 8, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        sym = h[1] == 0;
+    }
+done:
+    if (flags) cudaFree(flags);
+    if (copy) cudaFree(copy);
+    return rc;
+}
+
+int csr_hub_first(DeviceCsr &c, cudaStream_t st, std::string &err)
+{
+    int rc = GBFS_OK;
+    k_hub_first_warp<<<grid_for((int64_t)c.n * 32, 256), 256, 0, st>>>(c.row, c.n, c.col);
+    CK(cudaGetLastError());
+    k_hub_first_cta<<<152 * 2, 512, 0, st>>>(c.row, c.n, c.col);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+done:
+    return rc;
+}
 
 void csr_free(DeviceCsr &c)
 {

@@ -31,6 +31,12 @@ int csr_build_from_edges(int32_t n, int64_t m, const int *d_src, const int *d_ds
 int csr_adopt(int32_t n, int64_t m, int *d_row, int *d_col, cudaStream_t st, DeviceCsr &out,
               std::string &err);
 
+// in-edges == out-edges?  Rows need not be sorted (a sorted copy is checked).
+int csr_check_symmetric(const DeviceCsr &c, cudaStream_t st, bool &sym, std::string &err);
+
+// Move each row's highest-degree neighbour to the row's front.
+int csr_hub_first(DeviceCsr &c, cudaStream_t st, std::string &err);
+
 void csr_free(DeviceCsr &c);
 
 }  // namespace gbfs

@@ -68,6 +68,7 @@ __global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
     const unsigned lane = lane_id();
     const unsigned long long all = a.k >= 64 ? ~0ull : ((1ull << a.k) - 1ull);
     MsCtrl *ctrl = a.ctrl;
+    unsigned epoch = 0;
 
     // ---- init ----
     for (long long v = gtid; v < n; v += gthreads) {
@@ -90,7 +91,7 @@ __global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
         ctrl->reached = 0;
         ctrl->edges_c = 0;
     }
-    if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns)) return;
+    if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
     if (blockIdx.x == 0 && threadIdx.x < (unsigned)a.k) {
         const int s = a.src[threadIdx.x];
         const unsigned long long bit = 1ull << threadIdx.x;
@@ -99,7 +100,7 @@ __global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
         a.out[(size_t)threadIdx.x * n + s] = 0;
         if (old == 0) atomicAdd(&ctrl->cnt[0], 1ull);
     }
-    if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns)) return;
+    if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
 
     int L = 0, push_levels = 0, pull_levels = 0;
     bool last_pull = false;
@@ -147,7 +148,7 @@ __global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
             if (last_pull) {
                 // the array that becomes nxt still holds an old frontier
                 for (long long u = gtid; u < n; u += gthreads) nxt[u] = 0;
-                if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns)) return;
+                if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
             }
             // phase 1: warp per active frontier vertex
             const long long nwarps = gthreads >> 5;
@@ -168,7 +169,7 @@ __global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
                     }
                 }
             }
-            if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns)) return;
+            if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
             // phase 2: filter, record, clear the old frontier
             for (long long u = gtid; u < n; u += gthreads) {
                 const unsigned long long x = __ldcg(nxt + u);
@@ -188,7 +189,7 @@ __global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
         last_pull = pull;
         const unsigned long long bc = block_reduce_sum(my_cnt, s_red);
         if (threadIdx.x == 0 && bc) atomicAdd(cnt_next, bc);
-        if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns)) return;
+        if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
         ++L;
     }
 
@@ -213,6 +214,7 @@ __global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
         ctrl->pull_levels = pull_levels;
         for (int i = 0; i < 3; i++) ctrl->cnt[i] = 0;
     }
+    grid_exit(&ctrl->bar);
 }
 
 }  // namespace

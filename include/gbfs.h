@@ -60,13 +60,18 @@ const char *gbfs_version(void);
 #define GBFS_DEDUP            2u  /* drop repeated (u,v)                     */
 #define GBFS_DROP_SELF_LOOPS  4u  /* drop (u,u)                              */
 #define GBFS_UNDIRECTED (GBFS_SYMMETRIZE | GBFS_DEDUP | GBFS_DROP_SELF_LOOPS)
+/* Layout option: after the build, each row's highest-degree neighbour is
+ * moved to the row's front (the rest stays ascending).  Bottom-up steps
+ * probe it first, which resolves most unvisited vertices with one probe on
+ * power-law graphs.  Levels are unaffected. */
+#define GBFS_HUB_FIRST        8u
 
 typedef struct gbfs_graph gbfs_graph;
 
 /*
  * Edge list -> device CSR, built on the GPU (degree count, look-back scan,
  * scatter, per-row sort, dedup, compaction).  Rows come out sorted
- * ascending.  src/dst: m int32 vertex ids in [0, n), host or device.
+ * ascending (see GBFS_HUB_FIRST for the one exception).  src/dst: m int32 vertex ids in [0, n), host or device.
  * Replaces csr::csr / csc::csc (which parse a file into host CSR; the file
  * parser is gbfs_read_edge_list below).  Limits: n <= 2^31-2, stored
  * directed edges <= 2^31-1 (GBFS_ERR_TOO_LARGE otherwise).
@@ -163,6 +168,23 @@ int gbfs_bfs(gbfs_graph *g, int32_t source, int32_t *levels_out,
  */
 int gbfs_bfs_many(gbfs_graph *g, const int32_t *sources, int32_t k,
                   int32_t *levels_out, gbfs_stats *stats);
+
+/* Per-level trace of the graph's last single-source or multi-root
+ * traversal (thread 0 stamps %globaltimer after each level's barrier). */
+typedef struct gbfs_level_trace {
+    int32_t level;              /* frontier expanded by this step            */
+    int32_t direction;          /* 0 top-down, 1 bottom-up, 2 top-down with
+                                   a grid-split pass over long rows          */
+    int64_t frontier_vertices;
+    int64_t frontier_edges;     /* out-edges of the frontier                 */
+    double  t_us;               /* end of the step, us after initialisation  */
+} gbfs_level_trace;
+
+/* Copies up to cap rows; returns the number of rows (>= 0) or a status.
+ * Row 0 describes initialisation: level -1, t_us = minus its duration
+ * (from the first CTA's entry to the first level).  The last row (level
+ * -2) marks the end of the level loop, termination check included. */
+int gbfs_last_trace(gbfs_graph *g, gbfs_level_trace *rows, int32_t cap);
 
 /* The CUDA stream (cudaStream_t) the graph's work is ordered on, for
  * callers that record their own events around it. */

@@ -200,3 +200,34 @@ def test_reference_interface_mirror(gb, orc, tmp_path):
         assert b.iteration == int(want.max()) + 1
         assert b.total_edges_traversed == int((want >= 0).sum()) - 1
         assert b.exec_time > 0
+
+
+def test_hub_first_layout(gb, orc):
+    n = 1 << 16
+    src, dst = gb.gen_rmat(16, 16, seed=21)
+    o = orc.csr_build(n, src, dst, orc.UNDIRECTED)
+    g = gb.Graph.from_edges(n, src, dst, gb.UNDIRECTED | gb.HUB_FIRST)
+    row, col = g.csr()
+    assert sorted_rows_equal(row, col, o.row_offset, o.col_idx)
+    deg = np.diff(o.row_offset)
+    for r in np.flatnonzero(deg >= 2)[:2000]:
+        nb = col[row[r]:row[r + 1]]
+        assert deg[nb[0]] == deg[nb].max()
+    rng = np.random.default_rng(3)
+    for s in rng.choice(np.flatnonzero(deg > 0), 4, replace=False):
+        for mode in (0, 1, 2):
+            g.set_params(direction=mode)
+            assert np.array_equal(g.bfs(int(s)), orc.bfs_queue(o, int(s)))
+    # an unsorted symmetric CSR is still recognised as symmetric (bottom-up on)
+    g2 = gb.Graph.from_csr(row, col)
+    _, st = g2.bfs(int(np.argmax(deg)), stats=True)
+    assert st.bu_levels > 0
+    # and an unsorted asymmetric one is not
+    src2, dst2 = gb.gen_er(4000, 12000, seed=22)
+    o2 = orc.csr_build(4000, src2, dst2, 0)
+    rev = o2.col_idx.copy()
+    for r in range(4000):
+        rev[o2.row_offset[r]:o2.row_offset[r + 1]] = rev[o2.row_offset[r]:o2.row_offset[r + 1]][::-1]
+    g3 = gb.Graph.from_csr(o2.row_offset.astype(np.int32), rev)
+    g3.set_params(direction=2)
+    assert np.array_equal(g3.bfs(0), orc.bfs_queue(o2, 0))
