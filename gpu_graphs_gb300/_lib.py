@@ -154,6 +154,7 @@ SIGNATURES = {
     "gbfs_bfs_batch": (C.c_int, [P, P, P, C.POINTER(Stats)]),
     "gbfs_bfs_batch_graphs": (C.c_int, [P, P, I32, P, C.POINTER(Stats)]),
     "gbfs_exclusive_scan_i32": (C.c_int, [P, P, I64, P]),
+    "gbfs_exclusive_scan_i32_noalloc": (C.c_int, [P, P, I64, P]),
     "gbfs_read_edge_list": (C.c_int, [C.c_char_p, I32, PI32, PI64, C.POINTER(PI32), C.POINTER(PI32)]),
     "gbfs_free": (None, [P]),
     "gbfs_graph_save": (C.c_int, [P, C.c_char_p]),

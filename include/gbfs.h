@@ -247,6 +247,28 @@ int gbfs_bfs_batch_graphs(gbfs_graph *const *graphs, const int32_t *sources,
 int gbfs_exclusive_scan_i32(const int32_t *d_in, int64_t *d_out, int64_t n,
                             void *stream);
 
+/*
+ * Allocation-free variant of gbfs_exclusive_scan_i32 (no counterpart in the
+ * reference).  For callers that cannot let a library allocate device memory
+ * while they run: processes that reserve all of HBM up front in their own
+ * pools, loops that must not take the driver's allocation locks (cudaMalloc
+ * and cudaFree may synchronise the device), allocators calling in from their
+ * own critical section.  The look-back scratch is a fixed array compiled
+ * into the library (under 1 MB, held on every GPU that loads the library
+ * until the process exits), so this call makes no cudaMalloc, cudaFree or
+ * other allocating call.  Limits and rules:
+ *   - n <= GBFS_SCAN_NOALLOC_MAX_N, else GBFS_ERR_TOO_LARGE;
+ *   - the first call on a device looks the array's address up once (with
+ *     that device current); make that first call before any stream capture;
+ *   - all calls share the array: calls whose work overlaps on the GPU
+ *     (different streams or threads) race; serialise them;
+ *   - the call synchronises `stream` to report the scan's status.
+ * Same result as gbfs_exclusive_scan_i32 otherwise.
+ */
+#define GBFS_SCAN_NOALLOC_MAX_N (1LL << 26)
+int gbfs_exclusive_scan_i32_noalloc(const int32_t *d_in, int64_t *d_out,
+                                    int64_t n, void *stream);
+
 /* ---- file format and workload generators ------------------------------ */
 /*
  * Read the reference's text format: "n", "m", then whitespace-separated
