@@ -61,6 +61,9 @@ def parse_args():
     ap.add_argument("--params", type=str, default="", help="k=v,... overrides of the traversal parameters")
     ap.add_argument("--layout", choices=["hub-first", "sorted"], default="hub-first",
                     help="CSR row order: sorted ids, or highest-degree neighbour first")
+    ap.add_argument("--no-extra", action="store_true", help="skip the grid and batched measurements")
+    ap.add_argument("--serving", action="store_true", help="also run the serving sweep (32 resident graphs)")
+    ap.add_argument("--grid-side", type=int, default=7000)
     return ap.parse_args()
 
 
@@ -167,6 +170,10 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def log(msg: str) -> None:
+    print(f"[bench] {msg}", file=sys.stderr, flush=True)
+
+
 def measured_peak() -> tuple[float, str]:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -233,6 +240,169 @@ def config_block(args, n: int, m: int) -> dict:
             "vertices": n, "directed_edges": m, "sources_per_step": args.sources,
             "l2": "inputs larger than L2 (CSR ~0.5 GB vs 129 MB L2)"}
 
+
+# ---- the other configurations (extra objects on the same line) --------------------
+
+def measure_grid(side: int, torch) -> dict:
+    """High-diameter grid: one persistent launch vs one launch per level."""
+    import gpu_graphs_gb300 as gb
+    src, dst = gb.gen_grid(side, 0.1, 0.001, 8, seed=1)
+    n = side * side
+    g = gb.Graph.from_edges(n, src, dst, gb.UNDIRECTED)
+    del src, dst
+    row, _ = g.csr()
+    deg = np.diff(row)
+    source = int(pick_sources(deg, 1)[0])
+    out = torch.empty(n, dtype=torch.int32, device="cuda")
+    g.bfs(source, out=out)
+    ref = out.clone()
+    runs = [g.bfs(source, out=out, stats=True)[1] for _ in range(3)]
+    st = runs[-1]
+    t_p = float(np.mean([r.ms for r in runs]))
+    g.set_params(per_level_launch=1)
+    runs_l = [g.bfs(source, out=out, stats=True)[1] for _ in range(2)]
+    same = bool(torch.equal(out, ref))
+    t_l = float(np.mean([r.ms for r in runs_l]))
+    return {"workload": f"grid {side}x{side}, 10% edges dropped, 0.1% extra edges within radius 8",
+            "vertices": n, "directed_edges": int(g.m), "source": source, "levels": int(st.levels),
+            "persistent_ms": round(t_p, 3), "per_level_launch_ms": round(t_l, 3),
+            "per_level_launches": int(runs_l[-1].launches), "speedup_vs_per_level": round(t_l / t_p, 2),
+            "gteps_persistent": round(st.edges_in_component / 2 / (t_p / 1e3) / 1e9, 3),
+            "us_per_level_persistent": round(1e3 * t_p / max(1, st.levels), 3),
+            "levels_identical": same}
+
+
+def measure_batched(torch) -> dict:
+    """64 sources per launch on RMAT scale 20, and 512 small ER graphs in one launch,
+    each against the plain one-query-per-launch BFS on the same GPU."""
+    import gpu_graphs_gb300 as gb
+    res = {}
+    n20 = 1 << 20
+    src, dst = gb.gen_rmat(20, 16, 0.57, 0.19, 0.19, seed=1)
+    g = gb.Graph.from_edges(n20, src, dst, gb.UNDIRECTED | gb.HUB_FIRST)
+    del src, dst
+    row, _ = g.csr()
+    sources = pick_sources(np.diff(row), 64)
+    plain_out = torch.empty((64, n20), dtype=torch.int32, device="cuda")
+    multi_out = torch.empty((64, n20), dtype=torch.int32, device="cuda")
+    g.bfs_many(sources, out=plain_out)
+    g.bfs_multi(sources, out=multi_out)
+    t_plain = min(sum(s.ms for s in g.bfs_many(sources, out=plain_out)[1]) for _ in range(3))
+    t_multi = min(g.bfs_multi(sources, out=multi_out, stats=True)[1].ms for _ in range(3))
+    same = bool(torch.equal(plain_out, multi_out))
+    res["multi_source"] = {
+        "workload": "RMAT scale 20, ef 16, 64 sources per launch (uint64 lane masks)",
+        "plain_ms": round(t_plain, 3), "batched_ms": round(t_multi, 3),
+        "plain_queries_per_s": round(64 / (t_plain / 1e3), 1), "batched_queries_per_s": round(64 / (t_multi / 1e3), 1),
+        "speedup": round(t_plain / t_multi, 2), "levels_identical": same}
+    del plain_out, multi_out, g
+
+    rng = np.random.default_rng(1)
+    sizes = np.exp(rng.uniform(np.log(256), np.log(65536), 512)).astype(np.int64)
+    graphs, srcs = [], []
+    for i, ni in enumerate(sizes):
+        s_, d_ = gb.gen_er(int(ni), int(4 * ni), 1000 + i)
+        deg = np.bincount(np.concatenate([s_, d_]), minlength=int(ni)) - 2 * np.bincount(s_[s_ == d_], minlength=int(ni))
+        graphs.append((int(ni), s_, d_))
+        srcs.append(int(rng.choice(np.flatnonzero(deg > 0))))
+    gs = gb.GraphSet.from_edges(graphs)
+    fused, st = gs.bfs(srcs, stats=True)
+    t_fused = min(gs.bfs(srcs, stats=True)[1].ms for _ in range(3))
+    handles = [gb.Graph.from_edges(ni, s_, d_) for ni, s_, d_ in graphs]
+    douts = [torch.empty(h.n, dtype=torch.int32, device="cuda") for h in handles]
+    for h, o, s0 in zip(handles, douts, srcs):
+        h.bfs(s0, out=o)
+    t_plain = min(sum(h.bfs(s0, out=o, stats=True)[1].ms for h, o, s0 in zip(handles, douts, srcs)) for _ in range(2))
+    same = all(np.array_equal(f, o.cpu().numpy()) for f, o in zip(fused, douts))
+    res["many_graphs"] = {
+        "workload": f"512 ER graphs, n log-uniform in [256, 65536] (total {int(sizes.sum())} vertices), avg degree 8, "
+                    "one source each, one fused launch",
+        "plain_ms": round(t_plain, 3), "fused_ms": round(t_fused, 3),
+        "plain_queries_per_s": round(512 / (t_plain / 1e3), 1), "fused_queries_per_s": round(512 / (t_fused / 1e3), 1),
+        "speedup": round(t_plain / t_fused, 2), "levels_identical": bool(same)}
+    return res
+
+
+def measure_serving(torch, seconds: float = 2.0, fractions=(0.25, 0.5, 0.75, 1.0), max_queries: int = 3000) -> dict:
+    """32 resident graphs, Poisson arrivals at fractions of the measured capacity."""
+    import gpu_graphs_gb300 as gb
+    rng = np.random.default_rng(5)
+    graphs = []
+    for i in range(16):
+        sc = int(rng.integers(12, 23))
+        s_, d_ = gb.gen_rmat(sc, 16, 0.57, 0.19, 0.19, seed=100 + i)
+        graphs.append(gb.Graph.from_edges(1 << sc, s_, d_, gb.UNDIRECTED | gb.HUB_FIRST))
+    for i in range(16):
+        side = int(rng.integers(64, 4097))
+        s_, d_ = gb.gen_grid(side, 0.1, 0.001, 8, seed=200 + i)
+        graphs.append(gb.Graph.from_edges(side * side, s_, d_, gb.UNDIRECTED))
+    del s_, d_
+    log("serving: 32 graphs built")
+    nz = []
+    for g in graphs:
+        r, _ = g.csr()
+        nz.append(np.flatnonzero(np.diff(r) > 0))
+
+    def draw():
+        gi = int(rng.integers(32))
+        return gi, int(rng.choice(nz[gi]))
+
+    # plain: one query per launch, back to back, device-timed
+    plain_ms = sorted(graphs[gi].bfs(s0, stats=True)[1].ms for gi, s0 in (draw() for _ in range(96)))
+    out = {"workload": "32 resident graphs: 16 RMAT scale U{12..22} ef 16, 16 grids side U[64, 4096]; "
+                       "queries pick a graph uniformly and a source uniformly among degree>0 vertices",
+           "plain_one_query_per_launch": {"queries_per_s": round(len(plain_ms) / (sum(plain_ms) / 1e3), 1),
+                                          "p50_ms": round(plain_ms[len(plain_ms) // 2], 3),
+                                          "p99_ms": round(plain_ms[int(0.99 * (len(plain_ms) - 1))], 3)}}
+    log("serving: plain baseline done")
+    sweep = []
+    with gb.Server(mem_budget_bytes=150 << 30, num_slots=4, max_lanes=64, batch_window_us=500) as srv:
+        gids = [srv.add_graph(g) for g in graphs]
+        pools = [[np.empty(g.n, np.int32) for _ in range(64)] for g in graphs]
+        counters = [0] * 32
+
+        def submit():
+            gi, s0 = draw()
+            buf = pools[gi][counters[gi] % 64]
+            counters[gi] += 1
+            return srv.submit(gids[gi], s0, buf)
+
+        # closed loop: everything queued at once -> capacity
+        t0 = time.perf_counter()
+        ts = [submit() for _ in range(1024)]
+        for t in ts:
+            srv.wait(t)
+        capacity = 1024 / (time.perf_counter() - t0)
+        out["capacity_queries_per_s"] = round(capacity, 1)
+        log(f"serving: capacity {capacity:.0f} q/s")
+        for frac in fractions:
+            rate = frac * capacity
+            srv.reset_stats()
+            tickets = []
+            t0 = time.perf_counter()
+            next_t = t0
+            while len(tickets) < max_queries:
+                now = time.perf_counter()
+                if now - t0 >= seconds:
+                    break
+                if now < next_t:
+                    time.sleep(min(next_t - now, 0.0005))
+                    continue
+                tickets.append(submit())
+                next_t += rng.exponential(1.0 / rate)
+            for t in tickets:
+                srv.wait(t)
+            wall = time.perf_counter() - t0
+            st = srv.stats()
+            sweep.append({"offered_queries_per_s": round(rate, 1), "submitted": len(tickets),
+                          "achieved_queries_per_s": round(len(tickets) / wall, 1),
+                          "p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
+                          "mean_batch_lanes": round(st["mean_batch_lanes"], 2)})
+            log(f"serving: {sweep[-1]}")
+        out["peak_hbm_bytes"] = srv.stats()["peak_bytes"]
+    out["sweep"] = sweep
+    out["capacity_vs_plain"] = round(capacity / out["plain_one_query_per_launch"]["queries_per_s"], 2)
+    return out
 
 def main():
     args = parse_args()
@@ -323,6 +493,15 @@ def main():
                "steps": steps_e2e}
         del host, hv
 
+    extra = {}
+    if rank == 0 and not args.no_extra:
+        extra["grid"] = measure_grid(args.grid_side, torch)
+        log("grid done")
+        extra["batched"] = measure_batched(torch)
+        log("batched done")
+    if rank == 0 and args.serving:
+        extra["serving"] = measure_serving(torch)
+
     cpu = None
     if not args.no_cpu and rank == 0:
         threads = args.cpu_threads or (os.cpu_count() or 1)
@@ -345,6 +524,7 @@ def main():
                                  "max": round(max(gteps_each), 2)},
             "levels_td_bu": sorted(set(lvls))[:8],
         }
+        line.update(extra)
         print(json.dumps(line), flush=True)
     dist.close()
 

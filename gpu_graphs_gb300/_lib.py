@@ -163,9 +163,7 @@ SIGNATURES = {
     "gbfs_gen_rmat": (I64, [I32, I32, C.c_double, C.c_double, C.c_double, C.c_uint64, P, P, I64]),
     "gbfs_gen_grid": (I64, [I32, C.c_double, C.c_double, I32, C.c_uint64, P, P, I64]),
     "gbfs_gen_grid_capacity": (I64, [I32, C.c_double]),
-}
-
-OPTIONAL_SIGNATURES = {
+    "gbfs_selftest_wait_timeout": (C.c_int, [I32]),
     "gbfs_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(P)]),
     "gbfs_server_destroy": (None, [P]),
     "gbfs_server_add_graph": (C.c_int, [P, P, PI32]),
@@ -175,6 +173,7 @@ OPTIONAL_SIGNATURES = {
     "gbfs_server_get_stats": (C.c_int, [P, C.POINTER(ServerStats)]),
     "gbfs_server_reset_stats": (None, [P]),
 }
+
 
 
 def _load() -> C.CDLL:
@@ -187,11 +186,6 @@ def _load() -> C.CDLL:
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    for name, (res, args) in OPTIONAL_SIGNATURES.items():
-        fn = getattr(lib, name, None)
-        if fn is not None:
-            fn.restype = res
-            fn.argtypes = args
     return lib
 
 

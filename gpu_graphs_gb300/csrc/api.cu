@@ -371,6 +371,21 @@ extern "C" int gbfs_bfs_many(gbfs_graph *g, const int32_t *sources, int32_t k, i
     const size_t n = (size_t)g->csr.n;
     const bool dev_out = levels_out && is_device_ptr(levels_out);
     const gbfs_params p = effective_params(g);
+    if (p.per_level_launch) {  // host loop per level: one source at a time
+        for (int32_t i = 0; i < k; i++) {
+            BfsResult r;
+            int32_t *dst = levels_out ? levels_out + n * i : nullptr;
+            int *d_level = dev_out ? dst : w.level;
+            rc = bfs_run(g->csr, p, w, nullptr, 1, hsrc[i], d_level, g->stream, r, err, g->symmetric);
+            if (rc) return fail(rc, err);
+            if (dst && !dev_out) {
+                cudaError_t e2 = cudaMemcpy(dst, w.level, sizeof(int) * n, cudaMemcpyDeviceToHost);
+                if (e2 != cudaSuccess) return cuda_fail(e2, "levels D2H");
+            }
+            if (stats) fill_stats(&stats[i], r, 1);
+        }
+        return GBFS_OK;
+    }
     cudaError_t e = cudaSuccess;
     for (int32_t i = 0; i < k && e == cudaSuccess; i++) {
         int *d_level = dev_out ? levels_out + n * i : w.level;

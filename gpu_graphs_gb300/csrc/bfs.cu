@@ -37,12 +37,12 @@
 #include <cstring>
 
 #include "bfs.cuh"
+#include "blockq.cuh"
 
 namespace gbfs {
 
 namespace {
 
-constexpr int QCAP = 256;    // per-warp staging queue entries
 constexpr int SEG = 2048;    // frontier rows expanded edge-balanced per pass
 constexpr int ILP = 4;       // edges in flight per lane in top-down passes
 constexpr int PROBE = 8;     // neighbours probed per step in bottom-up
@@ -66,93 +66,11 @@ struct BfsArgs {
     const int *roots;
     int nroots;
     int single_root;         // >= 0: fast init for one root
+    int resume;              // 1: continue the level loop saved in ctrl->rs
+    int max_steps;           // > 0: leave after this many levels (state saved)
     int alpha, beta, big_degree, direction;
     unsigned long long timeout_ns;
 };
-
-struct WarpQ {
-    int *buf;
-    int n;
-};
-
-__device__ __forceinline__ void wq_flush(WarpQ &q, unsigned long long *cnt, int *out)
-{
-    __syncwarp();
-    if (q.n == 0) return;
-    unsigned long long base = 0;
-    if (lane_id() == 0) base = atomicAdd(cnt, (unsigned long long)q.n);
-    base = __shfl_sync(FULL, base, 0);
-    for (int i = lane_id(); i < q.n; i += 32) out[base + i] = q.buf[i];
-    __syncwarp();
-    q.n = 0;
-}
-
-__device__ __forceinline__ void wq_push(WarpQ &q, bool has, int v, unsigned long long *cnt, int *out)
-{
-    unsigned m = __ballot_sync(FULL, has);
-    if (!m) return;
-    int c = __popc(m);
-    if (q.n + c > QCAP) wq_flush(q, cnt, out);
-    if (has) q.buf[q.n + __popc(m & lanemask_lt())] = v;
-    q.n += c;
-}
-
-// Flush every warp queue of the block with one global atomic (all threads call).
-__device__ __forceinline__ void block_flush(WarpQ &q, unsigned long long *cnt, int *out, int *s_wq,
-                                            unsigned long long *s_base)
-{
-    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    __syncwarp();
-    if (lane_id() == 0) s_wq[w] = q.n;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int tot = 0;
-        for (int i = 0; i < nw; i++) {
-            const int c = s_wq[i];
-            s_wq[i] = tot;
-            tot += c;
-        }
-        *s_base = tot ? atomicAdd(cnt, (unsigned long long)tot) : 0ull;
-    }
-    __syncthreads();
-    const unsigned long long base = *s_base + (unsigned long long)s_wq[w];
-    for (int i = lane_id(); i < q.n; i += 32) out[base + i] = q.buf[i];
-    q.n = 0;
-    __syncthreads();
-}
-
-template <typename T>
-__device__ __forceinline__ T block_reduce_sum(T x, T *s_red)
-{
-    x = warp_sum(x);
-    __syncthreads();
-    if (lane_id() == 0) s_red[threadIdx.x >> 5] = x;
-    __syncthreads();
-    T t = 0;
-    if (threadIdx.x < 32) {
-        t = threadIdx.x < (blockDim.x >> 5) ? s_red[threadIdx.x] : 0;
-        t = warp_sum(t);
-    }
-    return t;  // thread 0
-}
-
-__device__ __forceinline__ int block_excl_scan_int(int x, int *s_warp, int *total)
-{
-    const unsigned lane = lane_id(), warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    int incl = warp_incl_scan(x);
-    __syncthreads();
-    if (lane == 31) s_warp[warp] = incl;
-    __syncthreads();
-    if (warp == 0) {
-        int w = lane < nw ? s_warp[lane] : 0;
-        int wi = warp_incl_scan(w);
-        if (lane < nw) s_warp[lane] = wi - w;
-        if (lane == nw - 1) s_warp[32] = wi;
-    }
-    __syncthreads();
-    *total = s_warp[32];
-    return s_warp[warp] + incl - x;
-}
 
 // Top-down claim of ILP neighbours per lane, all loads and atomics issued
 // before any result is used.  w[j] < 0 means "no edge".  A vertex is won by
@@ -190,9 +108,10 @@ __device__ __forceinline__ void claim_batch(const int (&w)[ILP], const BfsArgs &
     }
 }
 
-// Expand the rows of list[0, cnt) with every warp of the grid, the edges
-// split evenly: each CTA builds the degree prefix of a SEG-row segment in
-// shared memory and warp g takes edges [E*g/W, E*(g+1)/W) of it.
+// Expand the rows of list[0, cnt) with the edges split evenly: each CTA
+// builds the degree prefix of a SEG-row segment in shared memory and warp g
+// of W takes edges [E*g/W, E*(g+1)/W) of it -- all warps of the grid when
+// the list is one segment, the CTA's own warps on its own segments beyond.
 template <int BLOCK>
 __device__ void grid_expand_list(const int *list, int cnt, const BfsArgs &a, int nl, WarpQ &q,
                                  unsigned long long *cnt_next, int *qn, unsigned long long &my_deg, int *s_pre,
@@ -200,9 +119,14 @@ __device__ void grid_expand_list(const int *list, int cnt, const BfsArgs &a, int
 {
     constexpr int PER = SEG / BLOCK;
     const int lane = (int)lane_id();
-    const long long gwarp = ((long long)blockIdx.x * BLOCK + threadIdx.x) >> 5;
-    const long long nwarps = ((long long)gridDim.x * BLOCK) >> 5;
-    for (int seg = 0; seg < cnt; seg += SEG) {
+    // One segment: the grid's warps split its edges.  More: CTA b takes
+    // segments b, b+G, ... and its own warps split each one.
+    const bool one_seg = cnt <= SEG;
+    const long long gwarp = one_seg ? ((long long)blockIdx.x * BLOCK + threadIdx.x) >> 5 : (long long)(threadIdx.x >> 5);
+    const long long nwarps = one_seg ? ((long long)gridDim.x * BLOCK) >> 5 : (long long)(BLOCK / 32);
+    const int seg0 = one_seg ? 0 : (int)blockIdx.x * SEG;
+    const int seg_step = one_seg ? SEG : (int)gridDim.x * SEG;
+    for (int seg = seg0; seg < cnt; seg += seg_step) {
         const int segn = min(SEG, cnt - seg);
         int d[PER];
         int sum = 0;
@@ -309,7 +233,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
     if (gtid == 0) ctrl->t_entry = globaltimer_ns();
 
     // ---- init ----------------------------------------------------------
-    {
+    if (!a.resume) {
         const int root = a.single_root;
         if (((uintptr_t)a.level & 15) == 0) {
             int4 *l4 = (int4 *)a.level;
@@ -350,7 +274,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
             if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
         }
     }
-    if (gtid == 0) ctrl->t_start = globaltimer_ns();
+    if (gtid == 0 && !a.resume) ctrl->t_start = globaltimer_ns();
 
     // ---- level loop ------------------------------------------------------
     // Frontier L lives in queue q[L&1] after a top-down step and in bitmap
@@ -359,7 +283,39 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
     unsigned long long prev_nf = 0, reached = 0, edges_c = 0, roots = 0;
     int L = 0, td_levels = 0, bu_levels = 0;
     bool td = true;
-    for (;;) {
+    if (a.resume) {
+        const BfsResume r = ctrl->rs;
+        m_u = r.m_u;
+        prev_nf = r.prev_nf;
+        reached = r.reached;
+        edges_c = r.edges_c;
+        roots = r.roots;
+        L = r.L;
+        td_levels = r.td_levels;
+        bu_levels = r.bu_levels;
+        td = r.td != 0;
+    }
+    for (int steps = 0;; ++steps) {
+        if (a.max_steps > 0 && steps == a.max_steps) {
+            // per-level-launch mode: park the loop state for the next launch
+            if (gtid == 0) {
+                BfsResume r;
+                r.m_u = m_u;
+                r.prev_nf = prev_nf;
+                r.reached = reached;
+                r.edges_c = edges_c;
+                r.roots = roots;
+                r.L = L;
+                r.td_levels = td_levels;
+                r.bu_levels = bu_levels;
+                r.td = td ? 1 : 0;
+                r.done = 0;
+                r.pad = 0;
+                ctrl->rs = r;
+            }
+            grid_exit(&ctrl->bar);
+            return;
+        }
         const unsigned long long nf = ld_relaxed_u64(&ctrl->cnt[L % 3]);
         const unsigned long long mf = ld_relaxed_u64(&ctrl->deg[L % 3]);
         if (nf == 0) break;
@@ -606,6 +562,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
         o.reached = reached;
         o.edges_c = edges_c;
         *a.out = o;
+        ctrl->rs.done = 1;
         for (int i = 0; i < 3; i++) {
             ctrl->cnt[i] = 0;
             ctrl->deg[i] = 0;
@@ -623,7 +580,7 @@ size_t bfs_smem_bytes()
 }
 
 template <int BLOCK, int MINB>
-cudaError_t bfs_launch(BfsArgs &args, int blocks_per_sm, cudaStream_t st)
+cudaError_t bfs_launch(BfsArgs &args, int blocks_per_sm, cudaStream_t st, int max_ctas)
 {
     static int sms = 0;
     static bool attr_set = false;
@@ -644,24 +601,54 @@ cudaError_t bfs_launch(BfsArgs &args, int blocks_per_sm, cudaStream_t st)
     if (e != cudaSuccess) return e;
     if (occ < 1) return cudaErrorInvalidConfiguration;
     const int per = std::max(1, std::min(blocks_per_sm, occ));
+    int grid = sms * per;
+    if (max_ctas > 0) grid = std::max(1, std::min(grid, max_ctas));
     void *kargs[] = {&args};
-    return cudaLaunchCooperativeKernel((const void *)k_bfs<BLOCK, MINB>, dim3(sms * per), dim3(BLOCK), kargs,
-                                       smem, st);
+    return cudaLaunchCooperativeKernel((const void *)k_bfs<BLOCK, MINB>, dim3(grid), dim3(BLOCK), kargs, smem, st);
 }
 
-cudaError_t bfs_launch_any(BfsArgs &a, int threads, int bps, cudaStream_t st)
+cudaError_t bfs_launch_any(BfsArgs &a, int threads, int bps, cudaStream_t st, int max_ctas)
 {
     switch (threads) {
-    case 256: return bps <= 4 ? bfs_launch<256, 4>(a, bps, st) : bfs_launch<256, 8>(a, bps, st);
-    case 1024: return bps <= 1 ? bfs_launch<1024, 1>(a, bps, st) : bfs_launch<1024, 2>(a, bps, st);
+    case 256: return bps <= 4 ? bfs_launch<256, 4>(a, bps, st, max_ctas) : bfs_launch<256, 8>(a, bps, st, max_ctas);
+    case 1024:
+        return bps <= 1 ? bfs_launch<1024, 1>(a, bps, st, max_ctas) : bfs_launch<1024, 2>(a, bps, st, max_ctas);
     default:
-        if (bps <= 2) return bfs_launch<512, 2>(a, bps, st);
-        if (bps == 3) return bfs_launch<512, 3>(a, bps, st);
-        return bfs_launch<512, 4>(a, bps, st);
+        if (bps <= 2) return bfs_launch<512, 2>(a, bps, st, max_ctas);
+        if (bps == 3) return bfs_launch<512, 3>(a, bps, st, max_ctas);
+        return bfs_launch<512, 4>(a, bps, st, max_ctas);
     }
 }
 
+template <int BLOCK, int MINB>
+int occupancy_ctas(int blocks_per_sm)
+{
+    int dev = 0, sms = 0, occ = 0;
+    if (cudaFuncSetAttribute(k_bfs<BLOCK, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)bfs_smem_bytes<BLOCK>()) != cudaSuccess)
+        return 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bfs<BLOCK, MINB>, BLOCK, bfs_smem_bytes<BLOCK>()) !=
+        cudaSuccess)
+        return 0;
+    return sms * std::max(1, std::min(blocks_per_sm, occ));
+}
+
 }  // namespace
+
+int bfs_max_ctas(const gbfs_params &p)
+{
+    const int bps = p.blocks_per_sm;
+    switch (p.threads_per_block) {
+    case 256: return bps <= 4 ? occupancy_ctas<256, 4>(bps) : occupancy_ctas<256, 8>(bps);
+    case 1024: return bps <= 1 ? occupancy_ctas<1024, 1>(bps) : occupancy_ctas<1024, 2>(bps);
+    default:
+        if (bps <= 2) return occupancy_ctas<512, 2>(bps);
+        if (bps == 3) return occupancy_ctas<512, 3>(bps);
+        return occupancy_ctas<512, 4>(bps);
+    }
+}
 
 int bfs_work_alloc(BfsWork &w, int32_t n, std::string &err)
 {
@@ -715,7 +702,8 @@ void bfs_work_free(BfsWork &w)
 }
 
 cudaError_t bfs_enqueue(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_roots, int k,
-                        int single_root, int *d_level, BfsOut *slot, cudaStream_t st, bool symmetric)
+                        int single_root, int *d_level, BfsOut *slot, cudaStream_t st, bool symmetric, int resume,
+                        int max_steps, int max_ctas)
 {
     BfsArgs a;
     a.n = g.n;
@@ -737,12 +725,14 @@ cudaError_t bfs_enqueue(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, co
     a.roots = d_roots;
     a.nroots = k;
     a.single_root = single_root;
+    a.resume = resume;
+    a.max_steps = max_steps;
     a.alpha = std::max(1, p.alpha);
     a.beta = std::max(1, p.beta);
     a.big_degree = std::max(32, p.big_degree);
     a.direction = p.direction;
     a.timeout_ns = (unsigned long long)std::max(1, p.timeout_ms) * 1000000ull;
-    return bfs_launch_any(a, p.threads_per_block, p.blocks_per_sm, st);
+    return bfs_launch_any(a, p.threads_per_block, p.blocks_per_sm, st, max_ctas);
 }
 
 int bfs_work_reserve_many(BfsWork &w, int k, std::string &err)
@@ -778,7 +768,24 @@ int bfs_run(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_r
             int single_root, int *d_level, cudaStream_t st, BfsResult &res, std::string &err, bool symmetric)
 {
     cudaError_t e = cudaEventRecord(w.ev0, st);
-    if (e == cudaSuccess) e = bfs_enqueue(g, p, w, d_roots, k, single_root, d_level, &w.ctrl->out, st, symmetric);
+    int launches = 1;
+    if (!p.per_level_launch) {
+        if (e == cudaSuccess) e = bfs_enqueue(g, p, w, d_roots, k, single_root, d_level, &w.ctrl->out, st, symmetric);
+    } else {
+        // The reference's shape: one launch per level, then a device->host
+        // read of the loop state before deciding to launch again
+        // (1D Partition/src/gpuBFS.cu:66-100).
+        for (int resume = 0; e == cudaSuccess; resume = 1, ++launches) {
+            e = bfs_enqueue(g, p, w, d_roots, k, single_root, d_level, &w.ctrl->out, st, symmetric, resume, 1);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(&w.h_ctrl->rs, &w.ctrl->rs, sizeof(BfsResume), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) break;
+            int status = 0;
+            e = cudaMemcpy(&status, &w.ctrl->status, sizeof(int), cudaMemcpyDeviceToHost);
+            if (e != cudaSuccess || status != DEV_OK || w.h_ctrl->rs.done) break;
+        }
+    }
     if (e == cudaSuccess) e = cudaEventRecord(w.ev1, st);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(w.h_ctrl, w.ctrl, offsetof(BfsCtrl, t_entry), cudaMemcpyDeviceToHost, st);
@@ -800,7 +807,7 @@ int bfs_run(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_r
     res.levels = h.out.levels;
     res.td_levels = h.out.td_levels;
     res.bu_levels = h.out.bu_levels;
-    res.launches = 1;
+    res.launches = launches;
     res.roots = h.out.roots;
     res.reached = (int64_t)h.out.reached;
     res.edges_c = (int64_t)h.out.edges_c;

@@ -29,6 +29,13 @@ struct BfsOut {
     unsigned long long reached, edges_c;
 };
 
+// Level-loop state kept between launches in per-level-launch mode.
+struct BfsResume {
+    long long m_u;
+    unsigned long long prev_nf, reached, edges_c, roots;
+    int L, td_levels, bu_levels, td, done, pad;
+};
+
 struct BfsCtrl {
     GridBarrier bar;
     int status;
@@ -39,6 +46,7 @@ struct BfsCtrl {
     unsigned pad1;
     unsigned long long fill;     // bitmap -> queue conversion slots
     BfsOut out;                  // results of the last traversal (default slot)
+    BfsResume rs;                // per-level-launch mode: state between launches
     unsigned long long t_entry;  // %globaltimer when CTA 0 started
     unsigned long long t_start;  // %globaltimer after initialisation
     unsigned long long t_end;    // %globaltimer when CTA 0 left the level loop
@@ -86,11 +94,17 @@ struct BfsResult {
 // zero-degree shortcut; bottom-up must already be off in `p` otherwise).
 // Does not synchronise.
 cudaError_t bfs_enqueue(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_roots, int k,
-                        int single_root, int *d_level, BfsOut *slot, cudaStream_t st, bool symmetric);
+                        int single_root, int *d_level, BfsOut *slot, cudaStream_t st, bool symmetric,
+                        int resume = 0, int max_steps = 0, int max_ctas = 0);
 
-// bfs_enqueue + events + result read-back; synchronises `st`.
+// bfs_enqueue + events + result read-back; synchronises `st`.  With
+// p.per_level_launch, one launch per level and a host read-back of the
+// level count after each (the reference's loop shape).
 int bfs_run(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_roots, int k,
             int single_root, int *d_level, cudaStream_t st, BfsResult &res, std::string &err, bool symmetric);
+
+// CTAs of one full-GPU single-source launch with these parameters (0 on error).
+int bfs_max_ctas(const gbfs_params &p);
 
 // Grow the per-launch slots / events of `w` to at least `k`.
 int bfs_work_reserve_many(BfsWork &w, int k, std::string &err);

@@ -390,6 +390,21 @@ __global__ void k_finalize(const int *__restrict__ row, int n, unsigned *zmask, 
     }
 }
 
+__global__ void k_heavy_list(const int *__restrict__ row, int n, int *heavy, unsigned *cnt)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
+        const int64_t v = base + lane_id();
+        const bool h = v < n && row[v + 1] - row[v] > HEAVY_DEGREE;
+        const unsigned m = __ballot_sync(FULL, h);
+        if (!m) continue;
+        unsigned pos = 0;
+        if (lane_id() == 0) pos = atomicAdd(cnt, (unsigned)__popc(m));
+        pos = __shfl_sync(FULL, pos, 0);
+        if (h) heavy[pos + __popc(m & lanemask_lt())] = (int)v;
+    }
+}
+
 __global__ void k_validate_csr(const int *__restrict__ row, const int *__restrict__ col, int n,
                                int64_t m, int *status)
 {
@@ -516,7 +531,7 @@ struct Scratch {
 int finalize(DeviceCsr &out, cudaStream_t st, std::string &err)
 {
     int rc = GBFS_OK;
-    struct Res { unsigned long long nonisolated; int maxdeg; int pad; } h{};
+    struct Res { unsigned long long nonisolated; int maxdeg; unsigned nheavy; } h{};
     Res *d_res = nullptr;
     const int W = (out.n + 31) / 32;
     CK(cudaMalloc(&out.zmask, sizeof(unsigned) * (size_t)W));
@@ -529,6 +544,15 @@ int finalize(DeviceCsr &out, cudaStream_t st, std::string &err)
     CK(cudaStreamSynchronize(st));
     out.max_degree = h.maxdeg;
     out.nonisolated = (int64_t)h.nonisolated;
+    {
+        // heavy-row list (sized by a first count pass folded into k_heavy_list's atomic)
+        CK(cudaMalloc(&out.heavy, sizeof(int) * (size_t)std::max<int64_t>(1, out.n)));
+        k_heavy_list<<<grid_for(out.n, 256), 256, 0, st>>>(out.row, out.n, out.heavy, &d_res->nheavy);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(&h, d_res, sizeof(Res), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        out.nheavy = (int32_t)h.nheavy;
+    }
 done:
     if (d_res) cudaFree(d_res);
     return rc;
@@ -617,6 +641,7 @@ done:
 
 void csr_free(DeviceCsr &c)
 {
+    if (c.heavy) cudaFree(c.heavy);
     if (c.row) cudaFree(c.row);
     if (c.col) cudaFree(c.col);
     if (c.zmask) cudaFree(c.zmask);

@@ -18,7 +18,12 @@ struct DeviceCsr {
     unsigned *zmask = nullptr; // (n+31)/32
     int32_t max_degree = 0;
     int64_t nonisolated = 0;
+    int *heavy = nullptr;      // vertices of out-degree > HEAVY_DEGREE (any order)
+    int32_t nheavy = 0;
 };
+
+// Rows longer than this are walked by a whole warp in multi-source passes.
+constexpr int HEAVY_DEGREE = 64;
 
 // Build from device edge arrays (m entries each).  Returns a GBFS_* status;
 // on failure `err` says why.  All work is ordered on `st`; the call

@@ -2,20 +2,29 @@
 //
 // The reference answers one source per gpuBFS construction
 // (1D Partition/src/gpuBFS.cu:13-116).  Here up to 64 searches on the same
-// graph share every pass over it: per vertex, uint64 lane masks record
-// which searches reached it (vis) and which have it in their frontier
-// (cur / nxt).  A lane's level at v is the step in which its bit first
-// appears in vis[v], written straight into that lane's int32 level row.
-//   push step (sparse frontiers): each frontier vertex ORs its lane mask,
-//       minus lanes already visited, into nxt[u] of every neighbour
-//       (warp per frontier vertex, coalesced row reads); a second phase
-//       filters nxt by vis, records levels and clears the old frontier.
-//   pull step (dense frontiers, symmetric graphs): every vertex with
-//       unreached lanes ORs cur[] over its row until all those lanes are
-//       covered; vertices own their masks, so no atomics.
-// One bounded grid barrier separates pull steps; push steps take two.
+// graph share every pass over it: per vertex, uint64 lane masks record which
+// searches reached it (vis) and which have it in their frontier (F).  A
+// lane's level at v is the step in which its bit first appears in vis[v],
+// written straight into that lane's int32 level row.
+//
+// Work per level follows the frontier, not the graph:
+//   * the active vertices of a level (F != 0) are kept in a queue;
+//   * push step (sparse frontiers): the queue's rows are expanded with the
+//     edges split evenly over every warp of the grid (per-CTA degree prefix
+//     in shared memory); each edge ORs its lanes, minus lanes already at the
+//     neighbour, into N[u] with one atomicOr, and the first writer of N[u]
+//     appends u to a touched list; a second phase walks only the touched
+//     list, filters N by vis, records levels and builds the next queue;
+//   * pull step (dense frontiers, symmetric graphs): every vertex with
+//     unreached lanes ORs F over its row until those lanes are covered --
+//     one thread per light row, a whole warp per row of degree > 64;
+//   * frontier masks and queues rotate by level, and the masks of level L-1
+//     are cleared through their queue during level L, so no pass touches all
+//     n vertices after initialisation except pull steps.
+// Levels are separated by the bounded grid barrier of common.cuh.
 #include <algorithm>
 
+#include "blockq.cuh"
 #include "msbfs.cuh"
 
 namespace gbfs {
@@ -23,32 +32,25 @@ namespace gbfs {
 namespace {
 
 constexpr int MS_BLOCK = 512;
+constexpr int MS_SEG = 2048;                 // queue entries per edge-balanced pass
+constexpr int MS_PER = MS_SEG / MS_BLOCK;    // entries per thread in the prefix
+constexpr int MS_GRID_SEGS = 8;              // queues up to 8 segments are split grid-wide
 
 struct MsArgs {
     int n, n_active, k;
     const int *row, *col;
-    unsigned long long *vis, *fa, *fb;
+    const int *heavy;
+    int nheavy;
+    unsigned long long *vis, *N;
+    unsigned long long *F[3];
+    int *Q[4];
+    int *T;
     int *out;
     const int *src;
     MsCtrl *ctrl;
     int pull_allowed, direction, pull_div;
     unsigned long long timeout_ns;
 };
-
-template <typename T>
-__device__ __forceinline__ T block_reduce_sum(T x, T *s_red)
-{
-    x = warp_sum(x);
-    __syncthreads();
-    if (lane_id() == 0) s_red[threadIdx.x >> 5] = x;
-    __syncthreads();
-    T t = 0;
-    if (threadIdx.x < 32) {
-        t = threadIdx.x < (blockDim.x >> 5) ? s_red[threadIdx.x] : 0;
-        t = warp_sum(t);
-    }
-    return t;
-}
 
 __device__ __forceinline__ void write_levels(int *out, int n, int u, unsigned long long bits, int nl)
 {
@@ -59,22 +61,44 @@ __device__ __forceinline__ void write_levels(int *out, int n, int u, unsigned lo
     }
 }
 
+__device__ __forceinline__ unsigned long long warp_or64(unsigned long long x)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x |= __shfl_xor_sync(FULL, x, o);
+    return x;
+}
+
 __global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
 {
+    extern __shared__ int ms_smem[];
     __shared__ unsigned long long s_red[32];
+    __shared__ unsigned long long s_base;
+    __shared__ int s_warp[33];
+    __shared__ int s_wq[33];
+    constexpr int NW = MS_BLOCK / 32;
+    int *s_q = ms_smem;                                                // NW * QCAP
+    int *s_pre = s_q + NW * QCAP;                                      // MS_SEG
+    int *s_beg = s_pre + MS_SEG;                                       // MS_SEG
+    unsigned long long *s_f = (unsigned long long *)(s_beg + MS_SEG);  // MS_SEG
+
     const int n = a.n;
     const long long gtid = (long long)blockIdx.x * MS_BLOCK + threadIdx.x;
     const long long gthreads = (long long)gridDim.x * MS_BLOCK;
+    const long long gwarp = gtid >> 5;
+    const long long nwarps = gthreads >> 5;
     const unsigned lane = lane_id();
     const unsigned long long all = a.k >= 64 ? ~0ull : ((1ull << a.k) - 1ull);
     MsCtrl *ctrl = a.ctrl;
     unsigned epoch = 0;
+    WarpQ q{s_q + (threadIdx.x >> 5) * QCAP, 0};
 
     // ---- init ----
     for (long long v = gtid; v < n; v += gthreads) {
         a.vis[v] = 0;
-        a.fa[v] = 0;
-        a.fb[v] = 0;
+        a.N[v] = 0;
+        a.F[0][v] = 0;
+        a.F[1][v] = 0;
+        a.F[2][v] = 0;
     }
     {
         const long long total = (long long)a.k * n;
@@ -88,6 +112,8 @@ __global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
         }
     }
     if (gtid == 0) {
+        for (int i = 0; i < 4; i++) ctrl->qcnt[i] = 0;
+        ctrl->tcnt[0] = ctrl->tcnt[1] = 0;
         ctrl->reached = 0;
         ctrl->edges_c = 0;
     }
@@ -96,100 +122,194 @@ __global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
         const int s = a.src[threadIdx.x];
         const unsigned long long bit = 1ull << threadIdx.x;
         atomicOr(&a.vis[s], bit);
-        const unsigned long long old = atomicOr(&a.fa[s], bit);
+        const unsigned long long old = atomicOr(&a.F[0][s], bit);
         a.out[(size_t)threadIdx.x * n + s] = 0;
-        if (old == 0) atomicAdd(&ctrl->cnt[0], 1ull);
+        if (old == 0) a.Q[0][atomicAdd(&ctrl->qcnt[0], 1ull)] = s;
     }
     if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
 
     int L = 0, push_levels = 0, pull_levels = 0;
-    bool last_pull = false;
     for (;;) {
-        const unsigned long long nf = ld_relaxed_u64(&ctrl->cnt[L % 3]);
-        if (nf == 0) break;
+        const unsigned long long nq = ld_relaxed_u64(&ctrl->qcnt[L % 4]);
+        if (nq == 0) break;
+        const unsigned long long nz = L >= 1 ? ld_relaxed_u64(&ctrl->qcnt[(L + 3) % 4]) : 0ull;
         bool pull;
         if (!a.pull_allowed || a.direction == GBFS_DIR_TOPDOWN) pull = false;
         else if (a.direction == GBFS_DIR_BOTTOMUP) pull = true;
-        else pull = (long long)nf * a.pull_div > a.n_active;
-        unsigned long long *cur = (L & 1) ? a.fb : a.fa;
-        unsigned long long *nxt = (L & 1) ? a.fa : a.fb;
-        unsigned long long *cnt_next = &ctrl->cnt[(L + 1) % 3];
+        else pull = (long long)nq * a.pull_div > a.n_active;
+        const unsigned long long *Fc = a.F[L % 3];
+        unsigned long long *Fn = a.F[(L + 1) % 3];
+        unsigned long long *Fz = a.F[(L + 2) % 3];   // level L-1's masks, cleared now
+        const int *Qc = a.Q[L % 4];
+        int *Qn = a.Q[(L + 1) % 4];
+        const int *Qz = a.Q[(L + 3) % 4];            // level L-1's queue
+        unsigned long long *qcnt_next = &ctrl->qcnt[(L + 1) % 4];
         const int nl = L + 1;
-        if (gtid == 0) ctrl->cnt[(L + 2) % 3] = 0;
-        unsigned long long my_cnt = 0;
+        // Q[(L+2)%4] held level L-2; its count was last read during level L-1
+        if (gtid == 0) ctrl->qcnt[(L + 2) % 4] = 0;
+        for (long long i = gtid; i < (long long)nz; i += gthreads) Fz[__ldcg(Qz + i)] = 0;
 
         if (pull) {
             ++pull_levels;
-            for (long long u = gtid; u < n; u += gthreads) {
+            // light rows: one thread per vertex
+            for (long long base = gwarp * 32; base < n; base += nwarps * 32) {
+                const long long u = base + lane;
+                unsigned long long nw = 0;
+                if (u < n) {
+                    const int b = __ldg(a.row + u), e = __ldg(a.row + u + 1);
+                    if (e > b && e - b <= HEAVY_DEGREE) {
+                        const unsigned long long vu = __ldcg(a.vis + u);
+                        const unsigned long long need = ~vu & all;
+                        if (need) {
+                            unsigned long long acc = 0;
+                            for (int i = b; i < e; i += 4) {
+                                const int v0 = __ldg(a.col + i);
+                                const int v1 = i + 1 < e ? __ldg(a.col + i + 1) : v0;
+                                const int v2 = i + 2 < e ? __ldg(a.col + i + 2) : v0;
+                                const int v3 = i + 3 < e ? __ldg(a.col + i + 3) : v0;
+                                acc |= __ldcg(Fc + v0) | __ldcg(Fc + v1) | __ldcg(Fc + v2) | __ldcg(Fc + v3);
+                                if ((acc & need) == need) break;
+                            }
+                            nw = acc & need;
+                            if (nw) {
+                                a.vis[u] = vu | nw;
+                                Fn[u] = nw;
+                                write_levels(a.out, n, (int)u, nw, nl);
+                            }
+                        }
+                    }
+                }
+                wq_push(q, nw != 0, (int)u, qcnt_next, Qn);
+            }
+            // heavy rows: one warp per vertex
+            for (long long h = gwarp; h < a.nheavy; h += nwarps) {
+                const int u = __ldg(a.heavy + h);
                 const unsigned long long vu = __ldcg(a.vis + u);
                 const unsigned long long need = ~vu & all;
-                unsigned long long nw = 0;
+                unsigned long long acc = 0;
                 if (need) {
                     const int b = __ldg(a.row + u), e = __ldg(a.row + u + 1);
-                    unsigned long long acc = 0;
-                    int i = b;
-                    for (; i + 1 < e; i += 2) {
-                        const int v0 = __ldg(a.col + i), v1 = __ldg(a.col + i + 1);
-                        acc |= __ldcg(cur + v0) | __ldcg(cur + v1);
+                    for (int i0 = b; i0 < e; i0 += 128) {
+                        unsigned long long x = 0;
+#pragma unroll
+                        for (int t = 0; t < 4; t++) {
+                            const int i = i0 + t * 32 + (int)lane;
+                            if (i < e) x |= __ldcg(Fc + __ldg(a.col + i));
+                        }
+                        acc |= warp_or64(x);
                         if ((acc & need) == need) break;
                     }
-                    if (i + 1 == e) acc |= __ldcg(cur + __ldg(a.col + i));
-                    nw = acc & need;
-                    if (nw) {
-                        a.vis[u] = vu | nw;
-                        write_levels(a.out, n, (int)u, nw, nl);
-                        ++my_cnt;
-                    }
                 }
-                nxt[u] = nw;
+                const unsigned long long nw = acc & need;
+                if (nw) {
+                    if (lane == 0) {
+                        a.vis[u] = vu | nw;
+                        Fn[u] = nw;
+                    }
+                    if ((nw >> lane) & 1ull) a.out[(size_t)lane * n + u] = nl;
+                    if ((nw >> (lane + 32)) & 1ull) a.out[(size_t)(lane + 32) * n + u] = nl;
+                }
+                wq_push(q, lane == 0 && nw != 0, u, qcnt_next, Qn);
             }
+            block_flush(q, qcnt_next, Qn, s_wq, &s_base);
+            if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
         } else {
             ++push_levels;
-            if (last_pull) {
-                // the array that becomes nxt still holds an old frontier
-                for (long long u = gtid; u < n; u += gthreads) nxt[u] = 0;
-                if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
-            }
-            // phase 1: warp per active frontier vertex
-            const long long nwarps = gthreads >> 5;
-            for (long long base = (gtid >> 5) * 32; base < n; base += nwarps * 32) {
-                const long long v = base + lane;
-                const unsigned long long c = v < n ? __ldcg(cur + v) : 0ull;
-                unsigned act = __ballot_sync(FULL, c != 0);
-                while (act) {
-                    const int src_lane = __ffs(act) - 1;
-                    act &= act - 1;
-                    const unsigned long long cv = __shfl_sync(FULL, c, src_lane);
-                    const int vv = (int)(base + src_lane);
-                    const int b = __ldg(a.row + vv), e = __ldg(a.row + vv + 1);
-                    for (int i = b + (int)lane; i < e; i += 32) {
-                        const int u = __ldg(a.col + i);
-                        const unsigned long long nw = cv & ~__ldcg(a.vis + u);
-                        if (nw && (__ldcg(nxt + u) & nw) != nw) atomicOr(nxt + u, nw);
+            unsigned long long *tcnt = &ctrl->tcnt[L & 1];
+            // phase 1: the queue's edges.  Up to MS_GRID_SEGS segments of
+            // MS_SEG rows: every CTA builds each segment's degree prefix and the
+            // grid's warps split its edges evenly (hub rows of power-law graphs
+            // appear in these short early queues).  Longer queues: CTA b takes
+            // segments b, b+G, ... and its own warps split each one.
+            const bool one_seg = nq <= (unsigned long long)MS_SEG * MS_GRID_SEGS;
+            const long long seg0 = one_seg ? 0 : (long long)blockIdx.x * MS_SEG;
+            const long long seg_step = one_seg ? MS_SEG : (long long)gridDim.x * MS_SEG;
+            const long long wid = one_seg ? gwarp : (long long)(threadIdx.x >> 5);
+            const long long wcount = one_seg ? nwarps : (long long)(MS_BLOCK / 32);
+            for (long long seg = seg0; seg < (long long)nq; seg += seg_step) {
+                const int segn = (int)min((long long)MS_SEG, (long long)nq - seg);
+                int d[MS_PER];
+                int sum = 0;
+#pragma unroll
+                for (int t = 0; t < MS_PER; t++) {
+                    const int j = threadIdx.x * MS_PER + t;
+                    d[t] = 0;
+                    if (j < segn) {
+                        const int v = __ldcg(Qc + seg + j);
+                        const int b = __ldg(a.row + v);
+                        s_beg[j] = b;
+                        s_f[j] = __ldcg(Fc + v);
+                        d[t] = __ldg(a.row + v + 1) - b;
                     }
+                    sum += d[t];
                 }
+                int total;
+                int run = block_excl_scan_int(sum, s_warp, &total);
+#pragma unroll
+                for (int t = 0; t < MS_PER; t++) {
+                    const int j = threadIdx.x * MS_PER + t;
+                    if (j < segn) s_pre[j] = run;
+                    run += d[t];
+                }
+                __syncthreads();
+                const long long lo = (long long)total * wid / wcount;
+                const long long hi = (long long)total * (wid + 1) / wcount;
+                for (long long e0 = lo; e0 < hi; e0 += 64) {
+                    int uu[2];
+                    bool tt[2];
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        const long long e = e0 + h * 32 + lane;
+                        uu[h] = -1;
+                        tt[h] = false;
+                        if (e < hi) {
+                            int l = 0, r = segn - 1;  // max j with s_pre[j] <= e
+                            while (l < r) {
+                                const int mid = (l + r + 1) >> 1;
+                                if (s_pre[mid] <= e) l = mid; else r = mid - 1;
+                            }
+                            const int u = __ldg(a.col + s_beg[l] + (int)(e - s_pre[l]));
+                            // vis may be read stale (it only gains bits: at worst an
+                            // extra atomic); N is cleared between levels by other SMs,
+                            // so it is read from L2
+                            const unsigned long long nw = s_f[l] & ~a.vis[u];
+                            if (nw && (__ldcg(a.N + u) & nw) != nw) {
+                                tt[h] = atomicOr(a.N + u, nw) == 0ull;
+                                uu[h] = u;
+                            }
+                        }
+                    }
+                    wq_push(q, tt[0], uu[0], tcnt, a.T);
+                    wq_push(q, tt[1], uu[1], tcnt, a.T);
+                }
+                __syncthreads();
             }
+            block_flush(q, tcnt, a.T, s_wq, &s_base);
+            if (gtid == 0) ctrl->tcnt[(L + 1) & 1] = 0;
             if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
-            // phase 2: filter, record, clear the old frontier
-            for (long long u = gtid; u < n; u += gthreads) {
-                const unsigned long long x = __ldcg(nxt + u);
-                cur[u] = 0;
-                if (x) {
+            // phase 2: touched vertices only
+            const unsigned long long nt = ld_relaxed_u64(tcnt);
+            for (long long base = gwarp * 32; base < (long long)nt; base += nwarps * 32) {
+                const long long i = base + lane;
+                int u = 0;
+                unsigned long long nw = 0;
+                if (i < (long long)nt) {
+                    u = __ldcg(a.T + i);
+                    const unsigned long long x = __ldcg(a.N + u);
+                    a.N[u] = 0;
                     const unsigned long long vu = __ldcg(a.vis + u);
-                    const unsigned long long nw = x & ~vu;
-                    nxt[u] = nw;
+                    nw = x & ~vu;
                     if (nw) {
                         a.vis[u] = vu | nw;
-                        write_levels(a.out, n, (int)u, nw, nl);
-                        ++my_cnt;
+                        Fn[u] = nw;
+                        write_levels(a.out, n, u, nw, nl);
                     }
                 }
+                wq_push(q, nw != 0, u, qcnt_next, Qn);
             }
+            block_flush(q, qcnt_next, Qn, s_wq, &s_base);
+            if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
         }
-        last_pull = pull;
-        const unsigned long long bc = block_reduce_sum(my_cnt, s_red);
-        if (threadIdx.x == 0 && bc) atomicAdd(cnt_next, bc);
-        if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
         ++L;
     }
 
@@ -212,9 +332,14 @@ __global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
         ctrl->levels = L;
         ctrl->push_levels = push_levels;
         ctrl->pull_levels = pull_levels;
-        for (int i = 0; i < 3; i++) ctrl->cnt[i] = 0;
     }
     grid_exit(&ctrl->bar);
+}
+
+size_t ms_smem_bytes()
+{
+    return sizeof(int) * ((size_t)(MS_BLOCK / 32) * QCAP + 2 * (size_t)MS_SEG) +
+           sizeof(unsigned long long) * (size_t)MS_SEG;
 }
 
 }  // namespace
@@ -233,10 +358,13 @@ int ms_work_alloc(MsWork &w, int32_t n, std::string &err)
         return true;
     };
     w.bytes = 0;
-    const size_t b8 = sizeof(unsigned long long) * (size_t)n;
-    if (!al((void **)&w.vis, b8) || !al((void **)&w.cur, b8) || !al((void **)&w.nxt, b8) ||
-        !al((void **)&w.out, sizeof(int) * (size_t)n * MS_LANES) ||
-        !al((void **)&w.src, sizeof(int) * MS_LANES) || !al((void **)&w.ctrl, sizeof(MsCtrl))) {
+    const size_t b8 = sizeof(unsigned long long) * (size_t)n, b4 = sizeof(int) * (size_t)n;
+    bool ok = al((void **)&w.vis, b8) && al((void **)&w.N, b8) && al((void **)&w.T, b4) &&
+              al((void **)&w.out, b4 * MS_LANES) && al((void **)&w.src, sizeof(int) * MS_LANES) &&
+              al((void **)&w.ctrl, sizeof(MsCtrl));
+    for (int i = 0; ok && i < 3; i++) ok = al((void **)&w.F[i], b8);
+    for (int i = 0; ok && i < 4; i++) ok = al((void **)&w.Q[i], b4);
+    if (!ok) {
         ms_work_free(w);
         return GBFS_ERR_OOM;
     }
@@ -253,7 +381,7 @@ int ms_work_alloc(MsWork &w, int32_t n, std::string &err)
 
 void ms_work_free(MsWork &w)
 {
-    void *ps[] = {w.vis, w.cur, w.nxt, w.out, w.src, w.ctrl};
+    void *ps[] = {w.vis, w.N, w.T, w.out, w.src, w.ctrl, w.F[0], w.F[1], w.F[2], w.Q[0], w.Q[1], w.Q[2], w.Q[3]};
     for (void *p : ps)
         if (p) cudaFree(p);
     if (w.h_ctrl) cudaFreeHost(w.h_ctrl);
@@ -262,8 +390,13 @@ void ms_work_free(MsWork &w)
     w = MsWork{};
 }
 
-int msbfs_run(const DeviceCsr &g, const gbfs_params &p, bool pull_allowed, MsWork &w,
-              const int *d_src, int k, int *d_out, cudaStream_t st, MsResult &res, std::string &err)
+int64_t ms_work_bytes(int64_t n)
+{
+    return n > 0 ? (int64_t)(8 * 5 + 4 * 5 + 4 * MS_LANES) * n + 4096 : 0;
+}
+
+cudaError_t msbfs_enqueue(const DeviceCsr &g, const gbfs_params &p, bool pull_allowed, MsWork &w,
+                          const int *d_src, int k, int *d_out, cudaStream_t st, int max_ctas)
 {
     MsArgs a;
     a.n = g.n;
@@ -271,29 +404,61 @@ int msbfs_run(const DeviceCsr &g, const gbfs_params &p, bool pull_allowed, MsWor
     a.k = k;
     a.row = g.row;
     a.col = g.col;
+    a.heavy = g.heavy;
+    a.nheavy = g.nheavy;
     a.vis = w.vis;
-    a.fa = w.cur;
-    a.fb = w.nxt;
+    a.N = w.N;
+    for (int i = 0; i < 3; i++) a.F[i] = w.F[i];
+    for (int i = 0; i < 4; i++) a.Q[i] = w.Q[i];
+    a.T = w.T;
     a.out = d_out;
     a.src = d_src;
     a.ctrl = w.ctrl;
     a.pull_allowed = pull_allowed ? 1 : 0;
     a.direction = p.direction;
-    a.pull_div = 64;
+    a.pull_div = 16;
     a.timeout_ns = (unsigned long long)std::max(1, p.timeout_ms) * 1000000ull;
-
-    int dev = 0, sms = 0, occ = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_msbfs, MS_BLOCK, 0);
-    if (e == cudaSuccess && occ < 1) e = cudaErrorInvalidConfiguration;
-    if (e == cudaSuccess) e = cudaEventRecord(w.ev0, st);
-    if (e == cudaSuccess) {
-        const int per = std::max(1, std::min(occ, std::max(1, p.blocks_per_sm) * 2));
-        void *kargs[] = {&a};
-        e = cudaLaunchCooperativeKernel((const void *)k_msbfs, dim3(sms * per), dim3(MS_BLOCK), kargs, 0,
-                                        st);
+    static int sms = 0, occ = 0;
+    const size_t smem = ms_smem_bytes();
+    cudaError_t e = cudaSuccess;
+    if (!sms) {
+        int dev = 0;
+        e = cudaFuncSetAttribute(k_msbfs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess) e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_msbfs, MS_BLOCK, smem);
+        if (e != cudaSuccess) {
+            sms = 0;
+            return e;
+        }
+        if (occ < 1) {
+            sms = 0;
+            return cudaErrorInvalidConfiguration;
+        }
     }
+    const int per = std::max(1, std::min(occ, std::max(1, p.blocks_per_sm)));
+    int grid = sms * per;
+    if (max_ctas > 0) grid = std::max(1, std::min(grid, max_ctas));
+    void *kargs[] = {&a};
+    return cudaLaunchCooperativeKernel((const void *)k_msbfs, dim3(grid), dim3(MS_BLOCK), kargs, smem, st);
+}
+
+int ms_max_ctas()
+{
+    int dev = 0, sms = 0, occ = 0;
+    const size_t smem = ms_smem_bytes();
+    if (cudaFuncSetAttribute(k_msbfs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_msbfs, MS_BLOCK, smem) != cudaSuccess) return 0;
+    return sms * occ;
+}
+
+int msbfs_run(const DeviceCsr &g, const gbfs_params &p, bool pull_allowed, MsWork &w, const int *d_src, int k,
+              int *d_out, cudaStream_t st, MsResult &res, std::string &err)
+{
+    cudaError_t e = cudaEventRecord(w.ev0, st);
+    if (e == cudaSuccess) e = msbfs_enqueue(g, p, pull_allowed, w, d_src, k, d_out, st, 0);
     if (e == cudaSuccess) e = cudaEventRecord(w.ev1, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(w.h_ctrl, w.ctrl, sizeof(MsCtrl), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);

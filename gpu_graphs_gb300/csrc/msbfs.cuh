@@ -17,7 +17,8 @@ struct MsCtrl {
     GridBarrier bar;
     int status;
     int pad0;
-    unsigned long long cnt[3];   // vertices that gained a lane, rotating by level
+    unsigned long long qcnt[4];  // active-queue lengths, rotating by level
+    unsigned long long tcnt[2];  // touched-list lengths of push steps
     int levels, push_levels, pull_levels, pad1;
     unsigned long long reached, edges_c;
 };
@@ -25,8 +26,10 @@ struct MsCtrl {
 struct MsWork {
     int32_t n = 0;
     unsigned long long *vis = nullptr;   // n lane masks: lanes that reached v
-    unsigned long long *cur = nullptr;   // n lane masks: v in the lane's frontier
-    unsigned long long *nxt = nullptr;   // n lane masks: next frontier
+    unsigned long long *N = nullptr;     // n push accumulators (zero between levels)
+    unsigned long long *F[3] = {nullptr, nullptr, nullptr};  // frontier masks, rotating
+    int *Q[4] = {nullptr, nullptr, nullptr, nullptr};        // active queues, rotating
+    int *T = nullptr;                    // touched list of a push step
     int *out = nullptr;                  // MS_LANES * n levels (host-bound results)
     int *src = nullptr;                  // MS_LANES sources
     MsCtrl *ctrl = nullptr;
@@ -34,6 +37,9 @@ struct MsWork {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int64_t bytes = 0;
 };
+
+// Device bytes ms_work_alloc takes for n vertices.
+int64_t ms_work_bytes(int64_t n);
 
 int ms_work_alloc(MsWork &w, int32_t n, std::string &err);
 void ms_work_free(MsWork &w);
@@ -44,8 +50,18 @@ struct MsResult {
     int64_t reached = 0, edges_c = 0;
 };
 
-// k <= 64 sources (device array d_src); d_out: k*n int32, row i = levels of
-// source i.  pull_allowed: the graph is symmetric.  Synchronises `st`.
+// Enqueue one launch: k <= 64 sources (device array d_src); d_out: k*n
+// int32, row i = levels of source i; results land in w.ctrl.  max_ctas > 0
+// caps the grid (concurrent launches on several streams must fit on the GPU
+// together, since every launch waits on all of its own CTAs).  No sync.
+cudaError_t msbfs_enqueue(const DeviceCsr &g, const gbfs_params &p, bool pull_allowed, MsWork &w,
+                          const int *d_src, int k, int *d_out, cudaStream_t st, int max_ctas);
+
+// CTAs of one full-GPU multi-source launch (0 on error).
+int ms_max_ctas();
+
+// msbfs_enqueue + read-back; pull_allowed: the graph is symmetric.
+// Synchronises `st`.
 int msbfs_run(const DeviceCsr &g, const gbfs_params &p, bool pull_allowed, MsWork &w,
               const int *d_src, int k, int *d_out, cudaStream_t st, MsResult &res,
               std::string &err);

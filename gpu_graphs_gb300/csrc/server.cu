@@ -1,0 +1,426 @@
+// server.cu -- continuous-batching BFS serving loop over HBM-resident graphs.
+//
+// The reference answers one query per process run (1D Partition/main.cu:10-82).
+// Here a server keeps graphs resident, admits them against an HBM budget and
+// answers queries as they arrive:
+//   * every query joins its graph's FIFO;
+//   * `num_slots` worker threads, each owning a CUDA stream and a 64-lane
+//     multi-source workspace sized for the largest admitted graph, take the
+//     graph whose oldest query has waited longest and pack up to
+//     `max_lanes` of its queries into one multi-source launch (waiting at
+//     most `batch_window_us` for a fuller batch), so queries that arrive
+//     while others are on the GPU join the next free slot;
+//   * slots run concurrently on their streams, each launch capped to
+//     1/num_slots of the GPU's CTAs so all of them fit on the GPU together
+//     (every launch waits on all of its own CTAs);
+//   * results are copied to the caller's buffer before the ticket completes;
+//     latency = submit -> result in place.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "graph.cuh"
+
+using namespace gbfs;
+using Clock = std::chrono::steady_clock;
+
+namespace {
+
+struct SrvQuery {
+    int64_t ticket = 0;
+    int32_t gid = 0, source = 0;
+    int32_t *out = nullptr;
+    Clock::time_point t_submit, t_launch;
+    bool done = false;
+    int status = GBFS_OK;
+    double latency_ms = 0, queue_ms = 0;
+    int lanes = 0;
+};
+
+struct SrvGraph {
+    gbfs_graph *g = nullptr;
+    int64_t bytes = 0;
+    std::deque<std::shared_ptr<SrvQuery>> pending;
+    int inflight = 0;
+};
+
+// 64-lane workspace + single-source workspace (level, 3 bitmaps + visited, 4 int lists)
+int64_t slot_bytes(int64_t n) { return n > 0 ? ms_work_bytes(n) + 4 * n * 5 + n / 2 + (1 << 20) : 0; }
+
+double ms_between(Clock::time_point a, Clock::time_point b)
+{
+    return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+}  // namespace
+
+struct gbfs_server {
+    gbfs_server_config cfg{};
+    int device = 0;
+    int max_ctas = 0;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::map<int32_t, SrvGraph> graphs;
+    int32_t next_gid = 1;
+    std::unordered_map<int64_t, std::shared_ptr<SrvQuery>> queries;
+    int64_t next_ticket = 1;
+    int64_t n_cap = 0;            // slot workspaces cover graphs up to n_cap vertices
+    int64_t resident = 0;         // graph bytes admitted
+    int64_t peak = 0;
+    int busy_slots = 0;
+    bool resizing = false;
+    bool stop = false;
+    // stats
+    std::vector<double> lat;
+    int64_t launches = 0, rejected = 0;
+    double lanes_sum = 0;
+    // slots
+    struct Slot {
+        cudaStream_t st = nullptr;
+        MsWork w;       // 64-lane workspace (batches of two or more)
+        BfsWork bw;     // single-source workspace (batches of one)
+        int64_t cap = 0;
+    };
+    int bfs_ctas = 0;   // CTA cap of a single-source launch in a slot
+    std::vector<Slot> slots;
+    std::vector<std::thread> workers;
+
+    int64_t slots_total(int64_t cap) const { return slot_bytes(cap) * (int64_t)slots.size(); }
+    void worker(int idx);
+};
+
+void gbfs_server::worker(int idx)
+{
+    cudaSetDevice(device);
+    Slot &slot = slots[idx];
+    std::vector<std::shared_ptr<SrvQuery>> batch;
+    std::vector<int32_t> srcs;
+    for (;;) {
+        SrvGraph *sg = nullptr;
+        int32_t gid = 0;
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            for (;;) {
+                if (!resizing) {
+                    // the graph whose oldest query has waited longest
+                    Clock::time_point oldest = Clock::time_point::max();
+                    for (auto &kv : graphs)
+                        if (!kv.second.pending.empty() && kv.second.pending.front()->t_submit < oldest) {
+                            oldest = kv.second.pending.front()->t_submit;
+                            sg = &kv.second;
+                            gid = kv.first;
+                        }
+                    if (sg) {
+                        const auto now = Clock::now();
+                        const double age_us = std::chrono::duration<double, std::micro>(now - oldest).count();
+                        if ((int)sg->pending.size() >= cfg.max_lanes || age_us >= cfg.batch_window_us || stop) break;
+                        cv_work.wait_for(lk, std::chrono::microseconds(
+                                                 std::max(1, (int)(cfg.batch_window_us - age_us))));
+                        sg = nullptr;
+                        continue;
+                    }
+                }
+                if (stop) return;
+                cv_work.wait(lk);
+            }
+            const int k = std::min<int>((int)sg->pending.size(), cfg.max_lanes);
+            batch.clear();
+            srcs.clear();
+            const auto now = Clock::now();
+            for (int i = 0; i < k; i++) {
+                auto q = sg->pending.front();
+                sg->pending.pop_front();
+                q->t_launch = now;
+                q->lanes = k;
+                batch.push_back(q);
+                srcs.push_back(q->source);
+            }
+            sg->inflight += k;
+            ++busy_slots;
+            ++launches;
+            lanes_sum += k;
+        }
+        gbfs_graph *g = sg->g;
+        const int k = (int)batch.size();
+        const size_t n = (size_t)g->csr.n;
+        int status = GBFS_OK;
+        gbfs_params p = g->params;
+        p.timeout_ms = cfg.timeout_ms;
+        if (!g->symmetric) p.direction = GBFS_DIR_TOPDOWN;
+        cudaError_t e = cudaSuccess;
+        int dev_status = DEV_OK;
+        if (k == 1) {
+            // one query: the single-source direction-optimising kernel
+            e = bfs_enqueue(g->csr, p, slot.bw, nullptr, 1, srcs[0], slot.bw.level, &slot.bw.ctrl->out, slot.st,
+                            g->symmetric, 0, 0, bfs_ctas);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(&slot.bw.h_ctrl->status, &slot.bw.ctrl->status, sizeof(int),
+                                    cudaMemcpyDeviceToHost, slot.st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(slot.st);
+            if (e == cudaSuccess) dev_status = slot.bw.h_ctrl->status;
+            if (e == cudaSuccess && dev_status == DEV_OK)
+                e = cudaMemcpyAsync(batch[0]->out, slot.bw.level, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
+                                    slot.st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(slot.st);
+            if (e == cudaSuccess && dev_status != DEV_OK) {
+                cudaMemsetAsync(slot.bw.ctrl, 0, sizeof(BfsCtrl), slot.st);
+                cudaStreamSynchronize(slot.st);
+            }
+        } else {
+            e = cudaMemcpyAsync(slot.w.src, srcs.data(), sizeof(int32_t) * k, cudaMemcpyHostToDevice, slot.st);
+            if (e == cudaSuccess)
+                e = msbfs_enqueue(g->csr, p, g->symmetric, slot.w, slot.w.src, k, slot.w.out, slot.st, max_ctas);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(slot.w.h_ctrl, slot.w.ctrl, sizeof(MsCtrl), cudaMemcpyDeviceToHost, slot.st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(slot.st);
+            if (e == cudaSuccess) dev_status = slot.w.h_ctrl->status;
+            if (e == cudaSuccess && dev_status != DEV_OK) {
+                cudaMemsetAsync(slot.w.ctrl, 0, sizeof(MsCtrl), slot.st);
+                cudaStreamSynchronize(slot.st);
+            } else if (e == cudaSuccess) {
+                for (int i = 0; i < k && e == cudaSuccess; i++)
+                    e = cudaMemcpyAsync(batch[i]->out, slot.w.out + n * i, sizeof(int32_t) * n,
+                                        cudaMemcpyDeviceToHost, slot.st);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(slot.st);
+            }
+        }
+        if (e != cudaSuccess) status = GBFS_ERR_CUDA;
+        else if (dev_status != DEV_OK) status = GBFS_ERR_TIMEOUT;
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            const auto now = Clock::now();
+            for (auto &q : batch) {
+                q->status = status;
+                q->done = true;
+                q->latency_ms = ms_between(q->t_submit, now);
+                q->queue_ms = ms_between(q->t_submit, q->t_launch);
+                if (status == GBFS_OK) lat.push_back(q->latency_ms);
+            }
+            auto it = graphs.find(gid);
+            if (it != graphs.end()) it->second.inflight -= k;
+            --busy_slots;
+        }
+        cv_done.notify_all();
+        cv_work.notify_all();
+    }
+}
+
+extern "C" int gbfs_server_create(const gbfs_server_config *cfg, gbfs_server **out)
+{
+    if (!cfg || !out) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
+    *out = nullptr;
+    if (cfg->num_slots < 1 || cfg->num_slots > 16 || cfg->max_lanes < 1 || cfg->max_lanes > MS_LANES ||
+        cfg->mem_budget_bytes <= 0 || cfg->batch_window_us < 0 || cfg->timeout_ms < 1)
+        return fail(GBFS_ERR_INVALID_ARG, "bad server configuration");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(GBFS_ERR_CUDA, "no CUDA device available");
+    }
+    gbfs_server *s = new (std::nothrow) gbfs_server();
+    if (!s) return fail(GBFS_ERR_OOM, "host allocation failed");
+    s->cfg = *cfg;
+    cudaGetDevice(&s->device);
+    const int total = ms_max_ctas();
+    if (total <= 0) {
+        delete s;
+        return fail(GBFS_ERR_CUDA, "occupancy query failed");
+    }
+    s->max_ctas = std::max(1, total / cfg->num_slots);
+    {
+        gbfs_params dp;
+        gbfs_default_params(&dp);
+        const int tb = bfs_max_ctas(dp);
+        if (tb <= 0) {
+            delete s;
+            return fail(GBFS_ERR_CUDA, "occupancy query failed");
+        }
+        s->bfs_ctas = std::max(1, tb / cfg->num_slots);
+    }
+    s->slots.resize(cfg->num_slots);
+    for (auto &sl : s->slots)
+        if (cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking) != cudaSuccess) {
+            gbfs_server_destroy(s);
+            return fail(GBFS_ERR_CUDA, "cudaStreamCreate");
+        }
+    for (int i = 0; i < cfg->num_slots; i++) s->workers.emplace_back(&gbfs_server::worker, s, i);
+    *out = s;
+    return GBFS_OK;
+}
+
+extern "C" void gbfs_server_destroy(gbfs_server *s)
+{
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+    }
+    s->cv_work.notify_all();
+    for (auto &t : s->workers)
+        if (t.joinable()) t.join();
+    for (auto &sl : s->slots) {
+        if (sl.st) cudaStreamSynchronize(sl.st);
+        ms_work_free(sl.w);
+        bfs_work_free(sl.bw);
+        if (sl.st) cudaStreamDestroy(sl.st);
+    }
+    delete s;
+}
+
+extern "C" int gbfs_server_add_graph(gbfs_server *s, gbfs_graph *g, int32_t *graph_id)
+{
+    if (!s || !g || !graph_id) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
+    std::unique_lock<std::mutex> lk(s->mu);
+    const int64_t gbytes = (int64_t)sizeof(int) * ((int64_t)g->csr.n + 1 + g->csr.m) + 4 * (((int64_t)g->csr.n + 31) / 32);
+    const int64_t new_cap = std::max<int64_t>(s->n_cap, g->csr.n);
+    const int64_t need = s->resident + gbytes + s->slots_total(new_cap);
+    if (need > s->cfg.mem_budget_bytes) {
+        ++s->rejected;
+        return fail(GBFS_ERR_BUDGET, "graph plus slot workspaces exceed the memory budget (" + std::to_string(need) +
+                                         " > " + std::to_string(s->cfg.mem_budget_bytes) + " bytes)");
+    }
+    if (new_cap > s->n_cap) {
+        // grow every slot's workspace once the slots are idle
+        s->resizing = true;
+        s->cv_done.wait(lk, [&] { return s->busy_slots == 0; });
+        std::string err;
+        int rc = GBFS_OK;
+        for (auto &sl : s->slots) {
+            ms_work_free(sl.w);
+            bfs_work_free(sl.bw);
+            rc = ms_work_alloc(sl.w, (int32_t)new_cap, err);
+            if (!rc) rc = bfs_work_alloc(sl.bw, (int32_t)new_cap, err);
+            if (rc) break;
+            sl.cap = new_cap;
+        }
+        s->resizing = false;
+        if (rc) {
+            for (auto &sl : s->slots) {
+                ms_work_free(sl.w);
+                bfs_work_free(sl.bw);
+                sl.cap = 0;
+            }
+            const int64_t old = s->n_cap;
+            s->n_cap = 0;
+            // restore the previous capacity if possible
+            for (auto &sl : s->slots)
+                if (old > 0 && ms_work_alloc(sl.w, (int32_t)old, err) == GBFS_OK &&
+                    bfs_work_alloc(sl.bw, (int32_t)old, err) == GBFS_OK)
+                    sl.cap = old;
+            s->n_cap = old;
+            s->cv_work.notify_all();
+            return fail(rc, "slot workspace: " + err);
+        }
+        s->n_cap = new_cap;
+    }
+    const int32_t gid = s->next_gid++;
+    SrvGraph sg;
+    sg.g = g;
+    sg.bytes = gbytes;
+    s->graphs.emplace(gid, std::move(sg));
+    s->resident += gbytes;
+    s->peak = std::max(s->peak, s->resident + s->slots_total(s->n_cap));
+    *graph_id = gid;
+    s->cv_work.notify_all();
+    return GBFS_OK;
+}
+
+extern "C" int gbfs_server_remove_graph(gbfs_server *s, int32_t graph_id)
+{
+    if (!s) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->graphs.find(graph_id);
+    if (it == s->graphs.end()) return fail(GBFS_ERR_NOT_FOUND, "unknown graph id");
+    if (!it->second.pending.empty() || it->second.inflight > 0)
+        return fail(GBFS_ERR_INVALID_ARG, "graph has queries pending or in flight");
+    s->resident -= it->second.bytes;
+    s->graphs.erase(it);
+    return GBFS_OK;
+}
+
+extern "C" int gbfs_server_submit(gbfs_server *s, int32_t graph_id, int32_t source, int32_t *levels_out,
+                                  int64_t *ticket)
+{
+    if (!s || !levels_out || !ticket) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
+    auto q = std::make_shared<SrvQuery>();
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (s->stop) return fail(GBFS_ERR_SHUTDOWN, "server is shutting down");
+        auto it = s->graphs.find(graph_id);
+        if (it == s->graphs.end()) return fail(GBFS_ERR_NOT_FOUND, "unknown graph id");
+        if (source < 0 || source >= it->second.g->csr.n) return fail(GBFS_ERR_INVALID_ARG, "source outside [0, n)");
+        q->ticket = s->next_ticket++;
+        q->gid = graph_id;
+        q->source = source;
+        q->out = levels_out;
+        q->t_submit = Clock::now();
+        it->second.pending.push_back(q);
+        s->queries.emplace(q->ticket, q);
+        *ticket = q->ticket;
+    }
+    s->cv_work.notify_one();
+    return GBFS_OK;
+}
+
+extern "C" int gbfs_server_wait(gbfs_server *s, int64_t ticket, int32_t timeout_ms, gbfs_query_info *info)
+{
+    if (!s) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->queries.find(ticket);
+    if (it == s->queries.end()) return fail(GBFS_ERR_NOT_FOUND, "unknown ticket");
+    auto q = it->second;
+    auto pred = [&] { return q->done; };
+    if (timeout_ms < 0) s->cv_done.wait(lk, pred);
+    else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred))
+        return fail(GBFS_ERR_TIMEOUT, "query still pending");
+    if (info) {
+        info->latency_ms = q->latency_ms;
+        info->queue_ms = q->queue_ms;
+        info->batch_lanes = q->lanes;
+        info->status = q->status;
+    }
+    s->queries.erase(it);
+    return q->status == GBFS_OK ? GBFS_OK : fail(q->status, "query failed on the device");
+}
+
+extern "C" int gbfs_server_get_stats(gbfs_server *s, gbfs_server_stats *st)
+{
+    if (!s || !st) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    *st = gbfs_server_stats{};
+    st->completed = (int64_t)s->lat.size();
+    st->launches = s->launches;
+    st->rejected = s->rejected;
+    st->resident_bytes = s->resident;
+    st->peak_bytes = s->peak;
+    st->mean_batch_lanes = s->launches ? s->lanes_sum / (double)s->launches : 0;
+    if (!s->lat.empty()) {
+        std::vector<double> v = s->lat;
+        std::sort(v.begin(), v.end());
+        auto pct = [&](double p) { return v[std::min(v.size() - 1, (size_t)(p * (double)(v.size() - 1) + 0.5))]; };
+        st->p50_ms = pct(0.50);
+        st->p99_ms = pct(0.99);
+        st->max_ms = v.back();
+        double sum = 0;
+        for (double x : v) sum += x;
+        st->mean_ms = sum / (double)v.size();
+    }
+    return GBFS_OK;
+}
+
+extern "C" void gbfs_server_reset_stats(gbfs_server *s)
+{
+    if (!s) return;
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->lat.clear();
+    s->launches = 0;
+    s->lanes_sum = 0;
+}

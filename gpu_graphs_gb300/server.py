@@ -19,8 +19,6 @@ class Server:
 
     def __init__(self, mem_budget_bytes: int, num_slots: int = 4, max_lanes: int = 64,
                  batch_window_us: int = 200, timeout_ms: int = 2000):
-        if not hasattr(lib, "gbfs_server_create"):
-            raise RuntimeError("libgbfs.so was built without the serving loop")
         cfg = _lib.ServerConfig(int(mem_budget_bytes), int(num_slots), int(max_lanes), int(batch_window_us),
                                 int(timeout_ms))
         self._h = C.c_void_p()
@@ -39,9 +37,9 @@ class Server:
         self._graphs.pop(gid, None)
 
     def submit(self, gid: int, source: int, out: np.ndarray | None = None) -> int:
-        g = self._graphs[gid]
+        g = self._graphs.get(gid)
         if out is None:
-            out = np.empty(g.n, np.int32)
+            out = np.empty(g.n if g is not None else 1, np.int32)
         t = C.c_int64()
         check(lib.gbfs_server_submit(self._h, int(gid), int(source), C.c_void_p(out.ctypes.data), C.byref(t)),
               "gbfs_server_submit")

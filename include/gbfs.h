@@ -269,6 +269,15 @@ int gbfs_exclusive_scan_i32(const int32_t *d_in, int64_t *d_out, int64_t n,
 int gbfs_exclusive_scan_i32_noalloc(const int32_t *d_in, int64_t *d_out,
                                     int64_t n, void *stream);
 
+/*
+ * Failure-detection self-test (no counterpart in the reference): launches a
+ * two-CTA cooperative kernel whose second CTA never reaches the grid
+ * barrier, so the first CTA's bounded wait runs out after timeout_ms
+ * (1..10000).  Returns GBFS_ERR_TIMEOUT when the wait reported its timeout
+ * and the context is still usable; any other status is a failure.
+ */
+int gbfs_selftest_wait_timeout(int32_t timeout_ms);
+
 /* ---- file format and workload generators ------------------------------ */
 /*
  * Read the reference's text format: "n", "m", then whitespace-separated
@@ -307,6 +316,56 @@ int64_t gbfs_gen_grid(int32_t side, double drop, double extra, int32_t radius,
                       uint64_t seed, int32_t *src, int32_t *dst, int64_t cap);
 /* Upper bound of gbfs_gen_grid's edge count for the same arguments. */
 int64_t gbfs_gen_grid_capacity(int32_t side, double extra);
+
+/* ---- serving loop (no counterpart in the reference) --------------------
+ * A server keeps graphs resident, admits them against an HBM budget and
+ * answers BFS queries with continuous batching: same-graph queries that
+ * arrive while others run are packed into 64-lane multi-source launches as
+ * slots (streams with their own workspace) free up. */
+typedef struct gbfs_server gbfs_server;
+
+typedef struct gbfs_server_config {
+    int64_t mem_budget_bytes;   /* HBM the server may hold: graphs + slots  */
+    int32_t num_slots;          /* concurrent in-flight launches (streams)  */
+    int32_t max_lanes;          /* sources per multi-source launch (<= 64)  */
+    int32_t batch_window_us;    /* wait this long for same-graph arrivals   */
+    int32_t timeout_ms;         /* device wait bound for each launch        */
+} gbfs_server_config;
+
+typedef struct gbfs_query_info {
+    double  latency_ms;         /* submit -> result in the caller's buffer  */
+    double  queue_ms;           /* submit -> launch                         */
+    int32_t batch_lanes;        /* sources that shared the launch           */
+    int32_t status;             /* GBFS_OK or the launch's error            */
+} gbfs_query_info;
+
+typedef struct gbfs_server_stats {
+    int64_t completed;
+    int64_t launches;
+    int64_t rejected;           /* admissions refused by the budget         */
+    double  p50_ms, p99_ms, mean_ms, max_ms;
+    double  mean_batch_lanes;
+    int64_t resident_bytes;     /* graphs admitted                          */
+    int64_t peak_bytes;         /* high-water mark of graphs + slots        */
+} gbfs_server_stats;
+
+int gbfs_server_create(const gbfs_server_config *cfg, gbfs_server **out);
+/* Stops admission, drains in-flight work, frees slots (not the graphs). */
+void gbfs_server_destroy(gbfs_server *s);
+/* Admit a resident graph (borrowed; must outlive the server or be removed).
+ * GBFS_ERR_BUDGET if its CSR plus one slot's workspace does not fit. */
+int gbfs_server_add_graph(gbfs_server *s, gbfs_graph *g, int32_t *graph_id);
+int gbfs_server_remove_graph(gbfs_server *s, int32_t graph_id);
+/* Queue one query; levels_out (host, n int32) is written before completion
+ * is reported.  Returns at once with a ticket. */
+int gbfs_server_submit(gbfs_server *s, int32_t graph_id, int32_t source,
+                       int32_t *levels_out, int64_t *ticket);
+/* Wait for a ticket (timeout_ms < 0: forever).  GBFS_ERR_TIMEOUT if it is
+ * still pending; otherwise the query's own status.  info nullable. */
+int gbfs_server_wait(gbfs_server *s, int64_t ticket, int32_t timeout_ms,
+                     gbfs_query_info *info);
+int gbfs_server_get_stats(gbfs_server *s, gbfs_server_stats *st);
+void gbfs_server_reset_stats(gbfs_server *s);
 
 #ifdef __cplusplus
 }

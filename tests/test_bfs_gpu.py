@@ -81,7 +81,7 @@ def _check_against_oracle(gb, orc, n, src, dst, sources, flags=None, params=None
 @pytest.mark.parametrize("params", [
     {}, {"threads_per_block": 256, "blocks_per_sm": 4}, {"threads_per_block": 1024, "blocks_per_sm": 1},
     {"alpha": 2, "beta": 4}, {"alpha": 96, "beta": 96}, {"big_degree": 32}, {"big_degree": 4096},
-    {"direction": 1}, {"direction": 2},
+    {"direction": 1}, {"direction": 2}, {"per_level_launch": 1},
 ])
 def test_rmat18_param_grid(gb, orc, params):
     src, dst = gb.gen_rmat(18, 16, seed=2)
@@ -95,9 +95,13 @@ def test_grid_high_diameter(gb, orc):
     side = 400
     src, dst = gb.gen_grid(side, 0.1, 0.001, 8, seed=3)
     g, o = _check_against_oracle(gb, orc, side * side, src, dst, [0, side * side // 2 + 7])
-    _, st = g.bfs(0, stats=True)
+    want, st = g.bfs(0, stats=True)
     assert st.levels > side  # hundreds of levels in one persistent launch
     assert st.launches == 1
+    g.set_params(per_level_launch=1)  # the reference's shape: a launch per level
+    got, st2 = g.bfs(0, stats=True)
+    assert np.array_equal(got, want)
+    assert st2.launches == st.levels + 1 and st2.levels == st.levels
 
 
 def test_er_and_directed(gb, orc):

@@ -1,0 +1,98 @@
+"""GPU: the continuous-batching server (results alone == results in the mix)."""
+from __future__ import annotations
+
+import threading
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _graphs(gb, orc):
+    specs = [("rmat", 14, 1), ("rmat", 12, 2), ("grid", 60, 3), ("er", 3000, 4)]
+    out = []
+    for kind, size, seed in specs:
+        if kind == "rmat":
+            s, d = gb.gen_rmat(size, 16, seed=seed)
+            n = 1 << size
+        elif kind == "grid":
+            s, d = gb.gen_grid(size, 0.1, 0.001, 8, seed=seed)
+            n = size * size
+        else:
+            s, d = gb.gen_er(size, 3 * size, seed)
+            n = size
+        g = gb.Graph.from_edges(n, s, d)
+        out.append((g, orc.csr_build(n, s, d, orc.UNDIRECTED)))
+    return out
+
+
+def test_server_mix_equals_alone(gb, orc):
+    graphs = _graphs(gb, orc)
+    with gb.Server(mem_budget_bytes=8 << 30, num_slots=3, max_lanes=64, batch_window_us=300) as srv:
+        gids = [srv.add_graph(g) for g, _ in graphs]
+        rng = np.random.default_rng(5)
+        plan = [(int(rng.integers(len(graphs))), None) for _ in range(400)]
+        plan = [(gi, int(rng.integers(graphs[gi][0].n))) for gi, _ in plan]
+        tickets = [None] * len(plan)
+
+        def submitter(lo, hi):
+            for i in range(lo, hi):
+                gi, s = plan[i]
+                tickets[i] = srv.submit(gids[gi], s)
+
+        ths = [threading.Thread(target=submitter, args=(k * 100, (k + 1) * 100)) for k in range(4)]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+        lanes = []
+        for i, (gi, s) in enumerate(plan):
+            got, info = srv.wait(tickets[i])
+            assert info.status == 0
+            lanes.append(info.batch_lanes)
+            want = orc.bfs_queue(graphs[gi][1], s)
+            assert np.array_equal(got, want), (gi, s)
+        st = srv.stats()
+        assert st["completed"] == len(plan)
+        assert st["mean_batch_lanes"] > 1.0          # queries were batched
+        assert max(lanes) > 1
+        assert st["p99_ms"] >= st["p50_ms"] > 0
+        # the same query alone gives the same levels
+        gi, s = plan[0]
+        t = srv.submit(gids[gi], s)
+        alone, info = srv.wait(t)
+        assert info.batch_lanes == 1
+        assert np.array_equal(alone, orc.bfs_queue(graphs[gi][1], s))
+
+
+def test_server_budget_and_errors(gb, orc):
+    graphs = _graphs(gb, orc)
+    g = graphs[0][0]
+    with gb.Server(mem_budget_bytes=1 << 20, num_slots=2) as srv:
+        with pytest.raises(gb.GbfsError) as e:
+            srv.add_graph(g)
+        assert e.value.code == gb._lib.ERR_BUDGET
+        assert srv.stats()["rejected"] == 1
+    with gb.Server(mem_budget_bytes=4 << 30, num_slots=2) as srv:
+        gid = srv.add_graph(g)
+        with pytest.raises(gb.GbfsError) as e:
+            srv.submit(gid + 100, 0)
+        assert e.value.code == gb._lib.ERR_NOT_FOUND
+        with pytest.raises(gb.GbfsError) as e:
+            srv.submit(gid, g.n)
+        assert e.value.code == gb._lib.ERR_INVALID_ARG
+        t = srv.submit(gid, 0)
+        srv.wait(t)
+        srv.remove_graph(gid)
+        with pytest.raises(gb.GbfsError):
+            srv.remove_graph(gid)
+
+
+def test_bounded_wait_reports_timeout_and_context_survives(gb, orc):
+    lib = gb._lib.lib
+    assert lib.gbfs_selftest_wait_timeout(50) == gb._lib.ERR_TIMEOUT
+    # the context is still usable afterwards
+    s, d = gb.gen_er(1000, 3000, 1)
+    g = gb.Graph.from_edges(1000, s, d)
+    assert np.array_equal(g.bfs(0), orc.bfs_queue(orc.csr_build(1000, s, d, orc.UNDIRECTED), 0))
