@@ -174,6 +174,16 @@ def log(msg: str) -> None:
     print(f"[bench] {msg}", file=sys.stderr, flush=True)
 
 
+def profiled_traffic() -> int | None:
+    """DRAM bytes per k_bfs launch from the committed ncu summary, if present."""
+    p = ROOT / "profiles" / "k_bfs_rmat22.md"
+    if p.exists():
+        for ln in p.read_text().splitlines():
+            if ln.startswith("traffic_bytes_per_launch ="):
+                return int(ln.split("=")[1])
+    return None
+
+
 def measured_peak() -> tuple[float, str]:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -470,7 +480,8 @@ def main():
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                 "bytes_per_launch": int(b_alg / launches), "mean_launch_us": round(1e3 * float(np.mean(launch_ms)), 2),
-                "traffic": None}
+                "traffic": profiled_traffic() if args.scale == 22 else None,
+                "traffic_source": "ncu dram__bytes_read+write per launch, profiles/k_bfs_rmat22.md"}
     gteps_each = [(e / 2) / (t / 1e3) / 1e9 for e, t in zip(launch_ec, launch_ms)]
 
     # e2e through the C ABI with pinned host output buffers
