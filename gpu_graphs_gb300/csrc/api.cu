@@ -326,6 +326,7 @@ static int run_bfs_locked(gbfs_graph *g, const int *d_roots, int k, int single_r
     const bool dev_out = is_device_ptr(levels_out);
     int *d_level = dev_out ? levels_out : g->work.level;
     gbfs_params p = effective_params(g);
+    g->last_multi = false;
     rc = bfs_run(g->csr, p, g->work, d_roots, k, single_root, d_level, g->stream, res, err, g->symmetric);
     if (rc) return fail(rc, err);
     if (!dev_out) {
@@ -427,35 +428,52 @@ extern "C" int gbfs_last_trace(gbfs_graph *g, gbfs_level_trace *rows, int32_t ca
 {
     if (!g || (cap > 0 && !rows) || cap < 0) return fail(GBFS_ERR_INVALID_ARG, "bad argument");
     std::lock_guard<std::mutex> lk(g->mu);
-    if (!g->work.ctrl) return 0;
-    BfsCtrl *h = g->work.h_ctrl;
-    cudaError_t e = cudaMemcpyAsync(&h->t_entry, &g->work.ctrl->t_entry,
-                                    sizeof(BfsCtrl) - offsetof(BfsCtrl, t_entry), cudaMemcpyDeviceToHost, g->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
-    if (e != cudaSuccess) return cuda_fail(e, "trace D2H");
-    const int len = std::min<int>(std::min<int>(h->trace_len, TRACE_CAP), cap - 2);
+    unsigned long long t_entry, t_start, t_end;
+    int trace_len;
+    const LevelTrace *trace;
+    cudaError_t e;
+    if (g->last_multi) {
+        if (!g->ms.ctrl) return 0;
+        MsCtrl *h = g->ms.h_ctrl;
+        e = cudaMemcpyAsync(&h->t_entry, &g->ms.ctrl->t_entry, sizeof(MsCtrl) - offsetof(MsCtrl, t_entry),
+                            cudaMemcpyDeviceToHost, g->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&h->trace_len, &g->ms.ctrl->trace_len, sizeof(int),
+                                                  cudaMemcpyDeviceToHost, g->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "trace D2H");
+        t_entry = h->t_entry; t_start = h->t_start; t_end = h->t_end; trace_len = h->trace_len; trace = h->trace;
+    } else {
+        if (!g->work.ctrl) return 0;
+        BfsCtrl *h = g->work.h_ctrl;
+        e = cudaMemcpyAsync(&h->t_entry, &g->work.ctrl->t_entry, sizeof(BfsCtrl) - offsetof(BfsCtrl, t_entry),
+                            cudaMemcpyDeviceToHost, g->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "trace D2H");
+        t_entry = h->t_entry; t_start = h->t_start; t_end = h->t_end; trace_len = h->trace_len; trace = h->trace;
+    }
+    const int len = std::min<int>(std::min<int>(trace_len, TRACE_CAP), cap - 2);
     if (len < 0) return 0;
-    // row 0: initialisation (level -1), from CTA 0's entry to the end of init
+    // row 0: initialisation (level -1), from CTA 0's entry to the first level
     rows[0].level = -1;
     rows[0].direction = -1;
     rows[0].frontier_vertices = 0;
     rows[0].frontier_edges = 0;
-    rows[0].t_us = -(double)(h->t_start - h->t_entry) / 1000.0;
+    rows[0].t_us = -(double)(t_start - t_entry) / 1000.0;
     rows++;
     for (int i = 0; i < len; i++) {
-        const LevelTrace &t = h->trace[i];
+        const LevelTrace &t = trace[i];
         rows[i].level = t.level;
         rows[i].direction = t.dir;
         rows[i].frontier_vertices = (int64_t)t.frontier;
         rows[i].frontier_edges = (int64_t)t.edges;
-        rows[i].t_us = (double)(t.t_ns - h->t_start) / 1000.0;
+        rows[i].t_us = (double)(t.t_ns - t_start) / 1000.0;
     }
     // last row: the end of the level loop (the termination check included)
     rows[len].level = -2;
     rows[len].direction = -2;
     rows[len].frontier_vertices = 0;
     rows[len].frontier_edges = 0;
-    rows[len].t_us = (double)(h->t_end - h->t_start) / 1000.0;
+    rows[len].t_us = (double)(t_end - t_start) / 1000.0;
     return len + 2;
 }
 
@@ -507,6 +525,7 @@ extern "C" int gbfs_bfs_multi(gbfs_graph *g, const int32_t *sources, int32_t k, 
     const size_t n = (size_t)g->csr.n;
     gbfs_params p = g->params;
     MsResult tot;
+    g->last_multi = true;
     for (int32_t b0 = 0; b0 < k; b0 += MS_LANES) {
         const int kk = std::min<int>(MS_LANES, k - b0);
         cudaError_t e = cudaMemcpyAsync(g->ms.src, hsrc.data() + b0, sizeof(int) * kk, cudaMemcpyHostToDevice,

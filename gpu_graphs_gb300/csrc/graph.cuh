@@ -23,6 +23,7 @@ struct gbfs_graph {
     cudaStream_t stream = nullptr;
     int device = 0;
     bool symmetric = false;      // in-edges == out-edges (bottom-up allowed)
+    bool last_multi = false;     // the last traversal was multi-source (trace source)
     std::mutex mu;
     // graph set cached by gbfs_bfs_batch_graphs (keyed by the handle list)
     std::vector<const gbfs_graph *> batch_key;

@@ -23,6 +23,7 @@
 //     n vertices after initialisation except pull steps.
 // Levels are separated by the bounded grid barrier of common.cuh.
 #include <algorithm>
+#include <cstddef>
 
 #include "blockq.cuh"
 #include "msbfs.cuh"
@@ -68,7 +69,34 @@ __device__ __forceinline__ unsigned long long warp_or64(unsigned long long x)
     return x;
 }
 
-__global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
+// Warp-wide level writes for 32 consecutive vertices u = base + lane: the loop
+// runs over the union of the lanes' masks, so each store instruction covers
+// one output row and coalesces.  All 32 threads call it.
+__device__ __forceinline__ void write_levels_warp(int *out, int n, long long u, unsigned long long bits, int val)
+{
+    unsigned long long any = warp_or64(bits);
+    while (any) {
+        const int j = __ffsll((long long)any) - 1;
+        if ((bits >> j) & 1ull) out[(size_t)j * n + u] = val;
+        any &= any - 1ull;
+    }
+}
+
+// OR x over the block, then one atomicOr into *dst (all threads call).
+__device__ __forceinline__ void or_into(unsigned long long x, unsigned long long *dst, unsigned long long *s_red)
+{
+    x = warp_or64(x);
+    __syncthreads();
+    if (lane_id() == 0) s_red[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        unsigned long long t = threadIdx.x < (blockDim.x >> 5) ? s_red[threadIdx.x] : 0ull;
+        t = warp_or64(t);
+        if (threadIdx.x == 0 && t) atomicOr(dst, t);
+    }
+}
+
+__global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
 {
     extern __shared__ int ms_smem[];
     __shared__ unsigned long long s_red[32];
@@ -91,6 +119,7 @@ __global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
     MsCtrl *ctrl = a.ctrl;
     unsigned epoch = 0;
     WarpQ q{s_q + (threadIdx.x >> 5) * QCAP, 0};
+    if (gtid == 0) ctrl->t_entry = globaltimer_ns();
 
     // ---- init ----
     for (long long v = gtid; v < n; v += gthreads) {
@@ -100,19 +129,14 @@ __global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
         a.F[1][v] = 0;
         a.F[2][v] = 0;
     }
-    {
-        const long long total = (long long)a.k * n;
-        if (((uintptr_t)a.out & 15) == 0) {
-            int4 *o4 = (int4 *)a.out;
-            const long long t4 = total >> 2;
-            for (long long i = gtid; i < t4; i += gthreads) o4[i] = make_int4(-1, -1, -1, -1);
-            for (long long i = (t4 << 2) + gtid; i < total; i += gthreads) a.out[i] = -1;
-        } else {
-            for (long long i = gtid; i < total; i += gthreads) a.out[i] = -1;
-        }
-    }
+    // out is not pre-filled: every (lane, vertex) entry is written exactly
+    // once, with its level when reached, or with -1 after the last level
     if (gtid == 0) {
-        for (int i = 0; i < 4; i++) ctrl->qcnt[i] = 0;
+        for (int i = 0; i < 4; i++) {
+            ctrl->qcnt[i] = 0;
+            ctrl->alive[i] = 0;
+        }
+        ctrl->alive[0] = all;
         ctrl->tcnt[0] = ctrl->tcnt[1] = 0;
         ctrl->reached = 0;
         ctrl->edges_c = 0;
@@ -127,11 +151,15 @@ __global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
         if (old == 0) a.Q[0][atomicAdd(&ctrl->qcnt[0], 1ull)] = s;
     }
     if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
+    if (gtid == 0) ctrl->t_start = globaltimer_ns();
 
     int L = 0, push_levels = 0, pull_levels = 0;
     for (;;) {
         const unsigned long long nq = ld_relaxed_u64(&ctrl->qcnt[L % 4]);
         if (nq == 0) break;
+        // only lanes with a frontier at level L can reach anything at L+1
+        const unsigned long long live = ld_relaxed_u64(&ctrl->alive[L % 4]) & all;
+        unsigned long long my_or = 0;   // lanes this thread puts in the next frontier
         const unsigned long long nz = L >= 1 ? ld_relaxed_u64(&ctrl->qcnt[(L + 3) % 4]) : 0ull;
         bool pull;
         if (!a.pull_allowed || a.direction == GBFS_DIR_TOPDOWN) pull = false;
@@ -146,7 +174,10 @@ __global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
         unsigned long long *qcnt_next = &ctrl->qcnt[(L + 1) % 4];
         const int nl = L + 1;
         // Q[(L+2)%4] held level L-2; its count was last read during level L-1
-        if (gtid == 0) ctrl->qcnt[(L + 2) % 4] = 0;
+        if (gtid == 0) {
+            ctrl->qcnt[(L + 2) % 4] = 0;
+            ctrl->alive[(L + 2) % 4] = 0;
+        }
         for (long long i = gtid; i < (long long)nz; i += gthreads) Fz[__ldcg(Qz + i)] = 0;
 
         if (pull) {
@@ -159,7 +190,7 @@ __global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
                     const int b = __ldg(a.row + u), e = __ldg(a.row + u + 1);
                     if (e > b && e - b <= HEAVY_DEGREE) {
                         const unsigned long long vu = __ldcg(a.vis + u);
-                        const unsigned long long need = ~vu & all;
+                        const unsigned long long need = ~vu & live;
                         if (need) {
                             unsigned long long acc = 0;
                             for (int i = b; i < e; i += 4) {
@@ -174,18 +205,21 @@ __global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
                             if (nw) {
                                 a.vis[u] = vu | nw;
                                 Fn[u] = nw;
-                                write_levels(a.out, n, (int)u, nw, nl);
+                                my_or |= nw;
                             }
                         }
                     }
                 }
+                // level writes: one store per discovered lane, coalesced over the
+                // warp's 32 consecutive vertices
+                write_levels_warp(a.out, n, u, nw, nl);
                 wq_push(q, nw != 0, (int)u, qcnt_next, Qn);
             }
             // heavy rows: one warp per vertex
             for (long long h = gwarp; h < a.nheavy; h += nwarps) {
                 const int u = __ldg(a.heavy + h);
                 const unsigned long long vu = __ldcg(a.vis + u);
-                const unsigned long long need = ~vu & all;
+                const unsigned long long need = ~vu & live;
                 unsigned long long acc = 0;
                 if (need) {
                     const int b = __ldg(a.row + u), e = __ldg(a.row + u + 1);
@@ -205,6 +239,7 @@ __global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
                     if (lane == 0) {
                         a.vis[u] = vu | nw;
                         Fn[u] = nw;
+                        my_or |= nw;
                     }
                     if ((nw >> lane) & 1ull) a.out[(size_t)lane * n + u] = nl;
                     if ((nw >> (lane + 32)) & 1ull) a.out[(size_t)(lane + 32) * n + u] = nl;
@@ -212,6 +247,7 @@ __global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
                 wq_push(q, lane == 0 && nw != 0, u, qcnt_next, Qn);
             }
             block_flush(q, qcnt_next, Qn, s_wq, &s_base);
+            or_into(my_or, &ctrl->alive[(L + 1) % 4], s_red);
             if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
         } else {
             ++push_levels;
@@ -222,12 +258,15 @@ __global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
             // appear in these short early queues).  Longer queues: CTA b takes
             // segments b, b+G, ... and its own warps split each one.
             const bool one_seg = nq <= (unsigned long long)MS_SEG * MS_GRID_SEGS;
-            const long long seg0 = one_seg ? 0 : (long long)blockIdx.x * MS_SEG;
-            const long long seg_step = one_seg ? MS_SEG : (long long)gridDim.x * MS_SEG;
+            // CTA segments sized so every CTA gets about one
+            const long long cta_seg = min((long long)MS_SEG, max(32LL, ((long long)nq + gridDim.x - 1) / gridDim.x));
+            const long long seg_len = one_seg ? MS_SEG : cta_seg;
+            const long long seg0 = one_seg ? 0 : (long long)blockIdx.x * seg_len;
+            const long long seg_step = one_seg ? MS_SEG : (long long)gridDim.x * seg_len;
             const long long wid = one_seg ? gwarp : (long long)(threadIdx.x >> 5);
             const long long wcount = one_seg ? nwarps : (long long)(MS_BLOCK / 32);
             for (long long seg = seg0; seg < (long long)nq; seg += seg_step) {
-                const int segn = (int)min((long long)MS_SEG, (long long)nq - seg);
+                const int segn = (int)min(seg_len, (long long)nq - seg);
                 int d[MS_PER];
                 int sum = 0;
 #pragma unroll
@@ -302,25 +341,47 @@ __global__ void __launch_bounds__(MS_BLOCK) k_msbfs(MsArgs a)
                     if (nw) {
                         a.vis[u] = vu | nw;
                         Fn[u] = nw;
+                        my_or |= nw;
                         write_levels(a.out, n, u, nw, nl);
                     }
                 }
                 wq_push(q, nw != 0, u, qcnt_next, Qn);
             }
             block_flush(q, qcnt_next, Qn, s_wq, &s_base);
+            or_into(my_or, &ctrl->alive[(L + 1) % 4], s_red);
             if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
+        }
+        if (gtid == 0) {
+            LevelTrace t;
+            t.level = L;
+            t.dir = pull ? 1 : 0;
+            t.frontier = nq;
+            t.edges = 0;
+            t.t_ns = globaltimer_ns();
+            ctrl->trace[L < TRACE_CAP - 1 ? L : TRACE_CAP - 1] = t;
         }
         ++L;
     }
+    if (gtid == 0) {
+        ctrl->t_end = globaltimer_ns();
+        ctrl->trace_len = L < TRACE_CAP ? L : TRACE_CAP;
+    }
 
-    // per-lane totals for GTEPS: reached vertices and their out-edges
+    // -1 for the lanes that never reached a vertex; per-lane totals for GTEPS
     unsigned long long r = 0, ec = 0;
-    for (long long u = gtid; u < n; u += gthreads) {
-        const int c = __popcll(__ldcg(a.vis + u) & all);
-        if (c) {
-            r += c;
-            ec += (unsigned long long)c * (unsigned long long)(__ldg(a.row + u + 1) - __ldg(a.row + u));
+    for (long long base = gwarp * 32; base < n; base += nwarps * 32) {
+        const long long u = base + lane;
+        unsigned long long miss = 0;
+        if (u < n) {
+            const unsigned long long vu = __ldcg(a.vis + u) & all;
+            miss = ~vu & all;
+            const int c = __popcll(vu);
+            if (c) {
+                r += c;
+                ec += (unsigned long long)c * (unsigned long long)(__ldg(a.row + u + 1) - __ldg(a.row + u));
+            }
         }
+        write_levels_warp(a.out, n, u, miss, -1);
     }
     const unsigned long long br = block_reduce_sum(r, s_red);
     const unsigned long long be = block_reduce_sum(ec, s_red);
@@ -460,7 +521,7 @@ int msbfs_run(const DeviceCsr &g, const gbfs_params &p, bool pull_allowed, MsWor
     cudaError_t e = cudaEventRecord(w.ev0, st);
     if (e == cudaSuccess) e = msbfs_enqueue(g, p, pull_allowed, w, d_src, k, d_out, st, 0);
     if (e == cudaSuccess) e = cudaEventRecord(w.ev1, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(w.h_ctrl, w.ctrl, sizeof(MsCtrl), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(w.h_ctrl, w.ctrl, offsetof(MsCtrl, t_entry), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
         err = std::string("multi-source BFS launch: ") + cudaGetErrorString(e);

@@ -7,6 +7,7 @@
 #include <string>
 
 #include "common.cuh"
+#include "bfs.cuh"
 #include "csr_build.cuh"
 
 namespace gbfs {
@@ -19,8 +20,11 @@ struct MsCtrl {
     int pad0;
     unsigned long long qcnt[4];  // active-queue lengths, rotating by level
     unsigned long long tcnt[2];  // touched-list lengths of push steps
-    int levels, push_levels, pull_levels, pad1;
+    unsigned long long alive[4]; // lanes with a non-empty frontier, rotating by level
+    int levels, push_levels, pull_levels, trace_len;
     unsigned long long reached, edges_c;
+    unsigned long long t_entry, t_start, t_end;
+    LevelTrace trace[TRACE_CAP];   // per level: frontier = active vertices
 };
 
 struct MsWork {

@@ -16,6 +16,7 @@
 //   * results are copied to the caller's buffer before the ticket completes;
 //     latency = submit -> result in place.
 #include <algorithm>
+#include <cstddef>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -179,7 +180,7 @@ void gbfs_server::worker(int idx)
             if (e == cudaSuccess)
                 e = msbfs_enqueue(g->csr, p, g->symmetric, slot.w, slot.w.src, k, slot.w.out, slot.st, max_ctas);
             if (e == cudaSuccess)
-                e = cudaMemcpyAsync(slot.w.h_ctrl, slot.w.ctrl, sizeof(MsCtrl), cudaMemcpyDeviceToHost, slot.st);
+                e = cudaMemcpyAsync(slot.w.h_ctrl, slot.w.ctrl, offsetof(MsCtrl, t_entry), cudaMemcpyDeviceToHost, slot.st);
             if (e == cudaSuccess) e = cudaStreamSynchronize(slot.st);
             if (e == cudaSuccess) dev_status = slot.w.h_ctrl->status;
             if (e == cudaSuccess && dev_status != DEV_OK) {

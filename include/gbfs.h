@@ -169,8 +169,10 @@ int gbfs_bfs(gbfs_graph *g, int32_t source, int32_t *levels_out,
 int gbfs_bfs_many(gbfs_graph *g, const int32_t *sources, int32_t k,
                   int32_t *levels_out, gbfs_stats *stats);
 
-/* Per-level trace of the graph's last single-source or multi-root
- * traversal (thread 0 stamps %globaltimer after each level's barrier). */
+/* Per-level trace of the graph's last traversal, single-source,
+ * multi-root or multi-source (thread 0 stamps %globaltimer after each
+ * level's barrier; for multi-source, frontier_vertices counts vertices
+ * active in any lane, direction 0 push / 1 pull, frontier_edges 0). */
 typedef struct gbfs_level_trace {
     int32_t level;              /* frontier expanded by this step            */
     int32_t direction;          /* 0 top-down, 1 bottom-up, 2 top-down with

@@ -101,3 +101,26 @@ def test_exclusive_scan(gb, orc, n):
     assert np.array_equal(got, orc.exclusive_scan(x))
     got2 = gb.exclusive_scan(torch.from_numpy(x).cuda()).cpu().numpy()  # scratch reuse
     assert np.array_equal(got2, got)
+
+
+def test_autotune_keeps_levels_and_caches(gb, orc):
+    import time
+    n = 1 << 16
+    src, dst = gb.gen_rmat(16, 16, seed=31)
+    o = orc.csr_build(n, src, dst, orc.UNDIRECTED)
+    g = gb.Graph.from_edges(n, src, dst)
+    deg = np.diff(o.row_offset)
+    sources = [int(x) for x in np.flatnonzero(deg > 0)[:3]]
+    t0 = time.perf_counter()
+    p = g.autotune(sources)
+    t_first = time.perf_counter() - t0
+    assert p.threads_per_block in (256, 512, 1024) and p.alpha >= 1 and p.beta >= 1
+    assert g.params.as_dict() == p.as_dict()
+    for s in sources + [int(np.argmax(deg))]:
+        assert np.array_equal(g.bfs(s), orc.bfs_queue(o, s))
+    # same size/degree signature: answered from the cache
+    g2 = gb.Graph.from_edges(n, src, dst)
+    t0 = time.perf_counter()
+    p2 = g2.autotune(sources)
+    assert time.perf_counter() - t0 < t_first
+    assert p2.as_dict() == p.as_dict()
