@@ -162,6 +162,23 @@ class Graph:
         check(lib.gbfs_bfs(self._h, int(source), po, C.byref(st)), "gbfs_bfs")
         return (out, st) if stats else out
 
+    def bfs_parents(self, source: int, levels=None, parents=None, stats: bool = False):
+        """Levels and canonical BFS-tree parents (smallest neighbour one level
+        closer; -1 for the source and unreached vertices).  levels/parents:
+        host arrays or CUDA tensors of n int32.  Returns (levels, parents[, stats])."""
+        if levels is None:
+            levels = np.empty(self.n, np.int32)
+        if parents is None:
+            parents = np.empty(self.n, np.int32)
+        for name, a in (("levels", levels), ("parents", parents)):
+            if not _is_torch_cuda(a) and (a.dtype != np.int32 or not a.flags.c_contiguous or a.size != self.n):
+                raise ValueError(f"{name} must be a contiguous int32 array of n entries")
+        pl = _ptr_i32(levels, "levels")[0] if _is_torch_cuda(levels) else C.c_void_p(levels.ctypes.data)
+        pp = _ptr_i32(parents, "parents")[0] if _is_torch_cuda(parents) else C.c_void_p(parents.ctypes.data)
+        st = Stats()
+        check(lib.gbfs_bfs_parents(self._h, int(source), pl, pp, C.byref(st)), "gbfs_bfs_parents")
+        return (levels, parents, st) if stats else (levels, parents)
+
     def bfs_many(self, sources: Sequence[int], out=None, keep: bool = True):
         """One launch per source, back to back on the graph's stream.
 

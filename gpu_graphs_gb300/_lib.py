@@ -142,6 +142,7 @@ SIGNATURES = {
     "gbfs_set_params": (C.c_int, [P, C.POINTER(Params)]),
     "gbfs_autotune": (C.c_int, [P, P, I32, C.POINTER(Params)]),
     "gbfs_bfs": (C.c_int, [P, I32, P, C.POINTER(Stats)]),
+    "gbfs_bfs_parents": (C.c_int, [P, I32, P, P, C.POINTER(Stats)]),
     "gbfs_bfs_multiroot": (C.c_int, [P, P, I32, P, C.POINTER(Stats)]),
     "gbfs_bfs_many": (C.c_int, [P, P, I32, P, P]),
     "gbfs_graph_stream": (C.c_void_p, [P]),

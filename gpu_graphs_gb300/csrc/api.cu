@@ -12,6 +12,7 @@
 
 #include "../../include/gbfs.h"
 #include "graph.cuh"
+#include "parents.cuh"
 #include "scan.cuh"
 
 namespace gbfs {
@@ -350,6 +351,38 @@ extern "C" int gbfs_bfs(gbfs_graph *g, int32_t source, int32_t *levels_out, gbfs
     return GBFS_OK;
 }
 
+extern "C" int gbfs_bfs_parents(gbfs_graph *g, int32_t source, int32_t *levels_out, int32_t *parents_out,
+                                gbfs_stats *stats)
+{
+    if (!g || !parents_out) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
+    if (source < 0 || source >= g->csr.n) return fail(GBFS_ERR_INVALID_ARG, "source outside [0, n)");
+    std::lock_guard<std::mutex> lk(g->mu);
+    std::string err;
+    int rc = bfs_work_alloc(g->work, g->csr.n, err);
+    if (rc) return fail(rc, err);
+    BfsWork &w = g->work;
+    const size_t n = (size_t)g->csr.n;
+    const bool dev_lv = levels_out && is_device_ptr(levels_out);
+    const bool dev_par = is_device_ptr(parents_out);
+    int *d_level = dev_lv ? levels_out : w.level;
+    // the traversal's queues are free once it has finished
+    int *d_parent = dev_par ? parents_out : w.q0;
+    gbfs_params p = effective_params(g);
+    g->last_multi = false;
+    BfsResult res;
+    rc = bfs_run(g->csr, p, w, nullptr, 1, source, d_level, g->stream, res, err, g->symmetric);
+    if (rc) return fail(rc, err);
+    cudaError_t e = parents_enqueue(g->csr, g->symmetric, d_level, d_parent, g->stream);
+    if (e == cudaSuccess && !dev_par)
+        e = cudaMemcpyAsync(parents_out, d_parent, sizeof(int) * n, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess && levels_out && !dev_lv)
+        e = cudaMemcpyAsync(levels_out, d_level, sizeof(int) * n, cudaMemcpyDeviceToHost, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "parents");
+    fill_stats(stats, res, 1);
+    return GBFS_OK;
+}
+
 extern "C" int gbfs_bfs_many(gbfs_graph *g, const int32_t *sources, int32_t k, int32_t *levels_out,
                              gbfs_stats *stats)
 {
@@ -520,6 +553,8 @@ extern "C" int gbfs_bfs_multi(gbfs_graph *g, const int32_t *sources, int32_t k, 
     std::lock_guard<std::mutex> lk(g->mu);
     std::string err;
     int rc = ms_work_alloc(g->ms, g->csr.n, err);
+    if (rc) return fail(rc, err);
+    rc = ms_prepare(g->csr, g->stream, err);
     if (rc) return fail(rc, err);
     const bool dev_out = is_device_ptr(levels_out);
     const size_t n = (size_t)g->csr.n;

@@ -71,6 +71,16 @@ __device__ __forceinline__ void st_release_u64(unsigned long long *p, unsigned l
     asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
+// Fetch-add with acquire-release ordering at GPU scope: publishes this
+// thread's earlier writes and, for the thread that sees the final count,
+// makes everyone's published writes visible.
+__device__ __forceinline__ unsigned atom_add_acq_rel_gpu(unsigned *p, unsigned v)
+{
+    unsigned old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
 __device__ __forceinline__ int ld_relaxed_i32(const int *p)
 {
     int v;

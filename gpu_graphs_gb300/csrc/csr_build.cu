@@ -642,6 +642,7 @@ done:
 void csr_free(DeviceCsr &c)
 {
     if (c.heavy) cudaFree(c.heavy);
+    if (c.pieces) cudaFree(c.pieces);
     if (c.row) cudaFree(c.row);
     if (c.col) cudaFree(c.col);
     if (c.zmask) cudaFree(c.zmask);

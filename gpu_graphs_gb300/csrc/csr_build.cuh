@@ -20,6 +20,11 @@ struct DeviceCsr {
     int64_t nonisolated = 0;
     int *heavy = nullptr;      // vertices of out-degree > HEAVY_DEGREE (any order)
     int32_t nheavy = 0;
+    // multi-source pull pieces (built on demand by ms_prepare): every row of
+    // degree > 2 * MS_PIECE contributes {vertex, j} for its j-th MS_PIECE edges
+    int2 *pieces = nullptr;
+    int32_t npieces = 0;
+    bool pieces_built = false;
 };
 
 // Rows longer than this are walked by a whole warp in multi-source passes.

@@ -10,11 +10,10 @@
 // Work per level follows the frontier, not the graph:
 //   * the active vertices of a level (F != 0) are kept in a queue;
 //   * push step (sparse frontiers): the queue's rows are expanded with the
-//     edges split evenly over every warp of the grid (per-CTA degree prefix
-//     in shared memory); each edge ORs its lanes, minus lanes already at the
-//     neighbour, into N[u] with one atomicOr, and the first writer of N[u]
-//     appends u to a touched list; a second phase walks only the touched
-//     list, filters N by vis, records levels and builds the next queue;
+//     edges split evenly over warps (per-CTA degree prefix in shared
+//     memory); each edge claims its lanes at the neighbour with one atomicOr
+//     on vis, the claimed lanes go into the next frontier mask with a second
+//     atomicOr, whose first writer appends the neighbour to the next queue;
 //   * pull step (dense frontiers, symmetric graphs): every vertex with
 //     unreached lanes ORs F over its row until those lanes are covered --
 //     one thread per light row, a whole warp per row of degree > 64;
@@ -24,6 +23,7 @@
 // Levels are separated by the bounded grid barrier of common.cuh.
 #include <algorithm>
 #include <cstddef>
+#include <vector>
 
 #include "blockq.cuh"
 #include "msbfs.cuh"
@@ -42,10 +42,13 @@ struct MsArgs {
     const int *row, *col;
     const int *heavy;
     int nheavy;
-    unsigned long long *vis, *N;
+    const int2 *pieces;
+    int npieces;
+    unsigned long long *hacc;
+    unsigned *hcnt;
+    unsigned long long *vis;
     unsigned long long *F[3];
     int *Q[4];
-    int *T;
     int *out;
     const int *src;
     MsCtrl *ctrl;
@@ -122,9 +125,15 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
     if (gtid == 0) ctrl->t_entry = globaltimer_ns();
 
     // ---- init ----
+    for (long long c = gtid; c < a.npieces; c += gthreads) {
+        const int2 pc = a.pieces[c];
+        if (pc.y == 0) {
+            a.hacc[pc.x] = 0;
+            a.hcnt[pc.x] = 0;
+        }
+    }
     for (long long v = gtid; v < n; v += gthreads) {
         a.vis[v] = 0;
-        a.N[v] = 0;
         a.F[0][v] = 0;
         a.F[1][v] = 0;
         a.F[2][v] = 0;
@@ -137,7 +146,6 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
             ctrl->alive[i] = 0;
         }
         ctrl->alive[0] = all;
-        ctrl->tcnt[0] = ctrl->tcnt[1] = 0;
         ctrl->reached = 0;
         ctrl->edges_c = 0;
     }
@@ -215,50 +223,135 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
                 write_levels_warp(a.out, n, u, nw, nl);
                 wq_push(q, nw != 0, (int)u, qcnt_next, Qn);
             }
-            // heavy rows: one warp per vertex
-            for (long long h = gwarp; h < a.nheavy; h += nwarps) {
-                const int u = __ldg(a.heavy + h);
-                const unsigned long long vu = __ldcg(a.vis + u);
-                const unsigned long long need = ~vu & live;
-                unsigned long long acc = 0;
-                if (need) {
-                    const int b = __ldg(a.row + u), e = __ldg(a.row + u + 1);
-                    for (int i0 = b; i0 < e; i0 += 128) {
+            // heavy rows up to MS_HUGE edges: a warp screens 32 of them at once
+            // (one lane each, strided by the warp count so busy rows spread
+            // evenly over warps) and walks those with lanes to find, one by one
+            for (long long h0 = gwarp; h0 < a.nheavy; h0 += nwarps * 32) {
+                const long long h = h0 + (long long)lane * nwarps;
+                int u = 0, b = 0, e = 0;
+                unsigned long long vu = 0, need = 0;
+                if (h < a.nheavy) {
+                    u = __ldg(a.heavy + h);
+                    b = __ldg(a.row + u);
+                    e = __ldg(a.row + u + 1);
+                    if (e - b <= MS_HUGE) {  // longer rows: split into pieces below
+                        vu = __ldcg(a.vis + u);
+                        need = ~vu & live;
+                    }
+                }
+                unsigned todo = __ballot_sync(FULL, need != 0);
+                while (todo) {
+                    const int sl = __ffs(todo) - 1;
+                    todo &= todo - 1;
+                    const int ru = __shfl_sync(FULL, u, sl);
+                    const int rb = __shfl_sync(FULL, b, sl), re = __shfl_sync(FULL, e, sl);
+                    const unsigned long long rneed = __shfl_sync(FULL, need, sl);
+                    const unsigned long long rvu = __shfl_sync(FULL, vu, sl);
+                    unsigned long long acc = 0;
+                    for (int i0 = rb; i0 < re; i0 += 128) {
                         unsigned long long x = 0;
 #pragma unroll
                         for (int t = 0; t < 4; t++) {
                             const int i = i0 + t * 32 + (int)lane;
-                            if (i < e) x |= __ldcg(Fc + __ldg(a.col + i));
+                            if (i < re) x |= __ldcg(Fc + __ldg(a.col + i));
                         }
                         acc |= warp_or64(x);
-                        if ((acc & need) == need) break;
+                        if ((acc & rneed) == rneed) break;
                     }
+                    const unsigned long long nw = acc & rneed;
+                    if (nw) {
+                        if (lane == 0) {
+                            a.vis[ru] = rvu | nw;
+                            Fn[ru] = nw;
+                            my_or |= nw;
+                        }
+                        if ((nw >> lane) & 1ull) a.out[(size_t)lane * n + ru] = nl;
+                        if ((nw >> (lane + 32)) & 1ull) a.out[(size_t)(lane + 32) * n + ru] = nl;
+                    }
+                    wq_push(q, lane == 0 && nw != 0, ru, qcnt_next, Qn);
                 }
-                const unsigned long long nw = acc & need;
-                if (nw) {
+            }
+            // huge rows: pieces of MS_PIECE edges spread over all warps, so a
+            // hub that must be scanned to its end is not one warp's tail.  Each
+            // piece ORs what it found into hacc[u] and counts itself in
+            // hcnt[u]; the warp that counts a row's last piece settles the row.
+            // vis[u] only changes when the row is settled, after all of its
+            // pieces have counted, so every piece sees the same need: a row
+            // with nothing to find is skipped by all of its pieces.
+            for (long long c0 = gwarp; c0 < a.npieces; c0 += nwarps * 32) {
+                const long long c = c0 + (long long)lane * nwarps;
+                int2 pc = make_int2(0, 0);
+                unsigned long long vu = 0, need = 0;
+                if (c < a.npieces) {
+                    pc = __ldg(a.pieces + c);
+                    vu = __ldcg(a.vis + pc.x);
+                    need = ~vu & live;
+                }
+                unsigned todo = __ballot_sync(FULL, need != 0);
+                while (todo) {
+                    const int sl = __ffs(todo) - 1;
+                    todo &= todo - 1;
+                    const int u = __shfl_sync(FULL, pc.x, sl), j = __shfl_sync(FULL, pc.y, sl);
+                    const unsigned long long rvu = __shfl_sync(FULL, vu, sl);
+                    const unsigned long long rneed = __shfl_sync(FULL, need, sl);
+                    const int rb = __ldg(a.row + u), re = __ldg(a.row + u + 1);
+                    const unsigned pn = (unsigned)((re - rb + MS_PIECE - 1) / MS_PIECE);
+                    const int b = rb + j * MS_PIECE;
+                    const int e = min(re, b + MS_PIECE);
+                    unsigned long long acc = 0;
+                    // skip a piece whose row the others have already covered (one
+                    // read, broadcast: the loop below must be warp-uniform)
+                    unsigned long long seen = lane == 0 ? ld_relaxed_u64(a.hacc + u) : 0ull;
+                    seen = __shfl_sync(FULL, seen, 0);
+                    if ((seen & rneed) != rneed) {
+                        for (int i0 = b; i0 < e; i0 += 128) {
+                            unsigned long long x = 0;
+#pragma unroll
+                            for (int t = 0; t < 4; t++) {
+                                const int i = i0 + t * 32 + (int)lane;
+                                if (i < e) x |= __ldcg(Fc + __ldg(a.col + i));
+                            }
+                            acc |= warp_or64(x);
+                            if ((acc & rneed) == rneed) break;
+                        }
+                    }
+                    unsigned long long tot = 0;
+                    int last = 0;
                     if (lane == 0) {
-                        a.vis[u] = vu | nw;
-                        Fn[u] = nw;
-                        my_or |= nw;
+                        if (acc & rneed) atomicOr(a.hacc + u, acc & rneed);
+                        if (atom_add_acq_rel_gpu(a.hcnt + u, 1u) == pn - 1u) {
+                            tot = atomicExch(a.hacc + u, 0ull);
+                            a.hcnt[u] = 0;
+                            last = 1;
+                        }
                     }
-                    if ((nw >> lane) & 1ull) a.out[(size_t)lane * n + u] = nl;
-                    if ((nw >> (lane + 32)) & 1ull) a.out[(size_t)(lane + 32) * n + u] = nl;
+                    last = __shfl_sync(FULL, last, 0);
+                    if (!last) continue;
+                    const unsigned long long nw = __shfl_sync(FULL, tot, 0) & rneed;
+                    if (nw) {
+                        if (lane == 0) {
+                            a.vis[u] = rvu | nw;
+                            Fn[u] = nw;
+                            my_or |= nw;
+                        }
+                        if ((nw >> lane) & 1ull) a.out[(size_t)lane * n + u] = nl;
+                        if ((nw >> (lane + 32)) & 1ull) a.out[(size_t)(lane + 32) * n + u] = nl;
+                    }
+                    wq_push(q, lane == 0 && nw != 0, u, qcnt_next, Qn);
                 }
-                wq_push(q, lane == 0 && nw != 0, u, qcnt_next, Qn);
             }
             block_flush(q, qcnt_next, Qn, s_wq, &s_base);
             or_into(my_or, &ctrl->alive[(L + 1) % 4], s_red);
             if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
         } else {
             ++push_levels;
-            unsigned long long *tcnt = &ctrl->tcnt[L & 1];
-            // phase 1: the queue's edges.  Up to MS_GRID_SEGS segments of
-            // MS_SEG rows: every CTA builds each segment's degree prefix and the
-            // grid's warps split its edges evenly (hub rows of power-law graphs
-            // appear in these short early queues).  Longer queues: CTA b takes
-            // segments b, b+G, ... and its own warps split each one.
+            // the queue's edges.  Up to MS_GRID_SEGS segments of MS_SEG rows:
+            // every CTA builds each segment's degree prefix and the grid's warps
+            // split its edges evenly (hub rows of power-law graphs appear in
+            // these short early queues).  Longer queues: CTA b takes segments
+            // b, b+G, ... sized so every CTA gets about one, and its own warps
+            // split each one.
             const bool one_seg = nq <= (unsigned long long)MS_SEG * MS_GRID_SEGS;
-            // CTA segments sized so every CTA gets about one
             const long long cta_seg = min((long long)MS_SEG, max(32LL, ((long long)nq + gridDim.x - 1) / gridDim.x));
             const long long seg_len = one_seg ? MS_SEG : cta_seg;
             const long long seg0 = one_seg ? 0 : (long long)blockIdx.x * seg_len;
@@ -308,44 +401,27 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
                                 if (s_pre[mid] <= e) l = mid; else r = mid - 1;
                             }
                             const int u = __ldg(a.col + s_beg[l] + (int)(e - s_pre[l]));
-                            // vis may be read stale (it only gains bits: at worst an
-                            // extra atomic); N is cleared between levels by other SMs,
-                            // so it is read from L2
-                            const unsigned long long nw = s_f[l] & ~a.vis[u];
-                            if (nw && (__ldcg(a.N + u) & nw) != nw) {
-                                tt[h] = atomicOr(a.N + u, nw) == 0ull;
-                                uu[h] = u;
+                            // lanes of this edge not yet at u.  vis may be read
+                            // stale (it only gains bits): the atomic's old value
+                            // settles which lanes this edge discovers, so every
+                            // (lane, vertex) pair is claimed exactly once
+                            unsigned long long nw = s_f[l] & ~a.vis[u];
+                            if (nw) {
+                                nw &= ~atomicOr(a.vis + u, nw);
+                                if (nw) {
+                                    // the first claim of u in this level queues it
+                                    tt[h] = atomicOr(Fn + u, nw) == 0ull;
+                                    uu[h] = u;
+                                    my_or |= nw;
+                                    write_levels(a.out, n, u, nw, nl);
+                                }
                             }
                         }
                     }
-                    wq_push(q, tt[0], uu[0], tcnt, a.T);
-                    wq_push(q, tt[1], uu[1], tcnt, a.T);
+                    wq_push(q, tt[0], uu[0], qcnt_next, Qn);
+                    wq_push(q, tt[1], uu[1], qcnt_next, Qn);
                 }
                 __syncthreads();
-            }
-            block_flush(q, tcnt, a.T, s_wq, &s_base);
-            if (gtid == 0) ctrl->tcnt[(L + 1) & 1] = 0;
-            if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
-            // phase 2: touched vertices only
-            const unsigned long long nt = ld_relaxed_u64(tcnt);
-            for (long long base = gwarp * 32; base < (long long)nt; base += nwarps * 32) {
-                const long long i = base + lane;
-                int u = 0;
-                unsigned long long nw = 0;
-                if (i < (long long)nt) {
-                    u = __ldcg(a.T + i);
-                    const unsigned long long x = __ldcg(a.N + u);
-                    a.N[u] = 0;
-                    const unsigned long long vu = __ldcg(a.vis + u);
-                    nw = x & ~vu;
-                    if (nw) {
-                        a.vis[u] = vu | nw;
-                        Fn[u] = nw;
-                        my_or |= nw;
-                        write_levels(a.out, n, u, nw, nl);
-                    }
-                }
-                wq_push(q, nw != 0, u, qcnt_next, Qn);
             }
             block_flush(q, qcnt_next, Qn, s_wq, &s_base);
             or_into(my_or, &ctrl->alive[(L + 1) % 4], s_red);
@@ -397,6 +473,12 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
     grid_exit(&ctrl->bar);
 }
 
+__global__ void k_heavy_degrees(const int *__restrict__ row, const int *__restrict__ heavy, int nheavy, int *deg)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nheavy; i += gridDim.x * blockDim.x)
+        deg[i] = row[heavy[i] + 1] - row[heavy[i]];
+}
+
 size_t ms_smem_bytes()
 {
     return sizeof(int) * ((size_t)(MS_BLOCK / 32) * QCAP + 2 * (size_t)MS_SEG) +
@@ -404,6 +486,55 @@ size_t ms_smem_bytes()
 }
 
 }  // namespace
+
+int64_t ms_prepare_bytes(const DeviceCsr &g)
+{
+    // rows of degree d > 2 * MS_PIECE give ceil(d / MS_PIECE) < 1.5 d / MS_PIECE pieces
+    return g.pieces_built ? 0 : (int64_t)sizeof(int2) * (3 * g.m / (2 * MS_PIECE) + 1);
+}
+
+int ms_prepare(DeviceCsr &g, cudaStream_t st, std::string &err)
+{
+    if (g.pieces_built) return GBFS_OK;
+    std::vector<int2> h_pieces;
+    if (g.nheavy > 0 && g.max_degree > MS_HUGE) {
+        int *deg = nullptr;
+        std::vector<int> h_heavy(g.nheavy), h_deg(g.nheavy);
+        cudaError_t e = cudaMalloc(&deg, sizeof(int) * (size_t)g.nheavy);
+        if (e == cudaSuccess) {
+            k_heavy_degrees<<<std::max(1, std::min(1216, (g.nheavy + 255) / 256)), 256, 0, st>>>(g.row, g.heavy,
+                                                                                               g.nheavy, deg);
+            e = cudaMemcpyAsync(h_deg.data(), deg, sizeof(int) * (size_t)g.nheavy, cudaMemcpyDeviceToHost, st);
+        }
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(h_heavy.data(), g.heavy, sizeof(int) * (size_t)g.nheavy, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        cudaFree(deg);
+        if (e != cudaSuccess) {
+            err = std::string("pull pieces: ") + cudaGetErrorString(e);
+            return GBFS_ERR_CUDA;
+        }
+        for (int i = 0; i < g.nheavy; i++)
+            if (h_deg[i] > MS_HUGE)
+                for (int j = 0; j * MS_PIECE < h_deg[i]; j++) h_pieces.push_back(make_int2(h_heavy[i], j));
+    }
+    int2 *d = nullptr;
+    if (!h_pieces.empty()) {
+        cudaError_t e = cudaMalloc(&d, sizeof(int2) * h_pieces.size());
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d, h_pieces.data(), sizeof(int2) * h_pieces.size(), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            cudaFree(d);
+            err = std::string("pull pieces: ") + cudaGetErrorString(e);
+            return e == cudaErrorMemoryAllocation ? GBFS_ERR_OOM : GBFS_ERR_CUDA;
+        }
+    }
+    g.pieces = d;
+    g.npieces = (int32_t)h_pieces.size();
+    g.pieces_built = true;
+    return GBFS_OK;
+}
 
 int ms_work_alloc(MsWork &w, int32_t n, std::string &err)
 {
@@ -420,7 +551,7 @@ int ms_work_alloc(MsWork &w, int32_t n, std::string &err)
     };
     w.bytes = 0;
     const size_t b8 = sizeof(unsigned long long) * (size_t)n, b4 = sizeof(int) * (size_t)n;
-    bool ok = al((void **)&w.vis, b8) && al((void **)&w.N, b8) && al((void **)&w.T, b4) &&
+    bool ok = al((void **)&w.vis, b8) && al((void **)&w.hacc, b8) && al((void **)&w.hcnt, b4) &&
               al((void **)&w.out, b4 * MS_LANES) && al((void **)&w.src, sizeof(int) * MS_LANES) &&
               al((void **)&w.ctrl, sizeof(MsCtrl));
     for (int i = 0; ok && i < 3; i++) ok = al((void **)&w.F[i], b8);
@@ -442,7 +573,7 @@ int ms_work_alloc(MsWork &w, int32_t n, std::string &err)
 
 void ms_work_free(MsWork &w)
 {
-    void *ps[] = {w.vis, w.N, w.T, w.out, w.src, w.ctrl, w.F[0], w.F[1], w.F[2], w.Q[0], w.Q[1], w.Q[2], w.Q[3]};
+    void *ps[] = {w.vis, w.hacc, w.hcnt, w.out, w.src, w.ctrl, w.F[0], w.F[1], w.F[2], w.Q[0], w.Q[1], w.Q[2], w.Q[3]};
     for (void *p : ps)
         if (p) cudaFree(p);
     if (w.h_ctrl) cudaFreeHost(w.h_ctrl);
@@ -467,11 +598,14 @@ cudaError_t msbfs_enqueue(const DeviceCsr &g, const gbfs_params &p, bool pull_al
     a.col = g.col;
     a.heavy = g.heavy;
     a.nheavy = g.nheavy;
+    if (!g.pieces_built) return cudaErrorInvalidValue;  // ms_prepare not run
+    a.pieces = g.pieces;
+    a.npieces = g.npieces;
+    a.hacc = w.hacc;
+    a.hcnt = w.hcnt;
     a.vis = w.vis;
-    a.N = w.N;
     for (int i = 0; i < 3; i++) a.F[i] = w.F[i];
     for (int i = 0; i < 4; i++) a.Q[i] = w.Q[i];
-    a.T = w.T;
     a.out = d_out;
     a.src = d_src;
     a.ctrl = w.ctrl;

@@ -13,13 +13,14 @@
 namespace gbfs {
 
 constexpr int MS_LANES = 64;
+constexpr int MS_PIECE = 2048;           // edges of a huge row one warp takes in a pull step
+constexpr int MS_HUGE = 2 * MS_PIECE;    // rows longer than this are split into pieces
 
 struct MsCtrl {
     GridBarrier bar;
     int status;
     int pad0;
     unsigned long long qcnt[4];  // active-queue lengths, rotating by level
-    unsigned long long tcnt[2];  // touched-list lengths of push steps
     unsigned long long alive[4]; // lanes with a non-empty frontier, rotating by level
     int levels, push_levels, pull_levels, trace_len;
     unsigned long long reached, edges_c;
@@ -30,10 +31,10 @@ struct MsCtrl {
 struct MsWork {
     int32_t n = 0;
     unsigned long long *vis = nullptr;   // n lane masks: lanes that reached v
-    unsigned long long *N = nullptr;     // n push accumulators (zero between levels)
     unsigned long long *F[3] = {nullptr, nullptr, nullptr};  // frontier masks, rotating
     int *Q[4] = {nullptr, nullptr, nullptr, nullptr};        // active queues, rotating
-    int *T = nullptr;                    // touched list of a push step
+    unsigned long long *hacc = nullptr;  // n: per huge row, lanes its pull pieces found
+    unsigned *hcnt = nullptr;            // n: per huge row, pieces done this level
     int *out = nullptr;                  // MS_LANES * n levels (host-bound results)
     int *src = nullptr;                  // MS_LANES sources
     MsCtrl *ctrl = nullptr;
@@ -41,6 +42,12 @@ struct MsWork {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int64_t bytes = 0;
 };
+
+// Split the huge rows into pull pieces (DeviceCsr::pieces); a no-op once
+// built.  Synchronises st.
+int ms_prepare(DeviceCsr &g, cudaStream_t st, std::string &err);
+// Device bytes ms_prepare adds to a graph.
+int64_t ms_prepare_bytes(const DeviceCsr &g);
 
 // Device bytes ms_work_alloc takes for n vertices.
 int64_t ms_work_bytes(int64_t n);

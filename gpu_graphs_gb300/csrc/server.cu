@@ -280,7 +280,8 @@ extern "C" int gbfs_server_add_graph(gbfs_server *s, gbfs_graph *g, int32_t *gra
 {
     if (!s || !g || !graph_id) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
     std::unique_lock<std::mutex> lk(s->mu);
-    const int64_t gbytes = (int64_t)sizeof(int) * ((int64_t)g->csr.n + 1 + g->csr.m) + 4 * (((int64_t)g->csr.n + 31) / 32);
+    const int64_t gbytes = (int64_t)sizeof(int) * ((int64_t)g->csr.n + 1 + g->csr.m) + 4 * (((int64_t)g->csr.n + 31) / 32) +
+                           ms_prepare_bytes(g->csr);
     const int64_t new_cap = std::max<int64_t>(s->n_cap, g->csr.n);
     const int64_t need = s->resident + gbytes + s->slots_total(new_cap);
     if (need > s->cfg.mem_budget_bytes) {
@@ -321,6 +322,12 @@ extern "C" int gbfs_server_add_graph(gbfs_server *s, gbfs_graph *g, int32_t *gra
             return fail(rc, "slot workspace: " + err);
         }
         s->n_cap = new_cap;
+    }
+    {
+        std::lock_guard<std::mutex> glk(g->mu);
+        std::string err;
+        const int rc = ms_prepare(g->csr, g->stream, err);
+        if (rc) return fail(rc, err);
     }
     const int32_t gid = s->next_gid++;
     SrvGraph sg;

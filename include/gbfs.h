@@ -159,6 +159,19 @@ int gbfs_bfs(gbfs_graph *g, int32_t source, int32_t *levels_out,
              gbfs_stats *stats);
 
 /*
+ * BFS plus a BFS tree.  parents_out (n int32, host or device) receives the
+ * canonical parent of every vertex: the smallest u with an edge u -> v and
+ * level[u] == level[v] - 1, or -1 for the source and unreached vertices.
+ * Replaces the predecessor array of the reference's 2D BFS (`pred`,
+ * 2D Partition/src/cpuBFS.cpp:16,56; `d_pred`, 2D Partition/include/gpuBFS.cuh:45),
+ * whose entries depend on the order the frontier is walked; any of those is
+ * a valid parent, this one is unique.  levels_out: n int32 or NULL.
+ * stats.ms covers the traversal only.
+ */
+int gbfs_bfs_parents(gbfs_graph *g, int32_t source, int32_t *levels_out,
+                     int32_t *parents_out, gbfs_stats *stats);
+
+/*
  * k single-source searches run back to back, one launch each, queued on the
  * graph's stream with no host round trip in between (the plain
  * one-query-per-launch BFS).  levels_out: k*n int32 (host or device; row i

@@ -64,6 +64,8 @@ def lib() -> C.CDLL:
         L.oracle_exclusive_scan_i32.argtypes = [P, P, C.c_int64]
         L.oracle_component_edges.restype = C.c_int64
         L.oracle_component_edges.argtypes = [C.c_int32, P, P]
+        L.oracle_bfs_min_parents.restype = None
+        L.oracle_bfs_min_parents.argtypes = [C.c_int32, P, P, P, P]
         _lib = L
     return _lib
 
@@ -123,6 +125,22 @@ def exclusive_scan(x) -> np.ndarray:
     out = np.empty(len(a), np.int64)
     lib().oracle_exclusive_scan_i32(_p(a), _p(out), len(a))
     return out
+
+
+def min_parents(g: CSR, level: np.ndarray) -> np.ndarray:
+    lv = np.ascontiguousarray(level, np.int32)
+    out = np.empty(g.n, np.int32)
+    lib().oracle_bfs_min_parents(g.n, _p(g.row_offset), _p(g.col_idx), _p(lv), _p(out))
+    return out
+
+
+def bfs_levelsync_pred(g: CSR, source: int):
+    """Levels and the reference's order-dependent predecessors (C9 restatement)."""
+    level = np.empty(g.n, np.int32)
+    pred = np.empty(g.n, np.int32)
+    if lib().oracle_bfs_levelsync(g.n, _p(g.row_offset), _p(g.col_idx), source, _p(level), _p(pred)) < 0:
+        raise ValueError("bad source")
+    return level, pred
 
 
 def component_edges(g: CSR, level: np.ndarray) -> int:

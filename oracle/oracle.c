@@ -162,3 +162,19 @@ int64_t oracle_component_edges(int32_t n, const int64_t *row_offset,
         if (level[v] >= 0) s += row_offset[v + 1] - row_offset[v];
     return s;
 }
+
+void oracle_bfs_min_parents(int32_t n, const int64_t *row_offset,
+                            const int32_t *col_idx, const int32_t *level,
+                            int32_t *parent)
+{
+    int32_t u, v;
+    int64_t i;
+    for (v = 0; v < n; v++) parent[v] = level[v] > 0 ? INT32_MAX : -1;
+    for (u = 0; u < n; u++) {
+        if (level[u] < 0) continue;
+        for (i = row_offset[u]; i < row_offset[u + 1]; i++) {
+            v = col_idx[i];
+            if (level[v] == level[u] + 1 && u < parent[v]) parent[v] = u;
+        }
+    }
+}

@@ -78,6 +78,17 @@ void oracle_exclusive_scan_i32(const int32_t *in, int64_t *out, int64_t n);
 int64_t oracle_component_edges(int32_t n, const int64_t *row_offset,
                                const int32_t *level);
 
+/*
+ * Canonical BFS-tree parents from a level array: parent[v] = the smallest u
+ * with an edge u -> v and level[u] == level[v] - 1; -1 where level[v] <= 0.
+ * The reference's predecessor (pred, 2D Partition/src/cpuBFS.cpp:16,56) is
+ * the first such u in its frontier order; oracle_bfs_levelsync returns that
+ * one.  Both are valid parents; this one does not depend on any order.
+ */
+void oracle_bfs_min_parents(int32_t n, const int64_t *row_offset,
+                            const int32_t *col_idx, const int32_t *level,
+                            int32_t *parent);
+
 #ifdef __cplusplus
 }
 #endif

@@ -124,3 +124,25 @@ def test_autotune_keeps_levels_and_caches(gb, orc):
     p2 = g2.autotune(sources)
     assert time.perf_counter() - t0 < t_first
     assert p2.as_dict() == p.as_dict()
+
+
+def test_multi_source_huge_rows(gb, orc):
+    """Rows far above the pull piece size (hubs of degree 30000 and 9000) are
+    scanned in pieces by many warps and settled by the last one."""
+    n = 60000
+    s1, d1 = gb.gen_er(n, 90000, seed=51)
+    rng = np.random.default_rng(52)
+    hub_a = rng.choice(n, 30000, replace=False).astype(np.int32)
+    hub_b = rng.choice(n, 9000, replace=False).astype(np.int32)
+    src = np.concatenate([s1, np.full(30000, 7, np.int32), np.full(9000, 11, np.int32)])
+    dst = np.concatenate([d1, hub_a, hub_b])
+    o = orc.csr_build(n, src, dst, orc.UNDIRECTED)
+    g = gb.Graph.from_edges(n, src, dst)
+    deg = np.diff(o.row_offset)
+    assert deg.max() > 4 * 2048
+    sources = list(rng.choice(np.flatnonzero(deg > 0), 64, replace=False))
+    for direction in (0, 2):
+        g.set_params(direction=direction)
+        got = g.bfs_multi(sources)
+        for i, s in enumerate(sources):
+            assert np.array_equal(got[i], orc.bfs_queue(o, int(s))), (direction, i)

@@ -97,3 +97,41 @@ def test_reference_binaries_agree_when_present(orc):
     for s in d["sources"]:
         l9, _ = orc.ref_bfs("c9", int(s), csr=g)
         assert np.array_equal(l9, orc.bfs_levelsync(g, int(s)))
+
+
+def check_bfs_tree(g, source: int, level: np.ndarray, parent: np.ndarray) -> None:
+    """Graph500-style validation of a BFS tree against its level array."""
+    n = g.n
+    assert parent[source] == -1 and level[source] == 0
+    reached = level >= 0
+    assert np.all(parent[~reached] == -1)
+    v = np.flatnonzero(reached & (np.arange(n) != source))
+    p = parent[v]
+    assert np.all((p >= 0) & (p < n))
+    assert np.all(level[p] == level[v] - 1)
+    # every tree edge p -> v exists in the graph
+    row, col = g.row_offset, g.col_idx
+    for vi, pi in zip(v, p):
+        assert vi in col[row[pi]:row[pi + 1]]
+
+
+@pytest.mark.parametrize("name", golden_names("ref_"))
+def test_oracle_parents_on_reference_fixtures(orc, name):
+    d = load_golden(name)
+    g = orc.csr_build(int(d["n"]), d["src"], d["dst"], 0)
+    for s in d["sources"]:
+        level, pred = orc.bfs_levelsync_pred(g, int(s))
+        mp = orc.min_parents(g, level)
+        check_bfs_tree(g, int(s), level, mp)
+        check_bfs_tree(g, int(s), level, pred)  # the reference's own predecessors
+        # the canonical parent is the smallest valid one
+        assert np.all(mp[pred >= 0] <= pred[pred >= 0]) and np.all(mp[pred < 0] == -1)
+
+
+def test_oracle_parents_small_graph(orc):
+    # 0 -> {2, 1}, 1 -> 3, 2 -> 3: vertex 3 has parents 1 and 2 one level up
+    g = orc.csr_build(5, np.array([0, 0, 2, 1], np.int32), np.array([2, 1, 3, 3], np.int32), 0)
+    level, pred = orc.bfs_levelsync_pred(g, 0)
+    assert level.tolist() == [0, 1, 1, 2, -1]
+    assert pred[3] == 2  # row 0 lists 2 first, so 2 discovers 3 first
+    assert orc.min_parents(g, level).tolist() == [-1, 0, 0, 1, -1]
