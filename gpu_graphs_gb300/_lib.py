@@ -91,6 +91,7 @@ class ServerConfig(C.Structure):
         ("max_lanes", C.c_int32),
         ("batch_window_us", C.c_int32),
         ("timeout_ms", C.c_int32),
+        ("window_pct", C.c_int32),
     ]
 
 

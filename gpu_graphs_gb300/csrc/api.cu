@@ -461,7 +461,7 @@ extern "C" int gbfs_last_trace(gbfs_graph *g, gbfs_level_trace *rows, int32_t ca
 {
     if (!g || (cap > 0 && !rows) || cap < 0) return fail(GBFS_ERR_INVALID_ARG, "bad argument");
     std::lock_guard<std::mutex> lk(g->mu);
-    unsigned long long t_entry, t_start, t_end;
+    unsigned long long t_entry, t_start, t_end, t_exit;
     int trace_len;
     const LevelTrace *trace;
     cudaError_t e;
@@ -474,7 +474,8 @@ extern "C" int gbfs_last_trace(gbfs_graph *g, gbfs_level_trace *rows, int32_t ca
                                                   cudaMemcpyDeviceToHost, g->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
         if (e != cudaSuccess) return cuda_fail(e, "trace D2H");
-        t_entry = h->t_entry; t_start = h->t_start; t_end = h->t_end; trace_len = h->trace_len; trace = h->trace;
+        t_entry = h->t_entry; t_start = h->t_start; t_end = h->t_end; t_exit = h->t_exit;
+        trace_len = h->trace_len; trace = h->trace;
     } else {
         if (!g->work.ctrl) return 0;
         BfsCtrl *h = g->work.h_ctrl;
@@ -482,9 +483,10 @@ extern "C" int gbfs_last_trace(gbfs_graph *g, gbfs_level_trace *rows, int32_t ca
                             cudaMemcpyDeviceToHost, g->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
         if (e != cudaSuccess) return cuda_fail(e, "trace D2H");
-        t_entry = h->t_entry; t_start = h->t_start; t_end = h->t_end; trace_len = h->trace_len; trace = h->trace;
+        t_entry = h->t_entry; t_start = h->t_start; t_end = h->t_end; t_exit = h->t_exit;
+        trace_len = h->trace_len; trace = h->trace;
     }
-    const int len = std::min<int>(std::min<int>(trace_len, TRACE_CAP), cap - 2);
+    const int len = std::min<int>(std::min<int>(trace_len, TRACE_CAP), cap - 3);
     if (len < 0) return 0;
     // row 0: initialisation (level -1), from CTA 0's entry to the first level
     rows[0].level = -1;
@@ -507,7 +509,13 @@ extern "C" int gbfs_last_trace(gbfs_graph *g, gbfs_level_trace *rows, int32_t ca
     rows[len].frontier_vertices = 0;
     rows[len].frontier_edges = 0;
     rows[len].t_us = (double)(t_end - t_start) / 1000.0;
-    return len + 2;
+    // then the last CTA's exit: closing passes (unreached lanes, totals) done
+    rows[len + 1].level = -3;
+    rows[len + 1].direction = -3;
+    rows[len + 1].frontier_vertices = 0;
+    rows[len + 1].frontier_edges = 0;
+    rows[len + 1].t_us = (double)(t_exit - t_start) / 1000.0;
+    return len + 3;
 }
 
 extern "C" void *gbfs_graph_stream(const gbfs_graph *g) { return g ? (void *)g->stream : nullptr; }

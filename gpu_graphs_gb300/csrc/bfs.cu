@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                 r.pad = 0;
                 ctrl->rs = r;
             }
-            grid_exit(&ctrl->bar);
+            grid_exit(&ctrl->bar, &ctrl->t_exit);
             return;
         }
         const unsigned long long nf = ld_relaxed_u64(&ctrl->cnt[L % 3]);
@@ -570,7 +570,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
         }
         ctrl->fill = 0;
     }
-    grid_exit(&ctrl->bar);
+    grid_exit(&ctrl->bar, &ctrl->t_exit);
 }
 
 template <int BLOCK>

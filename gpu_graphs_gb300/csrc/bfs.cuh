@@ -50,6 +50,7 @@ struct BfsCtrl {
     unsigned long long t_entry;  // %globaltimer when CTA 0 started
     unsigned long long t_start;  // %globaltimer after initialisation
     unsigned long long t_end;    // %globaltimer when CTA 0 left the level loop
+    unsigned long long t_exit;   // %globaltimer when the last CTA left the kernel
     int trace_len;
     int pad3;
     LevelTrace trace[TRACE_CAP];

@@ -175,13 +175,17 @@ __device__ __forceinline__ bool grid_sync(GridBarrier *bar, int *status, unsigne
     return s_ok != 0;
 }
 
-__device__ __forceinline__ void grid_exit(GridBarrier *bar)
+// Count this CTA out; the last one resets the barrier for the next launch
+// and, if t_exit is given, stamps %globaltimer there.
+__device__ __forceinline__ void grid_exit(GridBarrier *bar, unsigned long long *t_exit = nullptr)
 {
+    __syncthreads();
     if (threadIdx.x == 0) {
         const unsigned old = atomicAdd(&bar->exit, 1u);
         if (old == gridDim.x - 1) {
             bar->count = 0;
             bar->exit = 0;
+            if (t_exit) *t_exit = globaltimer_ns();
             __threadfence();
         }
     }

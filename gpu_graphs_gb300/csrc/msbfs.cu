@@ -50,17 +50,38 @@ struct MsArgs {
     unsigned long long *F[3];
     int *Q[4];
     int *out;
+    unsigned char *lv8;
     const int *src;
     MsCtrl *ctrl;
     int pull_allowed, direction, pull_div;
     unsigned long long timeout_ns;
 };
 
-__device__ __forceinline__ void write_levels(int *out, int n, int u, unsigned long long bits, int nl)
+// Levels are recorded as bytes (lv8, 64 x n) while the search runs: a row of
+// 4 x n level ints written a few entries per level leaves partly written
+// sectors to be evicted and merged in DRAM over and over, while the byte
+// rows of a million-vertex graph stay in L2.  The closing pass expands them
+// into out with whole 128-byte lines.  Levels from LV8_DEEP on go straight
+// to out, their byte marked LV8_DEEP.
+constexpr int LV8_DEEP = 255;
+
+__device__ __forceinline__ void record_level(unsigned char *lv8, int *out, int n, long long u, int j, int nl)
+{
+    const size_t i = (size_t)j * n + u;
+    if (nl < LV8_DEEP) {
+        lv8[i] = (unsigned char)nl;
+    } else {
+        lv8[i] = (unsigned char)LV8_DEEP;
+        out[i] = nl;
+    }
+}
+
+__device__ __forceinline__ void write_levels(unsigned char *lv8, int *out, int n, int u, unsigned long long bits,
+                                             int nl)
 {
     while (bits) {
         const int j = __ffsll((long long)bits) - 1;
-        out[(size_t)j * n + u] = nl;
+        record_level(lv8, out, n, u, j, nl);
         bits &= bits - 1ull;
     }
 }
@@ -74,13 +95,14 @@ __device__ __forceinline__ unsigned long long warp_or64(unsigned long long x)
 
 // Warp-wide level writes for 32 consecutive vertices u = base + lane: the loop
 // runs over the union of the lanes' masks, so each store instruction covers
-// one output row and coalesces.  All 32 threads call it.
-__device__ __forceinline__ void write_levels_warp(int *out, int n, long long u, unsigned long long bits, int val)
+// one byte row and coalesces.  All 32 threads call it.
+__device__ __forceinline__ void write_levels_warp(unsigned char *lv8, int *out, int n, long long u,
+                                                  unsigned long long bits, int nl)
 {
     unsigned long long any = warp_or64(bits);
     while (any) {
         const int j = __ffsll((long long)any) - 1;
-        if ((bits >> j) & 1ull) out[(size_t)j * n + u] = val;
+        if ((bits >> j) & 1ull) record_level(lv8, out, n, u, j, nl);
         any &= any - 1ull;
     }
 }
@@ -155,7 +177,7 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
         const unsigned long long bit = 1ull << threadIdx.x;
         atomicOr(&a.vis[s], bit);
         const unsigned long long old = atomicOr(&a.F[0][s], bit);
-        a.out[(size_t)threadIdx.x * n + s] = 0;
+        a.lv8[(size_t)threadIdx.x * n + s] = 0;
         if (old == 0) a.Q[0][atomicAdd(&ctrl->qcnt[0], 1ull)] = s;
     }
     if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
@@ -220,7 +242,7 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
                 }
                 // level writes: one store per discovered lane, coalesced over the
                 // warp's 32 consecutive vertices
-                write_levels_warp(a.out, n, u, nw, nl);
+                write_levels_warp(a.lv8, a.out, n, u, nw, nl);
                 wq_push(q, nw != 0, (int)u, qcnt_next, Qn);
             }
             // heavy rows up to MS_HUGE edges: a warp screens 32 of them at once
@@ -265,8 +287,8 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
                             Fn[ru] = nw;
                             my_or |= nw;
                         }
-                        if ((nw >> lane) & 1ull) a.out[(size_t)lane * n + ru] = nl;
-                        if ((nw >> (lane + 32)) & 1ull) a.out[(size_t)(lane + 32) * n + ru] = nl;
+                        if ((nw >> lane) & 1ull) record_level(a.lv8, a.out, n, ru, lane, nl);
+                        if ((nw >> (lane + 32)) & 1ull) record_level(a.lv8, a.out, n, ru, lane + 32, nl);
                     }
                     wq_push(q, lane == 0 && nw != 0, ru, qcnt_next, Qn);
                 }
@@ -334,8 +356,8 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
                             Fn[u] = nw;
                             my_or |= nw;
                         }
-                        if ((nw >> lane) & 1ull) a.out[(size_t)lane * n + u] = nl;
-                        if ((nw >> (lane + 32)) & 1ull) a.out[(size_t)(lane + 32) * n + u] = nl;
+                        if ((nw >> lane) & 1ull) record_level(a.lv8, a.out, n, u, lane, nl);
+                        if ((nw >> (lane + 32)) & 1ull) record_level(a.lv8, a.out, n, u, lane + 32, nl);
                     }
                     wq_push(q, lane == 0 && nw != 0, u, qcnt_next, Qn);
                 }
@@ -413,7 +435,7 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
                                     tt[h] = atomicOr(Fn + u, nw) == 0ull;
                                     uu[h] = u;
                                     my_or |= nw;
-                                    write_levels(a.out, n, u, nw, nl);
+                                    write_levels(a.lv8, a.out, n, u, nw, nl);
                                 }
                             }
                         }
@@ -443,21 +465,33 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
         ctrl->trace_len = L < TRACE_CAP ? L : TRACE_CAP;
     }
 
-    // -1 for the lanes that never reached a vertex; per-lane totals for GTEPS
+    // closing pass: level rows from the byte rows (-1 where a lane never
+    // arrived), 32 consecutive vertices per warp so every store is a whole
+    // line of one row; per-lane totals for GTEPS
     unsigned long long r = 0, ec = 0;
     for (long long base = gwarp * 32; base < n; base += nwarps * 32) {
         const long long u = base + lane;
-        unsigned long long miss = 0;
-        if (u < n) {
-            const unsigned long long vu = __ldcg(a.vis + u) & all;
-            miss = ~vu & all;
-            const int c = __popcll(vu);
-            if (c) {
-                r += c;
-                ec += (unsigned long long)c * (unsigned long long)(__ldg(a.row + u + 1) - __ldg(a.row + u));
-            }
+        if (u >= n) continue;  // no warp-wide operations below
+        const unsigned long long vu = __ldcg(a.vis + u) & all;
+        const int c = __popcll(vu);
+        if (c) {
+            r += c;
+            ec += (unsigned long long)c * (unsigned long long)(__ldg(a.row + u + 1) - __ldg(a.row + u));
         }
-        write_levels_warp(a.out, n, u, miss, -1);
+        // 16 lanes' bytes are loaded before any of their stores, so the
+        // loads are in flight together
+        for (int j0 = 0; j0 < a.k; j0 += 16) {
+            int v[16];
+#pragma unroll
+            for (int t = 0; t < 16; t++) {
+                const int j = j0 + t;
+                v[t] = -1;
+                if (j < a.k && ((vu >> j) & 1ull)) v[t] = __ldcg(a.lv8 + (size_t)j * n + u);
+            }
+#pragma unroll
+            for (int t = 0; t < 16; t++)
+                if (j0 + t < a.k && v[t] != LV8_DEEP) a.out[(size_t)(j0 + t) * n + u] = v[t];
+        }
     }
     const unsigned long long br = block_reduce_sum(r, s_red);
     const unsigned long long be = block_reduce_sum(ec, s_red);
@@ -470,7 +504,7 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
         ctrl->push_levels = push_levels;
         ctrl->pull_levels = pull_levels;
     }
-    grid_exit(&ctrl->bar);
+    grid_exit(&ctrl->bar, &ctrl->t_exit);
 }
 
 __global__ void k_heavy_degrees(const int *__restrict__ row, const int *__restrict__ heavy, int nheavy, int *deg)
@@ -552,6 +586,7 @@ int ms_work_alloc(MsWork &w, int32_t n, std::string &err)
     w.bytes = 0;
     const size_t b8 = sizeof(unsigned long long) * (size_t)n, b4 = sizeof(int) * (size_t)n;
     bool ok = al((void **)&w.vis, b8) && al((void **)&w.hacc, b8) && al((void **)&w.hcnt, b4) &&
+              al((void **)&w.lv8, (size_t)n * MS_LANES) &&
               al((void **)&w.out, b4 * MS_LANES) && al((void **)&w.src, sizeof(int) * MS_LANES) &&
               al((void **)&w.ctrl, sizeof(MsCtrl));
     for (int i = 0; ok && i < 3; i++) ok = al((void **)&w.F[i], b8);
@@ -573,7 +608,7 @@ int ms_work_alloc(MsWork &w, int32_t n, std::string &err)
 
 void ms_work_free(MsWork &w)
 {
-    void *ps[] = {w.vis, w.hacc, w.hcnt, w.out, w.src, w.ctrl, w.F[0], w.F[1], w.F[2], w.Q[0], w.Q[1], w.Q[2], w.Q[3]};
+    void *ps[] = {w.vis, w.hacc, w.hcnt, w.lv8, w.out, w.src, w.ctrl, w.F[0], w.F[1], w.F[2], w.Q[0], w.Q[1], w.Q[2], w.Q[3]};
     for (void *p : ps)
         if (p) cudaFree(p);
     if (w.h_ctrl) cudaFreeHost(w.h_ctrl);
@@ -584,7 +619,7 @@ void ms_work_free(MsWork &w)
 
 int64_t ms_work_bytes(int64_t n)
 {
-    return n > 0 ? (int64_t)(8 * 5 + 4 * 5 + 4 * MS_LANES) * n + 4096 : 0;
+    return n > 0 ? (int64_t)(8 * 5 + 4 * 5 + 5 * MS_LANES) * n + 4096 : 0;
 }
 
 cudaError_t msbfs_enqueue(const DeviceCsr &g, const gbfs_params &p, bool pull_allowed, MsWork &w,
@@ -607,6 +642,7 @@ cudaError_t msbfs_enqueue(const DeviceCsr &g, const gbfs_params &p, bool pull_al
     for (int i = 0; i < 3; i++) a.F[i] = w.F[i];
     for (int i = 0; i < 4; i++) a.Q[i] = w.Q[i];
     a.out = d_out;
+    a.lv8 = w.lv8;
     a.src = d_src;
     a.ctrl = w.ctrl;
     a.pull_allowed = pull_allowed ? 1 : 0;

@@ -25,6 +25,7 @@ struct MsCtrl {
     int levels, push_levels, pull_levels, trace_len;
     unsigned long long reached, edges_c;
     unsigned long long t_entry, t_start, t_end;
+    unsigned long long t_exit;     // the last CTA leaving the kernel (after the closing pass)
     LevelTrace trace[TRACE_CAP];   // per level: frontier = active vertices
 };
 
@@ -35,6 +36,7 @@ struct MsWork {
     int *Q[4] = {nullptr, nullptr, nullptr, nullptr};        // active queues, rotating
     unsigned long long *hacc = nullptr;  // n: per huge row, lanes its pull pieces found
     unsigned *hcnt = nullptr;            // n: per huge row, pieces done this level
+    unsigned char *lv8 = nullptr;        // MS_LANES * n levels as bytes while the search runs
     int *out = nullptr;                  // MS_LANES * n levels (host-bound results)
     int *src = nullptr;                  // MS_LANES sources
     MsCtrl *ctrl = nullptr;

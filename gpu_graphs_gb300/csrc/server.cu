@@ -6,10 +6,13 @@
 //   * every query joins its graph's FIFO;
 //   * `num_slots` worker threads, each owning a CUDA stream and a 64-lane
 //     multi-source workspace sized for the largest admitted graph, take the
-//     graph whose oldest query has waited longest and pack up to
-//     `max_lanes` of its queries into one multi-source launch (waiting at
-//     most `batch_window_us` for a fuller batch), so queries that arrive
-//     while others are on the GPU join the next free slot;
+//     ready graph whose oldest query has waited longest and pack up to
+//     `max_lanes` of its queries into one multi-source launch.  A graph is
+//     ready with a full batch or once its oldest query has waited
+//     `batch_window_us`, or `window_pct` percent of the graph's recent launch
+//     time if longer: a launch costs about the same for one source as for
+//     64, so slow graphs gather bigger batches, while other graphs' queries
+//     keep the slots busy meanwhile;
 //   * slots run concurrently on their streams, each launch capped to
 //     1/num_slots of the GPU's CTAs so all of them fit on the GPU together
 //     (every launch waits on all of its own CTAs);
@@ -51,6 +54,7 @@ struct SrvGraph {
     int64_t bytes = 0;
     std::deque<std::shared_ptr<SrvQuery>> pending;
     int inflight = 0;
+    double est_us = 0;   // recent launch time (moving average), 0 before the first
 };
 
 // 64-lane workspace + single-source workspace (level, 3 bitmaps + visited, 4 int lists)
@@ -110,27 +114,35 @@ void gbfs_server::worker(int idx)
         {
             std::unique_lock<std::mutex> lk(mu);
             for (;;) {
+                Clock::time_point next_ready = Clock::time_point::max();
                 if (!resizing) {
-                    // the graph whose oldest query has waited longest
+                    // among the graphs that are ready (a full batch, or their
+                    // oldest query has waited out the graph's window), the one
+                    // whose oldest query has waited longest
+                    const auto now = Clock::now();
                     Clock::time_point oldest = Clock::time_point::max();
-                    for (auto &kv : graphs)
-                        if (!kv.second.pending.empty() && kv.second.pending.front()->t_submit < oldest) {
-                            oldest = kv.second.pending.front()->t_submit;
-                            sg = &kv.second;
-                            gid = kv.first;
+                    for (auto &kv : graphs) {
+                        SrvGraph &c = kv.second;
+                        if (c.pending.empty()) continue;
+                        const auto t0 = c.pending.front()->t_submit;
+                        const double window_us =
+                            std::min(1e6, std::max<double>(cfg.batch_window_us, 0.01 * cfg.window_pct * c.est_us));
+                        const auto ready_at = t0 + std::chrono::microseconds((int64_t)window_us);
+                        if ((int)c.pending.size() >= cfg.max_lanes || now >= ready_at || stop) {
+                            if (t0 < oldest) {
+                                oldest = t0;
+                                sg = &c;
+                                gid = kv.first;
+                            }
+                        } else {
+                            next_ready = std::min(next_ready, ready_at);
                         }
-                    if (sg) {
-                        const auto now = Clock::now();
-                        const double age_us = std::chrono::duration<double, std::micro>(now - oldest).count();
-                        if ((int)sg->pending.size() >= cfg.max_lanes || age_us >= cfg.batch_window_us || stop) break;
-                        cv_work.wait_for(lk, std::chrono::microseconds(
-                                                 std::max(1, (int)(cfg.batch_window_us - age_us))));
-                        sg = nullptr;
-                        continue;
                     }
+                    if (sg) break;
                 }
-                if (stop) return;
-                cv_work.wait(lk);
+                if (stop && next_ready == Clock::time_point::max()) return;
+                if (next_ready != Clock::time_point::max()) cv_work.wait_until(lk, next_ready);
+                else cv_work.wait(lk);
             }
             const int k = std::min<int>((int)sg->pending.size(), cfg.max_lanes);
             batch.clear();
@@ -151,6 +163,7 @@ void gbfs_server::worker(int idx)
         }
         gbfs_graph *g = sg->g;
         const int k = (int)batch.size();
+        const auto t_launch = Clock::now();
         const size_t n = (size_t)g->csr.n;
         int status = GBFS_OK;
         gbfs_params p = g->params;
@@ -206,7 +219,12 @@ void gbfs_server::worker(int idx)
                 if (status == GBFS_OK) lat.push_back(q->latency_ms);
             }
             auto it = graphs.find(gid);
-            if (it != graphs.end()) it->second.inflight -= k;
+            if (it != graphs.end()) {
+                SrvGraph &c = it->second;
+                c.inflight -= k;
+                const double us = std::chrono::duration<double, std::micro>(now - t_launch).count();
+                c.est_us = c.est_us > 0 ? 0.7 * c.est_us + 0.3 * us : us;
+            }
             --busy_slots;
         }
         cv_done.notify_all();
@@ -219,7 +237,8 @@ extern "C" int gbfs_server_create(const gbfs_server_config *cfg, gbfs_server **o
     if (!cfg || !out) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
     *out = nullptr;
     if (cfg->num_slots < 1 || cfg->num_slots > 16 || cfg->max_lanes < 1 || cfg->max_lanes > MS_LANES ||
-        cfg->mem_budget_bytes <= 0 || cfg->batch_window_us < 0 || cfg->timeout_ms < 1)
+        cfg->mem_budget_bytes <= 0 || cfg->batch_window_us < 0 || cfg->timeout_ms < 1 || cfg->window_pct < 0 ||
+        cfg->window_pct > 1000)
         return fail(GBFS_ERR_INVALID_ARG, "bad server configuration");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {

@@ -14,13 +14,16 @@ class Server:
 
     Graphs are admitted against an HBM budget; queries are queued per graph
     and packed (up to ``max_lanes`` sources) into multi-source launches as
-    slots free up, on ``num_slots`` concurrent streams.
+    slots free up, on ``num_slots`` concurrent streams.  A graph's queries
+    wait up to ``batch_window_us``, or ``window_pct`` percent of its recent
+    launch time if that is longer, for a fuller batch.  Result copies are
+    fastest into pinned host buffers.
     """
 
     def __init__(self, mem_budget_bytes: int, num_slots: int = 4, max_lanes: int = 64,
-                 batch_window_us: int = 200, timeout_ms: int = 2000):
+                 batch_window_us: int = 200, timeout_ms: int = 2000, window_pct: int = 0):
         cfg = _lib.ServerConfig(int(mem_budget_bytes), int(num_slots), int(max_lanes), int(batch_window_us),
-                                int(timeout_ms))
+                                int(timeout_ms), int(window_pct))
         self._h = C.c_void_p()
         check(lib.gbfs_server_create(C.byref(cfg), C.byref(self._h)), "gbfs_server_create")
         self._graphs = {}

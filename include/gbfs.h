@@ -197,8 +197,10 @@ typedef struct gbfs_level_trace {
 
 /* Copies up to cap rows; returns the number of rows (>= 0) or a status.
  * Row 0 describes initialisation: level -1, t_us = minus its duration
- * (from the first CTA's entry to the first level).  The last row (level
- * -2) marks the end of the level loop, termination check included. */
+ * (from the first CTA's entry to the first level).  Then one row per level,
+ * then a row with level -2 marking the end of the level loop (termination
+ * check included) and a last row with level -3: the moment the last CTA
+ * left the kernel, after the closing passes. */
 int gbfs_last_trace(gbfs_graph *g, gbfs_level_trace *rows, int32_t cap);
 
 /* The CUDA stream (cudaStream_t) the graph's work is ordered on, for
@@ -345,6 +347,11 @@ typedef struct gbfs_server_config {
     int32_t max_lanes;          /* sources per multi-source launch (<= 64)  */
     int32_t batch_window_us;    /* wait this long for same-graph arrivals   */
     int32_t timeout_ms;         /* device wait bound for each launch        */
+    int32_t window_pct;         /* ...or up to this percentage of the graph's
+                                   recent launch time, if longer (0: fixed
+                                   window).  A launch costs about the same
+                                   for 1 or 64 sources, so on slow graphs a
+                                   longer wait buys throughput.             */
 } gbfs_server_config;
 
 typedef struct gbfs_query_info {

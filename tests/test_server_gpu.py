@@ -27,9 +27,11 @@ def _graphs(gb, orc):
     return out
 
 
-def test_server_mix_equals_alone(gb, orc):
+@pytest.mark.parametrize("window_pct", [0, 50])
+def test_server_mix_equals_alone(gb, orc, window_pct):
     graphs = _graphs(gb, orc)
-    with gb.Server(mem_budget_bytes=8 << 30, num_slots=3, max_lanes=64, batch_window_us=300) as srv:
+    with gb.Server(mem_budget_bytes=8 << 30, num_slots=3, max_lanes=64, batch_window_us=300,
+                   window_pct=window_pct) as srv:
         gids = [srv.add_graph(g) for g, _ in graphs]
         rng = np.random.default_rng(5)
         plan = [(int(rng.integers(len(graphs))), None) for _ in range(400)]
@@ -67,6 +69,10 @@ def test_server_mix_equals_alone(gb, orc):
 
 
 def test_server_budget_and_errors(gb, orc):
+    for bad in ({"window_pct": -1}, {"window_pct": 1001}, {"max_lanes": 65}, {"num_slots": 0}):
+        with pytest.raises(gb.GbfsError) as e:
+            gb.Server(mem_budget_bytes=1 << 30, **bad)
+        assert e.value.code == gb._lib.ERR_INVALID_ARG
     graphs = _graphs(gb, orc)
     g = graphs[0][0]
     with gb.Server(mem_budget_bytes=1 << 20, num_slots=2) as srv:
