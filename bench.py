@@ -300,11 +300,18 @@ def measure_batched(torch) -> dict:
     t_plain = min(sum(s.ms for s in g.bfs_many(sources, out=plain_out)[1]) for _ in range(3))
     t_multi = min(g.bfs_multi(sources, out=multi_out, stats=True)[1].ms for _ in range(3))
     same = bool(torch.equal(plain_out, multi_out))
+    # the plain top-down BFS (one query per launch, no bottom-up steps)
+    g.set_params(direction=1)
+    t_plain_td = min(sum(s.ms for s in g.bfs_many(sources, out=plain_out)[1]) for _ in range(2))
+    same = same and bool(torch.equal(plain_out, multi_out))
+    g.set_params(direction=0)
     res["multi_source"] = {
         "workload": "RMAT scale 20, ef 16, 64 sources per launch (uint64 lane masks)",
-        "plain_ms": round(t_plain, 3), "batched_ms": round(t_multi, 3),
+        "plain_ms": round(t_plain, 3), "plain": "direction-optimising single-source kernel, one launch per source",
+        "plain_topdown_ms": round(t_plain_td, 3), "batched_ms": round(t_multi, 3),
         "plain_queries_per_s": round(64 / (t_plain / 1e3), 1), "batched_queries_per_s": round(64 / (t_multi / 1e3), 1),
-        "speedup": round(t_plain / t_multi, 2), "levels_identical": same}
+        "speedup": round(t_plain / t_multi, 2), "speedup_vs_topdown": round(t_plain_td / t_multi, 2),
+        "levels_identical": same}
     del plain_out, multi_out, g
 
     rng = np.random.default_rng(1)
@@ -333,6 +340,60 @@ def measure_batched(torch) -> dict:
     return res
 
 
+def measure_primitives(torch) -> dict:
+    """The path's other kernels: the CSR build (edge list in, CSR out) against the
+    oracle's CPU restatement of the reference loader on the same edges, and the
+    exclusive scan against the HBM peak."""
+    import gpu_graphs_gb300 as gb
+    import oracle
+    res = {}
+    n20 = 1 << 20
+    src, dst = gb.gen_rmat(20, 16, 0.57, 0.19, 0.19, seed=1)
+    gb.Graph.from_edges(n20, src, dst, gb.UNDIRECTED)  # warm-up
+    ts = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g = gb.Graph.from_edges(n20, src, dst, gb.UNDIRECTED)
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+        m = g.m
+        del g
+    t0 = time.perf_counter()
+    og = oracle.csr_build(n20, src, dst, oracle.UNDIRECTED)
+    t_cpu = time.perf_counter() - t0
+    res["csr_build"] = {
+        "workload": f"RMAT scale 20, {len(src)} input edges -> symmetrised, deduped, sorted CSR ({m} directed edges)",
+        "gpu_ms_host_arrays_in": round(min(ts) * 1e3, 2),
+        "gpu_input_edges_per_s": round(len(src) / min(ts), 1),
+        "cpu_ms": round(t_cpu * 1e3, 1), "cpu": "oracle restatement of the reference loader (csc.cpp), 1 thread",
+        "identical_edge_count": bool(og.m == m)}
+    del og
+    nscan = 1 << 28  # 3.2 GB moved per call: the per-call status read-back is a few % of it
+    x = torch.randint(-1000, 100000, (nscan,), dtype=torch.int32, device="cuda")
+    gb.exclusive_scan(x)
+    out = torch.empty(nscan, dtype=torch.int64, device="cuda")
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    reps = 5
+    e0.record(stream)
+    for _ in range(reps):
+        gb._lib.check(gb._lib.lib.gbfs_exclusive_scan_i32(gb._lib.C.c_void_p(x.data_ptr()),
+                                                          gb._lib.C.c_void_p(out.data_ptr()), nscan,
+                                                          gb._lib.C.c_void_p(stream.cuda_stream)), "scan")
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    peak, kind = measured_peak()
+    gbs = 12 * nscan / (ms / 1e3) / 1e9
+    res["exclusive_scan"] = {"workload": f"{nscan} int32 -> int64 exclusive prefix sum (12 B per element), "
+                                         "through the C ABI (each call reads its status back)",
+                             "ms": round(ms, 3), "GB_per_s": round(gbs, 1), "frac_of_hbm_peak": round(gbs / peak, 3),
+                             "peak_kind": kind}
+    return res
+
+
 def measure_serving(torch, seconds: float = 2.0, fractions=(0.25, 0.5, 0.75, 1.0), max_queries: int = 3000) -> dict:
     """32 resident graphs, Poisson arrivals at fractions of the measured capacity."""
     import gpu_graphs_gb300 as gb
@@ -358,14 +419,21 @@ def measure_serving(torch, seconds: float = 2.0, fractions=(0.25, 0.5, 0.75, 1.0
         return gi, int(rng.choice(nz[gi]))
 
     # plain: one query per launch, back to back, device-timed
-    plain_ms = sorted(graphs[gi].bfs(s0, stats=True)[1].ms for gi, s0 in (draw() for _ in range(96)))
+    draws = [draw() for _ in range(96)]
+    plain_ms = sorted(graphs[gi].bfs(s0, stats=True)[1].ms for gi, s0 in draws)
+    for g in graphs:
+        g.set_params(direction=1)
+    plain_td_ms = sum(graphs[gi].bfs(s0, stats=True)[1].ms for gi, s0 in draws)
+    for g in graphs:
+        g.set_params(direction=0)
     out = {"workload": "32 resident graphs: 16 RMAT scale U{12..22} ef 16, 16 grids side U[64, 4096]; "
                        "queries pick a graph uniformly and a source uniformly among degree>0 vertices; "
                        "4 slots, batch window max(0.5 ms, 50% of the graph's recent launch time); "
                        "results copied into pinned host buffers",
            "plain_one_query_per_launch": {"queries_per_s": round(len(plain_ms) / (sum(plain_ms) / 1e3), 1),
                                           "p50_ms": round(plain_ms[len(plain_ms) // 2], 3),
-                                          "p99_ms": round(plain_ms[int(0.99 * (len(plain_ms) - 1))], 3)}}
+                                          "p99_ms": round(plain_ms[int(0.99 * (len(plain_ms) - 1))], 3)},
+           "plain_topdown_queries_per_s": round(len(draws) / (plain_td_ms / 1e3), 1)}
     log("serving: plain baseline done")
     sweep = []
     with gb.Server(mem_budget_bytes=150 << 30, num_slots=4, max_lanes=64, batch_window_us=500,
@@ -418,6 +486,7 @@ def measure_serving(torch, seconds: float = 2.0, fractions=(0.25, 0.5, 0.75, 1.0
         out["peak_hbm_bytes"] = srv.stats()["peak_bytes"]
     out["sweep"] = sweep
     out["capacity_vs_plain"] = round(capacity / out["plain_one_query_per_launch"]["queries_per_s"], 2)
+    out["capacity_vs_plain_topdown"] = round(capacity / out["plain_topdown_queries_per_s"], 2)
     return out
 
 def main():
@@ -516,6 +585,8 @@ def main():
         log("grid done")
         extra["batched"] = measure_batched(torch)
         log("batched done")
+        extra["primitives"] = measure_primitives(torch)
+        log("primitives done")
     if rank == 0 and args.serving:
         extra["serving"] = measure_serving(torch)
 

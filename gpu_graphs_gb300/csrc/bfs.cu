@@ -111,17 +111,20 @@ __device__ __forceinline__ void claim_batch(const int (&w)[ILP], const BfsArgs &
 // Expand the rows of list[0, cnt) with the edges split evenly: each CTA
 // builds the degree prefix of a SEG-row segment in shared memory and warp g
 // of W takes edges [E*g/W, E*(g+1)/W) of it -- all warps of the grid when
-// the list is one segment, the CTA's own warps on its own segments beyond.
+// the list is one segment or `heavy` (every row long, so each segment holds
+// enough edges for the whole grid: segments are walked one after another),
+// the CTA's own warps on its own segments otherwise.
 template <int BLOCK>
 __device__ void grid_expand_list(const int *list, int cnt, const BfsArgs &a, int nl, WarpQ &q,
                                  unsigned long long *cnt_next, int *qn, unsigned long long &my_deg, int *s_pre,
-                                 int *s_beg, int *s_warp)
+                                 int *s_beg, int *s_warp, bool heavy = false)
 {
     constexpr int PER = SEG / BLOCK;
     const int lane = (int)lane_id();
-    // One segment: the grid's warps split its edges.  More: CTA b takes
-    // segments b, b+G, ... and its own warps split each one.
-    const bool one_seg = cnt <= SEG;
+    // One segment (or long rows): the grid's warps split each segment's
+    // edges.  Otherwise CTA b takes segments b, b+G, ... and its own warps
+    // split each one.
+    const bool one_seg = cnt <= SEG || heavy;
     const long long gwarp = one_seg ? ((long long)blockIdx.x * BLOCK + threadIdx.x) >> 5 : (long long)(threadIdx.x >> 5);
     const long long nwarps = one_seg ? ((long long)gridDim.x * BLOCK) >> 5 : (long long)(BLOCK / 32);
     const int seg0 = one_seg ? 0 : (int)blockIdx.x * SEG;
@@ -424,7 +427,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
             traced_big = nb > 0;
             if (nb > 0) {
                 my_deg = 0;
-                grid_expand_list<BLOCK>(a.bigl, nb, a, nl, q, cnt_next, qn, my_deg, s_pre, s_beg, s_warp);
+                grid_expand_list<BLOCK>(a.bigl, nb, a, nl, q, cnt_next, qn, my_deg, s_pre, s_beg, s_warp, true);
                 block_flush(q, cnt_next, qn, s_wq, &s_base);
                 const unsigned long long bd = block_reduce_sum(my_deg, s_red);
                 if (threadIdx.x == 0 && bd) atomicAdd(deg_next, bd);

@@ -9,12 +9,25 @@ namespace {
 constexpr unsigned ST_AGG = 1, ST_INC = 2;
 constexpr unsigned long long LOOKBACK_TIMEOUT_NS = 2000000000ULL;  // 2 s
 
+// Shared-memory index of tile element i with one pad word per 32 words, so
+// the blocked accesses (thread t: elements t*SCAN_ITEMS ... ) spread over the
+// banks; 8-byte elements are padded per 16.
+template <typename T>
+__device__ __forceinline__ int pad_index(int i)
+{
+    return sizeof(T) == 8 ? i + (i >> 4) : i + (i >> 5);
+}
+
 template <typename Tin, typename Tout>
-__global__ void __launch_bounds__(SCAN_THREADS)
+__global__ void __launch_bounds__(SCAN_THREADS, 4)
 k_scan_exclusive(const Tin *__restrict__ in, Tout *__restrict__ out, int64_t n,
                  Tout *__restrict__ total_out, unsigned *flags, long long *agg,
                  long long *inc, unsigned *ctl, unsigned epoch, int64_t ntiles)
 {
+    // staging area for the tile: read and written coalesced (striped), used
+    // blocked by the scan
+    constexpr int STAGE_WORDS = (SCAN_TILE + SCAN_TILE / 16) * 8 / 4;
+    __shared__ __align__(16) int s_stage[STAGE_WORDS];
     __shared__ long long s_warp[SCAN_THREADS / 32];
     __shared__ long long s_prefix;
     __shared__ unsigned s_tile;
@@ -22,77 +35,106 @@ k_scan_exclusive(const Tin *__restrict__ in, Tout *__restrict__ out, int64_t n,
     if (threadIdx.x == 0) s_tile = atomicAdd(&ctl[0], 1u);
     __syncthreads();
     const int64_t tile = s_tile;
-    const int64_t base = tile * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+    const int64_t tbase = tile * SCAN_TILE;
 
-    long long v[SCAN_ITEMS];
+    Tin *s_in = reinterpret_cast<Tin *>(s_stage);
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        const int j = k * SCAN_THREADS + threadIdx.x;
+        const int64_t i = tbase + j;
+        s_in[pad_index<Tin>(j)] = i < n ? in[i] : Tin(0);
+    }
+    __syncthreads();
+    Tin v[SCAN_ITEMS];
     long long sum = 0;
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS; k++) {
-        int64_t i = base + k;
-        v[k] = i < n ? (long long)in[i] : 0;
-        sum += v[k];
+        v[k] = s_in[pad_index<Tin>(threadIdx.x * SCAN_ITEMS + k)];
+        sum += (long long)v[k];
     }
     // Block exclusive scan of the per-thread sums.
     const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    long long incl = warp_incl_scan(sum);
+    const long long incl = warp_incl_scan(sum);
     if (lane == 31) s_warp[warp] = incl;
     __syncthreads();
     if (warp == 0) {
-        long long w = lane < SCAN_THREADS / 32 ? s_warp[lane] : 0;
-        long long wi = warp_incl_scan(w);
+        const long long w = lane < SCAN_THREADS / 32 ? s_warp[lane] : 0;
+        const long long wi = warp_incl_scan(w);
         if (lane < SCAN_THREADS / 32) s_warp[lane] = wi - w;  // exclusive warp offsets
-        if (lane == SCAN_THREADS / 32 - 1) {
-            // lane 7 holds the tile aggregate in wi
-            long long tile_sum = wi;
-            unsigned tag = epoch << 2;
-            if (tile == 0) {
+        const long long tile_sum = __shfl_sync(FULL, wi, SCAN_THREADS / 32 - 1);
+        const unsigned tag = epoch << 2;
+        long long prefix = 0;
+        if (tile == 0) {
+            if (lane == 0) {
                 inc[0] = tile_sum;
                 __threadfence();
                 st_release_gpu(&flags[0], tag | ST_INC);
-                s_prefix = 0;
-            } else {
+            }
+        } else {
+            if (lane == 0) {
                 agg[tile] = tile_sum;
                 __threadfence();
                 st_release_gpu(&flags[tile], tag | ST_AGG);
-                // Look back over predecessors until an inclusive prefix.
-                long long prefix = 0;
-                int64_t p = tile - 1;
-                unsigned long long t0 = globaltimer_ns();
-                unsigned spins = 0;
-                bool failed = false;
-                while (p >= 0) {
-                    unsigned f = ld_acquire_gpu(&flags[p]);
-                    if ((f >> 2) == (epoch & 0x3fffffffu) && (f & 3u) != 0) {
-                        if ((f & 3u) == ST_INC) {
-                            prefix += (long long)ld_relaxed_u64((const unsigned long long *)&inc[p]);
-                            break;
-                        }
-                        prefix += (long long)ld_relaxed_u64((const unsigned long long *)&agg[p]);
-                        p--;
-                        continue;
-                    }
-                    if ((++spins & 31u) == 0 && globaltimer_ns() - t0 > LOOKBACK_TIMEOUT_NS) {
-                        atomicExch(&ctl[2], (unsigned)DEV_TIMEOUT);
-                        failed = true;
-                        break;
-                    }
+            }
+            // Warp-wide look-back: lane l reads predecessor p - l.  The window
+            // is usable once every lane up to the nearest inclusive prefix
+            // has published; then the aggregates before it and that prefix
+            // are summed, else all 32 aggregates are and the window moves on.
+            int64_t p = tile - 1;
+            const unsigned long long t0 = globaltimer_ns();
+            unsigned spins = 0;
+            for (;;) {
+                const int64_t idx = p - (int64_t)lane;
+                unsigned f = tag | ST_INC;  // before tile 0: an inclusive prefix of 0
+                if (idx >= 0) f = ld_acquire_gpu(&flags[idx]);
+                const bool ok = (f >> 2) == (epoch & 0x3fffffffu) && (f & 3u) != 0;
+                const unsigned okm = __ballot_sync(FULL, ok);
+                const unsigned incm = __ballot_sync(FULL, ok && (f & 3u) == ST_INC);
+                const int first_inc = incm ? __ffs(incm) - 1 : 32;
+                const unsigned need = first_inc < 31 ? ((2u << first_inc) - 1u) : FULL;
+                if ((okm & need) == need) {
+                    long long val = 0;
+                    if ((int)lane <= first_inc && idx >= 0)
+                        val = (int)lane == first_inc ? (long long)ld_relaxed_u64((const unsigned long long *)&inc[idx])
+                                                     : (long long)ld_relaxed_u64((const unsigned long long *)&agg[idx]);
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(FULL, val, o);
+                    prefix += val;
+                    if (first_inc < 32) break;
+                    p -= 32;
+                    continue;
                 }
-                if (failed) prefix = 0;
+                if ((++spins & 31u) == 0 && globaltimer_ns() - t0 > LOOKBACK_TIMEOUT_NS) {
+                    if (lane == 0) atomicExch(&ctl[2], (unsigned)DEV_TIMEOUT);
+                    prefix = 0;
+                    break;
+                }
+            }
+            if (lane == 0) {
                 inc[tile] = prefix + tile_sum;
                 __threadfence();
                 st_release_gpu(&flags[tile], tag | ST_INC);
-                s_prefix = prefix;
             }
-            if (tile == ntiles - 1 && total_out) *total_out = (Tout)(s_prefix + tile_sum);
+        }
+        if (lane == 0) {
+            s_prefix = prefix;
+            if (tile == ntiles - 1 && total_out) *total_out = (Tout)(prefix + tile_sum);
         }
     }
-    __syncthreads();
+    __syncthreads();  // also: every thread has read its inputs from s_stage
     long long run = s_prefix + s_warp[warp] + (incl - sum);
+    Tout *s_out = reinterpret_cast<Tout *>(s_stage);
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS; k++) {
-        int64_t i = base + k;
-        if (i < n) out[i] = (Tout)run;
-        run += v[k];
+        s_out[pad_index<Tout>(threadIdx.x * SCAN_ITEMS + k)] = (Tout)run;
+        run += (long long)v[k];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        const int j = k * SCAN_THREADS + threadIdx.x;
+        const int64_t i = tbase + j;
+        if (i < n) out[i] = s_out[pad_index<Tout>(j)];
     }
     // Self-cleaning counters: the last tile to finish resets them.
     if (threadIdx.x == 0) {

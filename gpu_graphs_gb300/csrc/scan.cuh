@@ -3,9 +3,11 @@
 // Replaces the reference's three-launch recursive Blelloch scan
 // (2D Partition/src/prefixSum.cu:15-224, which cudaMallocs and frees its
 // block-sum arrays on every call) with one launch: each tile of
-// SCAN_THREADS * SCAN_ITEMS elements scans itself with warp shuffles,
-// publishes its aggregate, looks back over its predecessors' published
-// aggregates / inclusive prefixes, and publishes its inclusive prefix.
+// SCAN_THREADS * SCAN_ITEMS elements is staged through shared memory (loads
+// and stores coalesced), scans itself with warp shuffles, publishes its
+// aggregate, looks back over its predecessors' published aggregates /
+// inclusive prefixes 32 at a time (one warp), and publishes its inclusive
+// prefix.
 // Tiles take ids from an atomic counter in launch order, so a tile only
 // ever waits on tiles that are already running.  The scratch is
 // self-cleaning (epoch-tagged flags, counters reset by the last tile), so
@@ -18,7 +20,7 @@
 namespace gbfs {
 
 constexpr int SCAN_THREADS = 256;
-constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_ITEMS = 16;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
 struct ScanScratch {
