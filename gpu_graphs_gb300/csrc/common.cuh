@@ -81,6 +81,13 @@ __device__ __forceinline__ unsigned atom_add_acq_rel_gpu(unsigned *p, unsigned v
     return old;
 }
 
+__device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned *p)
+{
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
 __device__ __forceinline__ int ld_relaxed_i32(const int *p)
 {
     int v;

@@ -35,7 +35,7 @@ namespace {
 constexpr int MS_BLOCK = 512;
 constexpr int MS_SEG = 2048;                 // queue entries per edge-balanced pass
 constexpr int MS_PER = MS_SEG / MS_BLOCK;    // entries per thread in the prefix
-constexpr int MS_GRID_SEGS = 8;              // queues up to 8 segments are split grid-wide
+constexpr int MS_BIG = 256;                  // push rows this long go to a grid-wide pass
 
 struct MsArgs {
     int n, n_active, k;
@@ -47,6 +47,7 @@ struct MsArgs {
     unsigned long long *hacc;
     unsigned *hcnt;
     unsigned long long *vis;
+    int *bigl;
     unsigned long long *F[3];
     int *Q[4];
     int *out;
@@ -104,6 +105,99 @@ __device__ __forceinline__ void write_levels_warp(unsigned char *lv8, int *out, 
         const int j = __ffsll((long long)any) - 1;
         if ((bits >> j) & 1ull) record_level(lv8, out, n, u, j, nl);
         any &= any - 1ull;
+    }
+}
+
+// Push step over list[0, cnt): every edge offers its row's frontier lanes
+// to the neighbour.  grid_wide: all warps of the grid split each MS_SEG-row
+// segment's edges (segments one after another); otherwise CTA b takes
+// segments b, b+G, ... of about cnt/G rows and its own warps split them.
+// defer: rows of MS_BIG edges or more are appended to a.bigl (count in
+// *bigcnt) instead.  Each edge claims its lanes at the neighbour with one
+// atomicOr on vis (after a plain-load filter; vis only gains bits, and the
+// atomic's old value settles which lanes this edge discovers, so every
+// (lane, vertex) pair is claimed exactly once), and the claimed lanes go
+// into the next frontier mask with a second atomicOr whose first writer
+// queues the neighbour.  All threads of the CTA call it.
+__device__ __forceinline__ void push_rows(const MsArgs &a, const int *list, long long cnt, bool grid_wide, bool defer,
+                                          int nl, const unsigned long long *Fc, unsigned long long *Fn, WarpQ &q,
+                                          unsigned long long *qcnt_next, int *Qn, unsigned long long &my_or,
+                                          int *s_pre, int *s_beg, unsigned long long *s_f, int *s_warp,
+                                          unsigned long long *bigcnt)
+{
+    const unsigned lane = lane_id();
+    const long long gwarp = ((long long)blockIdx.x * MS_BLOCK + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * MS_BLOCK) >> 5;
+    const long long cta_seg = min((long long)MS_SEG, max(32LL, (cnt + gridDim.x - 1) / gridDim.x));
+    const long long seg_len = grid_wide ? MS_SEG : cta_seg;
+    const long long seg0 = grid_wide ? 0 : (long long)blockIdx.x * seg_len;
+    const long long seg_step = grid_wide ? MS_SEG : (long long)gridDim.x * seg_len;
+    const long long wid = grid_wide ? gwarp : (long long)(threadIdx.x >> 5);
+    const long long wcount = grid_wide ? nwarps : (long long)(MS_BLOCK / 32);
+    const int n = a.n;
+    for (long long seg = seg0; seg < cnt; seg += seg_step) {
+        const int segn = (int)min(seg_len, cnt - seg);
+        int d[MS_PER];
+        int sum = 0;
+#pragma unroll
+        for (int t = 0; t < MS_PER; t++) {
+            const int j = threadIdx.x * MS_PER + t;
+            d[t] = 0;
+            if (j < segn) {
+                const int v = __ldcg(list + seg + j);
+                const int b = __ldg(a.row + v);
+                s_beg[j] = b;
+                s_f[j] = __ldcg(Fc + v);
+                d[t] = __ldg(a.row + v + 1) - b;
+                if (defer && d[t] >= MS_BIG) {
+                    a.bigl[atomicAdd(bigcnt, 1ull)] = v;
+                    d[t] = 0;
+                }
+            }
+            sum += d[t];
+        }
+        int total;
+        int run = block_excl_scan_int(sum, s_warp, &total);
+#pragma unroll
+        for (int t = 0; t < MS_PER; t++) {
+            const int j = threadIdx.x * MS_PER + t;
+            if (j < segn) s_pre[j] = run;
+            run += d[t];
+        }
+        __syncthreads();
+        const long long lo = (long long)total * wid / wcount;
+        const long long hi = (long long)total * (wid + 1) / wcount;
+        for (long long e0 = lo; e0 < hi; e0 += 64) {
+            int uu[2];
+            bool tt[2];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const long long e = e0 + h * 32 + lane;
+                uu[h] = -1;
+                tt[h] = false;
+                if (e < hi) {
+                    int l = 0, r = segn - 1;  // max j with s_pre[j] <= e
+                    while (l < r) {
+                        const int mid = (l + r + 1) >> 1;
+                        if (s_pre[mid] <= e) l = mid; else r = mid - 1;
+                    }
+                    const int u = __ldg(a.col + s_beg[l] + (int)(e - s_pre[l]));
+                    unsigned long long nw = s_f[l] & ~a.vis[u];
+                    if (nw) {
+                        nw &= ~atomicOr(a.vis + u, nw);
+                        if (nw) {
+                            tt[h] = atomicOr(Fn + u, nw) == 0ull;
+                            uu[h] = u;
+                            my_or |= nw;
+                            write_levels(a.lv8, a.out, n, u, nw, nl);
+                        }
+                    }
+                }
+            }
+            wq_push(q, tt[0], uu[0], qcnt_next, Qn);
+            wq_push(q, tt[1], uu[1], qcnt_next, Qn);
+        }
+        __syncthreads();
     }
 }
 
@@ -168,6 +262,7 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
             ctrl->alive[i] = 0;
         }
         ctrl->alive[0] = all;
+        ctrl->big[0] = ctrl->big[1] = 0;
         ctrl->reached = 0;
         ctrl->edges_c = 0;
     }
@@ -207,6 +302,7 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
         if (gtid == 0) {
             ctrl->qcnt[(L + 2) % 4] = 0;
             ctrl->alive[(L + 2) % 4] = 0;
+            ctrl->big[(L + 1) & 1] = 0;  // last read during level L-1
         }
         for (long long i = gtid; i < (long long)nz; i += gthreads) Fz[__ldcg(Qz + i)] = 0;
 
@@ -367,87 +463,29 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
             if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
         } else {
             ++push_levels;
-            // the queue's edges.  Up to MS_GRID_SEGS segments of MS_SEG rows:
-            // every CTA builds each segment's degree prefix and the grid's warps
-            // split its edges evenly (hub rows of power-law graphs appear in
-            // these short early queues).  Longer queues: CTA b takes segments
-            // b, b+G, ... sized so every CTA gets about one, and its own warps
-            // split each one.
-            const bool one_seg = nq <= (unsigned long long)MS_SEG * MS_GRID_SEGS;
-            const long long cta_seg = min((long long)MS_SEG, max(32LL, ((long long)nq + gridDim.x - 1) / gridDim.x));
-            const long long seg_len = one_seg ? MS_SEG : cta_seg;
-            const long long seg0 = one_seg ? 0 : (long long)blockIdx.x * seg_len;
-            const long long seg_step = one_seg ? MS_SEG : (long long)gridDim.x * seg_len;
-            const long long wid = one_seg ? gwarp : (long long)(threadIdx.x >> 5);
-            const long long wcount = one_seg ? nwarps : (long long)(MS_BLOCK / 32);
-            for (long long seg = seg0; seg < (long long)nq; seg += seg_step) {
-                const int segn = (int)min(seg_len, (long long)nq - seg);
-                int d[MS_PER];
-                int sum = 0;
-#pragma unroll
-                for (int t = 0; t < MS_PER; t++) {
-                    const int j = threadIdx.x * MS_PER + t;
-                    d[t] = 0;
-                    if (j < segn) {
-                        const int v = __ldcg(Qc + seg + j);
-                        const int b = __ldg(a.row + v);
-                        s_beg[j] = b;
-                        s_f[j] = __ldcg(Fc + v);
-                        d[t] = __ldg(a.row + v + 1) - b;
-                    }
-                    sum += d[t];
-                }
-                int total;
-                int run = block_excl_scan_int(sum, s_warp, &total);
-#pragma unroll
-                for (int t = 0; t < MS_PER; t++) {
-                    const int j = threadIdx.x * MS_PER + t;
-                    if (j < segn) s_pre[j] = run;
-                    run += d[t];
-                }
-                __syncthreads();
-                const long long lo = (long long)total * wid / wcount;
-                const long long hi = (long long)total * (wid + 1) / wcount;
-                for (long long e0 = lo; e0 < hi; e0 += 64) {
-                    int uu[2];
-                    bool tt[2];
-#pragma unroll
-                    for (int h = 0; h < 2; h++) {
-                        const long long e = e0 + h * 32 + lane;
-                        uu[h] = -1;
-                        tt[h] = false;
-                        if (e < hi) {
-                            int l = 0, r = segn - 1;  // max j with s_pre[j] <= e
-                            while (l < r) {
-                                const int mid = (l + r + 1) >> 1;
-                                if (s_pre[mid] <= e) l = mid; else r = mid - 1;
-                            }
-                            const int u = __ldg(a.col + s_beg[l] + (int)(e - s_pre[l]));
-                            // lanes of this edge not yet at u.  vis may be read
-                            // stale (it only gains bits): the atomic's old value
-                            // settles which lanes this edge discovers, so every
-                            // (lane, vertex) pair is claimed exactly once
-                            unsigned long long nw = s_f[l] & ~a.vis[u];
-                            if (nw) {
-                                nw &= ~atomicOr(a.vis + u, nw);
-                                if (nw) {
-                                    // the first claim of u in this level queues it
-                                    tt[h] = atomicOr(Fn + u, nw) == 0ull;
-                                    uu[h] = u;
-                                    my_or |= nw;
-                                    write_levels(a.lv8, a.out, n, u, nw, nl);
-                                }
-                            }
-                        }
-                    }
-                    wq_push(q, tt[0], uu[0], qcnt_next, Qn);
-                    wq_push(q, tt[1], uu[1], qcnt_next, Qn);
-                }
-                __syncthreads();
-            }
+            // the queue's edges.  A queue of at most MS_SEG rows: every CTA
+            // builds its degree prefix and the grid's warps split the edges
+            // evenly.  Longer queues: CTA b takes segments b, b+G, ... sized so
+            // every CTA gets about one and its own warps split them, with rows
+            // of MS_BIG edges or more deferred to a second, grid-wide pass
+            // (hub rows of power-law graphs would leave a few CTAs with most
+            // of the edges).
+            const bool grid_wide = nq <= (unsigned long long)MS_SEG;
+            unsigned long long *bigcnt = &ctrl->big[L & 1];
+            push_rows(a, Qc, (long long)nq, grid_wide, !grid_wide, nl, Fc, Fn, q, qcnt_next, Qn, my_or, s_pre,
+                      s_beg, s_f, s_warp, bigcnt);
             block_flush(q, qcnt_next, Qn, s_wq, &s_base);
             or_into(my_or, &ctrl->alive[(L + 1) % 4], s_red);
             if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
+            const unsigned long long nb = grid_wide ? 0ull : ld_relaxed_u64(bigcnt);
+            if (nb) {
+                my_or = 0;
+                push_rows(a, a.bigl, (long long)nb, true, false, nl, Fc, Fn, q, qcnt_next, Qn, my_or, s_pre, s_beg,
+                          s_f, s_warp, bigcnt);
+                block_flush(q, qcnt_next, Qn, s_wq, &s_base);
+                or_into(my_or, &ctrl->alive[(L + 1) % 4], s_red);
+                if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
+            }
         }
         if (gtid == 0) {
             LevelTrace t;
@@ -586,7 +624,7 @@ int ms_work_alloc(MsWork &w, int32_t n, std::string &err)
     w.bytes = 0;
     const size_t b8 = sizeof(unsigned long long) * (size_t)n, b4 = sizeof(int) * (size_t)n;
     bool ok = al((void **)&w.vis, b8) && al((void **)&w.hacc, b8) && al((void **)&w.hcnt, b4) &&
-              al((void **)&w.lv8, (size_t)n * MS_LANES) &&
+              al((void **)&w.lv8, (size_t)n * MS_LANES) && al((void **)&w.bigl, b4) &&
               al((void **)&w.out, b4 * MS_LANES) && al((void **)&w.src, sizeof(int) * MS_LANES) &&
               al((void **)&w.ctrl, sizeof(MsCtrl));
     for (int i = 0; ok && i < 3; i++) ok = al((void **)&w.F[i], b8);
@@ -608,7 +646,7 @@ int ms_work_alloc(MsWork &w, int32_t n, std::string &err)
 
 void ms_work_free(MsWork &w)
 {
-    void *ps[] = {w.vis, w.hacc, w.hcnt, w.lv8, w.out, w.src, w.ctrl, w.F[0], w.F[1], w.F[2], w.Q[0], w.Q[1], w.Q[2], w.Q[3]};
+    void *ps[] = {w.vis, w.hacc, w.hcnt, w.lv8, w.bigl, w.out, w.src, w.ctrl, w.F[0], w.F[1], w.F[2], w.Q[0], w.Q[1], w.Q[2], w.Q[3]};
     for (void *p : ps)
         if (p) cudaFree(p);
     if (w.h_ctrl) cudaFreeHost(w.h_ctrl);
@@ -619,7 +657,7 @@ void ms_work_free(MsWork &w)
 
 int64_t ms_work_bytes(int64_t n)
 {
-    return n > 0 ? (int64_t)(8 * 5 + 4 * 5 + 5 * MS_LANES) * n + 4096 : 0;
+    return n > 0 ? (int64_t)(8 * 5 + 4 * 6 + 5 * MS_LANES) * n + 4096 : 0;
 }
 
 cudaError_t msbfs_enqueue(const DeviceCsr &g, const gbfs_params &p, bool pull_allowed, MsWork &w,
@@ -643,6 +681,7 @@ cudaError_t msbfs_enqueue(const DeviceCsr &g, const gbfs_params &p, bool pull_al
     for (int i = 0; i < 4; i++) a.Q[i] = w.Q[i];
     a.out = d_out;
     a.lv8 = w.lv8;
+    a.bigl = w.bigl;
     a.src = d_src;
     a.ctrl = w.ctrl;
     a.pull_allowed = pull_allowed ? 1 : 0;

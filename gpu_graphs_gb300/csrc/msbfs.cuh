@@ -22,6 +22,7 @@ struct MsCtrl {
     int pad0;
     unsigned long long qcnt[4];  // active-queue lengths, rotating by level
     unsigned long long alive[4]; // lanes with a non-empty frontier, rotating by level
+    unsigned long long big[2];   // long rows a push step deferred to its grid-wide pass
     int levels, push_levels, pull_levels, trace_len;
     unsigned long long reached, edges_c;
     unsigned long long t_entry, t_start, t_end;
@@ -37,6 +38,7 @@ struct MsWork {
     unsigned long long *hacc = nullptr;  // n: per huge row, lanes its pull pieces found
     unsigned *hcnt = nullptr;            // n: per huge row, pieces done this level
     unsigned char *lv8 = nullptr;        // MS_LANES * n levels as bytes while the search runs
+    int *bigl = nullptr;                 // n: long rows deferred by a push step
     int *out = nullptr;                  // MS_LANES * n levels (host-bound results)
     int *src = nullptr;                  // MS_LANES sources
     MsCtrl *ctrl = nullptr;

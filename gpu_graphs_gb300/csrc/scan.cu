@@ -19,15 +19,14 @@ __device__ __forceinline__ int pad_index(int i)
 }
 
 template <typename Tin, typename Tout>
-__global__ void __launch_bounds__(SCAN_THREADS, 4)
+__global__ void __launch_bounds__(SCAN_THREADS, 1)
 k_scan_exclusive(const Tin *__restrict__ in, Tout *__restrict__ out, int64_t n,
                  Tout *__restrict__ total_out, unsigned *flags, long long *agg,
                  long long *inc, unsigned *ctl, unsigned epoch, int64_t ntiles)
 {
-    // staging area for the tile: read and written coalesced (striped), used
-    // blocked by the scan
-    constexpr int STAGE_WORDS = (SCAN_TILE + SCAN_TILE / 16) * 8 / 4;
-    __shared__ __align__(16) int s_stage[STAGE_WORDS];
+    // staging area for the tile (dynamic, scan_stage_bytes()): read and
+    // written coalesced (striped), used blocked by the scan
+    extern __shared__ __align__(16) int s_stage[];
     __shared__ long long s_warp[SCAN_THREADS / 32];
     __shared__ long long s_prefix;
     __shared__ unsigned s_tile;
@@ -86,13 +85,14 @@ k_scan_exclusive(const Tin *__restrict__ in, Tout *__restrict__ out, int64_t n,
             for (;;) {
                 const int64_t idx = p - (int64_t)lane;
                 unsigned f = tag | ST_INC;  // before tile 0: an inclusive prefix of 0
-                if (idx >= 0) f = ld_acquire_gpu(&flags[idx]);
+                if (idx >= 0) f = ld_relaxed_u32(&flags[idx]);
                 const bool ok = (f >> 2) == (epoch & 0x3fffffffu) && (f & 3u) != 0;
                 const unsigned okm = __ballot_sync(FULL, ok);
                 const unsigned incm = __ballot_sync(FULL, ok && (f & 3u) == ST_INC);
                 const int first_inc = incm ? __ffs(incm) - 1 : 32;
                 const unsigned need = first_inc < 31 ? ((2u << first_inc) - 1u) : FULL;
                 if ((okm & need) == need) {
+                    __threadfence();  // acquire: the values published with those flags
                     long long val = 0;
                     if ((int)lane <= first_inc && idx >= 0)
                         val = (int)lane == first_inc ? (long long)ld_relaxed_u64((const unsigned long long *)&inc[idx])
@@ -136,17 +136,9 @@ k_scan_exclusive(const Tin *__restrict__ in, Tout *__restrict__ out, int64_t n,
         const int64_t i = tbase + j;
         if (i < n) out[i] = s_out[pad_index<Tout>(j)];
     }
-    // Self-cleaning counters: the last tile to finish resets them.
-    if (threadIdx.x == 0) {
-        __threadfence();
-        unsigned done = atomicAdd(&ctl[1], 1u);
-        if (done == (unsigned)(ntiles - 1)) {
-            ctl[0] = 0;
-            ctl[1] = 0;
-            __threadfence();
-        }
-    }
 }
+
+constexpr size_t scan_stage_bytes() { return (size_t)(SCAN_TILE + SCAN_TILE / 16) * 8; }
 
 template <typename Tin, typename Tout>
 cudaError_t launch_scan(const Tin *in, Tout *out, int64_t n, Tout *total_out, ScanScratch &s,
@@ -160,7 +152,17 @@ cudaError_t launch_scan(const Tin *in, Tout *out, int64_t n, Tout *total_out, Sc
     if (ntiles > s.max_tiles || ntiles > 0x7fffffff) return cudaErrorInvalidValue;
     s.epoch = (s.epoch + 1) & 0x3fffffffu;
     if (s.epoch == 0) s.epoch = 1;
-    k_scan_exclusive<Tin, Tout><<<(unsigned)ntiles, SCAN_THREADS, 0, st>>>(
+    static bool attr_set = false;  // per template instance
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_scan_exclusive<Tin, Tout>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)scan_stage_bytes());
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    // the tile ticket starts at zero (flags carry the call number instead)
+    cudaError_t e = cudaMemsetAsync(s.ctl, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    k_scan_exclusive<Tin, Tout><<<(unsigned)ntiles, SCAN_THREADS, scan_stage_bytes(), st>>>(
         in, out, n, total_out, s.flags, s.agg, s.inc, s.ctl, s.epoch, ntiles);
     return cudaGetLastError();
 }

@@ -19,7 +19,7 @@
 
 namespace gbfs {
 
-constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_THREADS = 1024;
 constexpr int SCAN_ITEMS = 16;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 

@@ -128,7 +128,8 @@ def test_autotune_keeps_levels_and_caches(gb, orc):
 
 def test_multi_source_huge_rows(gb, orc):
     """Rows far above the pull piece size (hubs of degree 30000 and 9000) are
-    scanned in pieces by many warps and settled by the last one."""
+    scanned in pieces by many warps and settled by the last one (pull), or
+    deferred from CTA segments to a grid-wide pass (push only)."""
     n = 60000
     s1, d1 = gb.gen_er(n, 90000, seed=51)
     rng = np.random.default_rng(52)
@@ -141,7 +142,7 @@ def test_multi_source_huge_rows(gb, orc):
     deg = np.diff(o.row_offset)
     assert deg.max() > 4 * 2048
     sources = list(rng.choice(np.flatnonzero(deg > 0), 64, replace=False))
-    for direction in (0, 2):
+    for direction in (0, 1, 2):
         g.set_params(direction=direction)
         got = g.bfs_multi(sources)
         for i, s in enumerate(sources):
