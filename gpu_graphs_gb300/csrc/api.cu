@@ -420,16 +420,31 @@ extern "C" int gbfs_bfs_many(gbfs_graph *g, const int32_t *sources, int32_t k, i
         }
         return GBFS_OK;
     }
+    const bool host_out = levels_out && !dev_out;
+    if (host_out) {
+        rc = bfs_work_reserve_overlap(w, err);
+        if (rc) return fail(rc, err);
+    }
     cudaError_t e = cudaSuccess;
     for (int32_t i = 0; i < k && e == cudaSuccess; i++) {
-        int *d_level = dev_out ? levels_out + n * i : w.level;
-        e = cudaEventRecord(w.evs[i], g->stream);
+        // host output: results alternate between two device buffers and are
+        // copied on a second stream while the next traversal runs; launch i
+        // waits for the copy that last used its buffer (launch i - 2)
+        int *d_level = dev_out ? levels_out + n * i : (host_out && (i & 1)) ? w.level2 : w.level;
+        if (host_out && i >= 2) e = cudaStreamWaitEvent(g->stream, w.ev_copied[i & 1], 0);
+        if (e == cudaSuccess) e = cudaEventRecord(w.evs[i], g->stream);
         if (e == cudaSuccess)
             e = bfs_enqueue(g->csr, p, w, nullptr, 1, hsrc[i], d_level, w.d_outs + i, g->stream, g->symmetric);
-        if (e == cudaSuccess && levels_out && !dev_out)
-            e = cudaMemcpyAsync(levels_out + n * i, d_level, sizeof(int) * n, cudaMemcpyDeviceToHost, g->stream);
+        if (e == cudaSuccess && host_out) {
+            e = cudaEventRecord(w.ev_ready[i & 1], g->stream);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(w.copy_st, w.ev_ready[i & 1], 0);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(levels_out + n * i, d_level, sizeof(int) * n, cudaMemcpyDeviceToHost, w.copy_st);
+            if (e == cudaSuccess) e = cudaEventRecord(w.ev_copied[i & 1], w.copy_st);
+        }
     }
     if (e == cudaSuccess) e = cudaEventRecord(w.evs[k], g->stream);
+    if (e == cudaSuccess && host_out) e = cudaStreamSynchronize(w.copy_st);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(w.h_outs, w.d_outs, sizeof(BfsOut) * (size_t)k, cudaMemcpyDeviceToHost, g->stream);
     if (e == cudaSuccess)

@@ -701,7 +701,36 @@ void bfs_work_free(BfsWork &w)
     if (w.h_ctrl) cudaFreeHost(w.h_ctrl);
     if (w.ev0) cudaEventDestroy(w.ev0);
     if (w.ev1) cudaEventDestroy(w.ev1);
+    if (w.level2) cudaFree(w.level2);
+    if (w.copy_st) cudaStreamDestroy(w.copy_st);
+    for (int i = 0; i < 2; i++) {
+        if (w.ev_ready[i]) cudaEventDestroy(w.ev_ready[i]);
+        if (w.ev_copied[i]) cudaEventDestroy(w.ev_copied[i]);
+    }
     w = BfsWork{};
+}
+
+int bfs_work_reserve_overlap(BfsWork &w, std::string &err)
+{
+    if (w.level2) return GBFS_OK;
+    cudaError_t e = cudaMalloc(&w.level2, sizeof(int) * (size_t)std::max(1, w.n));
+    if (e != cudaSuccess) {
+        w.level2 = nullptr;
+        err = "second level buffer";
+        return GBFS_ERR_OOM;
+    }
+    w.bytes += (int64_t)sizeof(int) * std::max(1, w.n);
+    if (cudaStreamCreateWithFlags(&w.copy_st, cudaStreamNonBlocking) != cudaSuccess) {
+        err = "copy stream";
+        return GBFS_ERR_CUDA;
+    }
+    for (int i = 0; i < 2; i++)
+        if (cudaEventCreateWithFlags(&w.ev_ready[i], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&w.ev_copied[i], cudaEventDisableTiming) != cudaSuccess) {
+            err = "copy events";
+            return GBFS_ERR_CUDA;
+        }
+    return GBFS_OK;
 }
 
 cudaError_t bfs_enqueue(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_roots, int k,

@@ -77,8 +77,16 @@ struct BfsWork {
     int outs_cap = 0;
     cudaEvent_t *evs = nullptr;
     int evs_cap = 0;
+    // back-to-back launches with host output: a second level buffer and a
+    // copy stream, so the copy of one result overlaps the next traversal
+    int *level2 = nullptr;
+    cudaStream_t copy_st = nullptr;
+    cudaEvent_t ev_ready[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
     int64_t bytes = 0;
 };
+
+// Allocate the second level buffer, the copy stream and its events.
+int bfs_work_reserve_overlap(BfsWork &w, std::string &err);
 
 int bfs_work_alloc(BfsWork &w, int32_t n, std::string &err);
 void bfs_work_free(BfsWork &w);

@@ -175,9 +175,11 @@ int gbfs_bfs_parents(gbfs_graph *g, int32_t source, int32_t *levels_out,
  * k single-source searches run back to back, one launch each, queued on the
  * graph's stream with no host round trip in between (the plain
  * one-query-per-launch BFS).  levels_out: k*n int32 (host or device; row i
- * for sources[i]) or NULL to discard the levels.  stats: k entries
- * (nullable); stats[i].ms spans launch i (and its D2H copy when levels_out
- * is on the host).
+ * for sources[i]) or NULL to discard the levels.  With levels_out on the
+ * host, results alternate between two device buffers and each is copied
+ * on a second stream while the next search runs.  stats: k entries
+ * (nullable); stats[i].ms spans launch i on the graph's stream (with host
+ * output, plus any wait for the copy two launches back to free its buffer).
  */
 int gbfs_bfs_many(gbfs_graph *g, const int32_t *sources, int32_t k,
                   int32_t *levels_out, gbfs_stats *stats);

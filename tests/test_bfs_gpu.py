@@ -235,3 +235,34 @@ def test_hub_first_layout(gb, orc):
     g3 = gb.Graph.from_csr(o2.row_offset.astype(np.int32), rev)
     g3.set_params(direction=2)
     assert np.array_equal(g3.bfs(0), orc.bfs_queue(o2, 0))
+
+
+@pytest.mark.parametrize("out_kind", ["host", "pinned", "device", "none"])
+def test_back_to_back_launches(gb, orc, out_kind):
+    """gbfs_bfs_many: one launch per source; host results go through two
+    alternating device buffers copied on a second stream."""
+    torch = pytest.importorskip("torch")
+    n = 1 << 15
+    src, dst = gb.gen_rmat(15, 16, seed=61)
+    o = orc.csr_build(n, src, dst, orc.UNDIRECTED)
+    g = gb.Graph.from_edges(n, src, dst)
+    deg = np.diff(o.row_offset)
+    sources = [int(x) for x in np.random.default_rng(62).choice(np.flatnonzero(deg > 0), 7, replace=False)]
+    sources[3] = int(np.flatnonzero(deg == 0)[0]) if (deg == 0).any() else sources[3]
+    if out_kind == "host":
+        out = np.full((7, n), 99, np.int32)
+    elif out_kind == "pinned":
+        out = torch.full((7, n), 99, dtype=torch.int32).pin_memory().numpy()
+    elif out_kind == "device":
+        out = torch.full((7, n), 99, dtype=torch.int32, device="cuda")
+    else:
+        out = None
+    for _ in range(2):  # the second call reuses the buffers and the copy stream
+        got, sts = g.bfs_many(sources, out=out, keep=out is not None)
+        assert len(sts) == 7 and all(s.ms > 0 for s in sts)
+        for i, s in enumerate(sources):
+            want = orc.bfs_queue(o, s)
+            assert sts[i].vertices_reached == int((want >= 0).sum())
+            if out is not None:
+                row = got[i].cpu().numpy() if out_kind == "device" else got[i]
+                assert np.array_equal(row, want), (out_kind, i)
