@@ -19,6 +19,12 @@ summed over the sources (Graph500 convention).
   cpu_baseline the oracle's restatement of the reference's CPU BFS (queue BFS
               of the migration path) on the host cores, one source per thread
 
+Extra objects on the same line (rank 0, skipped with --no-extra): grid
+(7000 x 7000, persistent vs one launch per level), batched (64-lane
+multi-source on RMAT-20; 512 small graphs in one launch), primitives (CSR
+build, exclusive scan) and serving (32 resident graphs, Poisson arrivals;
+--no-serving skips it).
+
 --impl reference times that CPU path alone (the reference's own code cannot
 be compiled on the GPU host: its sources are not shipped there).
 Multi-GPU (--gpus N under torchrun): independent replicas, no collective on
@@ -62,7 +68,7 @@ def parse_args():
     ap.add_argument("--layout", choices=["hub-first", "sorted"], default="hub-first",
                     help="CSR row order: sorted ids, or highest-degree neighbour first")
     ap.add_argument("--no-extra", action="store_true", help="skip the grid and batched measurements")
-    ap.add_argument("--serving", action="store_true", help="also run the serving sweep (32 resident graphs)")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep (32 resident graphs)")
     ap.add_argument("--grid-side", type=int, default=7000)
     return ap.parse_args()
 
@@ -587,7 +593,7 @@ def main():
         log("batched done")
         extra["primitives"] = measure_primitives(torch)
         log("primitives done")
-    if rank == 0 and args.serving:
+    if rank == 0 and not args.no_serving and not args.no_extra:
         extra["serving"] = measure_serving(torch)
 
     cpu = None
