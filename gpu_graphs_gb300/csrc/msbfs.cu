@@ -507,7 +507,54 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
     // arrived), 32 consecutive vertices per warp so every store is a whole
     // line of one row; per-lane totals for GTEPS
     unsigned long long r = 0, ec = 0;
-    for (long long base = gwarp * 32; base < n; base += nwarps * 32) {
+    const bool vec = ((n & 3) == 0) && (((uintptr_t)a.out & 15) == 0) && (((uintptr_t)a.lv8 & 3) == 0);
+    if (vec) {
+        // four consecutive vertices per thread: uchar4 byte loads, int4 stores
+        // (a lane whose level went straight to out, LV8_DEEP, keeps it)
+        const int nq4 = n >> 2;
+        for (long long q4 = gtid; q4 < nq4; q4 += gthreads) {
+            const long long u0 = q4 << 2;
+            unsigned long long vu[4];
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                vu[t] = __ldcg(a.vis + u0 + t) & all;
+                const int c = __popcll(vu[t]);
+                if (c) {
+                    r += c;
+                    ec += (unsigned long long)c * (unsigned long long)(__ldg(a.row + u0 + t + 1) - __ldg(a.row + u0 + t));
+                }
+            }
+            for (int j0 = 0; j0 < a.k; j0 += 4) {
+                uchar4 b[4];
+#pragma unroll
+                for (int t = 0; t < 4; t++)
+                    if (j0 + t < a.k) b[t] = __ldcg(reinterpret_cast<const uchar4 *>(a.lv8 + (size_t)(j0 + t) * n + u0));
+#pragma unroll
+                for (int t = 0; t < 4; t++) {
+                    const int j = j0 + t;
+                    if (j >= a.k) break;
+                    const int bv[4] = {b[t].x, b[t].y, b[t].z, b[t].w};
+                    int o[4];
+                    bool deep = false;
+#pragma unroll
+                    for (int x = 0; x < 4; x++) {
+                        const bool hit = (vu[x] >> j) & 1ull;
+                        o[x] = hit ? bv[x] : -1;
+                        deep |= hit && bv[x] == LV8_DEEP;
+                    }
+                    int *dst = a.out + (size_t)j * n + u0;
+                    if (!deep) {
+                        *reinterpret_cast<int4 *>(dst) = make_int4(o[0], o[1], o[2], o[3]);
+                    } else {
+#pragma unroll
+                        for (int x = 0; x < 4; x++)
+                            if (o[x] != LV8_DEEP) dst[x] = o[x];
+                    }
+                }
+            }
+        }
+    }
+    for (long long base = gwarp * 32; !vec && base < n; base += nwarps * 32) {
         const long long u = base + lane;
         if (u >= n) continue;  // no warp-wide operations below
         const unsigned long long vu = __ldcg(a.vis + u) & all;
