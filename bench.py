@@ -442,54 +442,67 @@ def measure_serving(torch, seconds: float = 2.0, fractions=(0.25, 0.5, 0.75, 1.0
            "plain_topdown_queries_per_s": round(len(draws) / (plain_td_ms / 1e3), 1)}
     log("serving: plain baseline done")
     sweep = []
-    with gb.Server(mem_budget_bytes=150 << 30, num_slots=4, max_lanes=64, batch_window_us=500,
-                   window_pct=50) as srv:
-        gids = [srv.add_graph(g) for g in graphs]
-        # pinned result buffers (8 per graph, reused round robin: contents are
-        # not checked here, the serving tests do that)
-        pinned = [[torch.empty(g.n, dtype=torch.int32, pin_memory=True) for _ in range(8)] for g in graphs]
-        pools = [[t.numpy() for t in ts] for ts in pinned]
-        counters = [0] * 32
+    # pinned result buffers (8 per graph, reused round robin: contents are not
+    # checked here, the serving tests do that)
+    pinned = [[torch.empty(g.n, dtype=torch.int32, pin_memory=True) for _ in range(8)] for g in graphs]
+    pools = [[t.numpy() for t in ts] for ts in pinned]
+    counters = [0] * 32
+    cfg = dict(mem_budget_bytes=150 << 30, num_slots=4, max_lanes=64, batch_window_us=500, window_pct=50)
 
+    def submitter(srv, gids):
         def submit():
             gi, s0 = draw()
             buf = pools[gi][counters[gi] % 8]
             counters[gi] += 1
             return srv.submit(gids[gi], s0, buf)
+        return submit
 
-        # closed loop: everything queued at once -> capacity
+    # closed loop: everything queued at once -> capacity
+    with gb.Server(**cfg) as srv:
+        submit = submitter(srv, [srv.add_graph(g) for g in graphs])
         t0 = time.perf_counter()
         ts = [submit() for _ in range(1024)]
         for t in ts:
             srv.wait(t)
         capacity = 1024 / (time.perf_counter() - t0)
         out["capacity_queries_per_s"] = round(capacity, 1)
-        log(f"serving: capacity {capacity:.0f} q/s")
-        for frac in fractions:
-            rate = frac * capacity
+        out["peak_hbm_bytes"] = srv.stats()["peak_bytes"]
+    log(f"serving: capacity {capacity:.0f} q/s")
+    # open loop, Poisson arrivals: 10x the plain rate, then fractions of the
+    # capacity; a fresh server per point (its launch-time estimates start from
+    # a short warm-up at that rate, not from the closed loop's full batches)
+    plain_qps = out["plain_one_query_per_launch"]["queries_per_s"]
+    rates = sorted([10 * plain_qps] + [f * capacity for f in fractions])
+    for rate in rates:
+        with gb.Server(**cfg) as srv:
+            submit = submitter(srv, [srv.add_graph(g) for g in graphs])
+
+            def run(duration):
+                tickets = []
+                t0 = time.perf_counter()
+                next_t = t0
+                while len(tickets) < max_queries:
+                    now = time.perf_counter()
+                    if now - t0 >= duration:
+                        break
+                    if now < next_t:
+                        time.sleep(min(next_t - now, 0.0005))
+                        continue
+                    tickets.append(submit())
+                    next_t += rng.exponential(1.0 / rate)
+                for t in tickets:
+                    srv.wait(t)
+                return len(tickets), time.perf_counter() - t0
+
+            run(0.5)  # warm-up at this rate
             srv.reset_stats()
-            tickets = []
-            t0 = time.perf_counter()
-            next_t = t0
-            while len(tickets) < max_queries:
-                now = time.perf_counter()
-                if now - t0 >= seconds:
-                    break
-                if now < next_t:
-                    time.sleep(min(next_t - now, 0.0005))
-                    continue
-                tickets.append(submit())
-                next_t += rng.exponential(1.0 / rate)
-            for t in tickets:
-                srv.wait(t)
-            wall = time.perf_counter() - t0
+            nsub, wall = run(seconds)
             st = srv.stats()
-            sweep.append({"offered_queries_per_s": round(rate, 1), "submitted": len(tickets),
-                          "achieved_queries_per_s": round(len(tickets) / wall, 1),
+            sweep.append({"offered_queries_per_s": round(rate, 1), "offered_vs_plain": round(rate / plain_qps, 2),
+                          "submitted": nsub, "achieved_queries_per_s": round(nsub / wall, 1),
                           "p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
                           "mean_batch_lanes": round(st["mean_batch_lanes"], 2)})
             log(f"serving: {sweep[-1]}")
-        out["peak_hbm_bytes"] = srv.stats()["peak_bytes"]
     out["sweep"] = sweep
     out["capacity_vs_plain"] = round(capacity / out["plain_one_query_per_launch"]["queries_per_s"], 2)
     out["capacity_vs_plain_topdown"] = round(capacity / out["plain_topdown_queries_per_s"], 2)
@@ -586,18 +599,20 @@ def main():
         del host, hv
 
     extra = {}
-    if rank == 0 and not args.no_extra:
+    # the other configurations and the CPU baseline: single-GPU runs only
+    # (a scaling run holds all N GPUs; its line needs the headline alone)
+    if rank == 0 and world == 1 and not args.no_extra:
         extra["grid"] = measure_grid(args.grid_side, torch)
         log("grid done")
         extra["batched"] = measure_batched(torch)
         log("batched done")
         extra["primitives"] = measure_primitives(torch)
         log("primitives done")
-    if rank == 0 and not args.no_serving and not args.no_extra:
+    if rank == 0 and world == 1 and not args.no_serving and not args.no_extra:
         extra["serving"] = measure_serving(torch)
 
     cpu = None
-    if not args.no_cpu and rank == 0:
+    if not args.no_cpu and rank == 0 and world == 1:
         threads = args.cpu_threads or (os.cpu_count() or 1)
         sel = sources[: min(threads, k)]
         wall, e, lv = cpu_bfs_sample(n, row, col, sel, len(sel))

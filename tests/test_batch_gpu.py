@@ -92,7 +92,7 @@ def test_batch_over_handles(gb, orc):
         assert np.array_equal(got, orc.bfs_queue(o, 0))
 
 
-@pytest.mark.parametrize("n", [1, 2047, 2048, 2049, 1000003, 20000000])
+@pytest.mark.parametrize("n", [1, 2047, 2048, 2049, 16383, 16384, 16385, 32769, 1000003, 20000000])
 def test_exclusive_scan(gb, orc, n):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(n)
