@@ -84,7 +84,12 @@ struct gbfs_server {
     bool resizing = false;
     bool stop = false;
     // stats
+    // latencies of completed queries since the last reset: the most recent
+    // LAT_WINDOW of them (a ring), and the total count
+    static constexpr size_t LAT_WINDOW = 1u << 17;
     std::vector<double> lat;
+    size_t lat_next = 0;
+    int64_t completed = 0;
     int64_t launches = 0, rejected = 0;
     double lanes_sum = 0;
     // slots
@@ -216,7 +221,12 @@ void gbfs_server::worker(int idx)
                 q->done = true;
                 q->latency_ms = ms_between(q->t_submit, now);
                 q->queue_ms = ms_between(q->t_submit, q->t_launch);
-                if (status == GBFS_OK) lat.push_back(q->latency_ms);
+                if (status == GBFS_OK) {
+                    if (lat.size() < LAT_WINDOW) lat.push_back(q->latency_ms);
+                    else lat[lat_next] = q->latency_ms;
+                    lat_next = (lat_next + 1) % LAT_WINDOW;
+                    ++completed;
+                }
             }
             auto it = graphs.find(gid);
             if (it != graphs.end()) {
@@ -423,7 +433,7 @@ extern "C" int gbfs_server_get_stats(gbfs_server *s, gbfs_server_stats *st)
     if (!s || !st) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
     std::lock_guard<std::mutex> lk(s->mu);
     *st = gbfs_server_stats{};
-    st->completed = (int64_t)s->lat.size();
+    st->completed = s->completed;
     st->launches = s->launches;
     st->rejected = s->rejected;
     st->resident_bytes = s->resident;
@@ -448,6 +458,8 @@ extern "C" void gbfs_server_reset_stats(gbfs_server *s)
     if (!s) return;
     std::lock_guard<std::mutex> lk(s->mu);
     s->lat.clear();
+    s->lat_next = 0;
+    s->completed = 0;
     s->launches = 0;
     s->lanes_sum = 0;
 }

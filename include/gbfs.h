@@ -363,7 +363,9 @@ typedef struct gbfs_query_info {
     int32_t status;             /* GBFS_OK or the launch's error            */
 } gbfs_query_info;
 
-typedef struct gbfs_server_stats {
+typedef struct gbfs_server_stats {      /* since the last reset; the latency
+                                           percentiles cover the most recent
+                                           131,072 completed queries          */
     int64_t completed;
     int64_t launches;
     int64_t rejected;           /* admissions refused by the budget         */
