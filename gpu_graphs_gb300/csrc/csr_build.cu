@@ -28,6 +28,8 @@ namespace gbfs {
 
 namespace {
 
+constexpr int W4_MAX = 128;       // rows up to this length: warp sort, 4 values per lane
+constexpr int W16_MAX = 512;      // rows up to this length: warp sort, 16 values per lane
 constexpr int MED_MAX = 4096;     // rows up to this length sort in shared memory
 constexpr int MED_THREADS = 512;
 constexpr int LARGE_THREADS = 1024;
@@ -146,26 +148,28 @@ __global__ void k_scatter(const int *__restrict__ src, const int *__restrict__ d
     }
 }
 
-// Rows longer than 32 go to the medium (<= MED_MAX) or large list.
-__global__ void k_bin(const int *__restrict__ row, int n, int *med, int *large, unsigned *cnt)
+// Rows longer than 32 go to one of four lists by length: up to W4_MAX and
+// up to W16_MAX (warp sorts in registers), up to MED_MAX (CTA sort in shared
+// memory), longer (radix sort).  cnt[0] medium, [1] large, [2] W4, [3] W16.
+__global__ void k_bin(const int *__restrict__ row, int n, int *med, int *large, int *w4, int *w16, unsigned *cnt)
 {
     __shared__ int s_warp[33];
-    __shared__ int s_base[2];
+    __shared__ int s_base[4];
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n;
          base += (int64_t)gridDim.x * blockDim.x) {
         int64_t r = base + threadIdx.x;
         int d = r < n ? row[r + 1] - row[r] : 0;
-        int is_med = d > 32 && d <= MED_MAX, is_large = d > MED_MAX;
-        int tm, tl;
-        int om = block_excl_scan(is_med, s_warp, &tm);
-        int ol = block_excl_scan(is_large, s_warp, &tl);
-        if (threadIdx.x == 0) {
-            s_base[0] = tm ? (int)atomicAdd(&cnt[0], (unsigned)tm) : 0;
-            s_base[1] = tl ? (int)atomicAdd(&cnt[1], (unsigned)tl) : 0;
-        }
+        const int cls = d <= 32 ? -1 : d <= W4_MAX ? 2 : d <= W16_MAX ? 3 : d <= MED_MAX ? 0 : 1;
+        int tot[4], off[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) off[c] = block_excl_scan(cls == c, s_warp, &tot[c]);
+        if (threadIdx.x == 0)
+            for (int c = 0; c < 4; c++) s_base[c] = tot[c] ? (int)atomicAdd(&cnt[c], (unsigned)tot[c]) : 0;
         __syncthreads();
-        if (is_med) med[s_base[0] + om] = (int)r;
-        if (is_large) large[s_base[1] + ol] = (int)r;
+        if (cls >= 0) {
+            int *dst = cls == 0 ? med : cls == 1 ? large : cls == 2 ? w4 : w16;
+            dst[s_base[cls] + off[cls]] = (int)r;
+        }
         __syncthreads();
     }
 }
@@ -213,7 +217,82 @@ __global__ void k_sort_small(const int *__restrict__ row, int n, int *tmp, int d
     }
 }
 
-// One CTA per row of length 33..MED_MAX: bitonic sort in shared memory.
+// Bitonic sort of 32*E values held E per lane (element i = lane i%32,
+// register i/32), ascending.  Compare-exchange distances below 32 go
+// through shuffles, larger ones between a lane's own registers; all loops
+// unroll, so the registers stay registers.
+template <int E>
+__device__ __forceinline__ void warp_bitonic_sort_regs(int (&v)[E])
+{
+    const int lane = (int)lane_id();
+#pragma unroll
+    for (int k = 2; k <= 32 * E; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            if (j >= 32) {
+#pragma unroll
+                for (int r = 0; r < E; r++) {
+                    const int r2 = r ^ (j >> 5);
+                    if (r2 > r) {
+                        const bool up = ((r * 32 + lane) & k) == 0;
+                        const int a = v[r], c = v[r2];
+                        if ((a > c) == up) {
+                            v[r] = c;
+                            v[r2] = a;
+                        }
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < E; r++) {
+                    const int y = __shfl_xor_sync(FULL, v[r], j);
+                    const bool up = ((r * 32 + lane) & k) == 0;
+                    const bool lower = (lane & j) == 0;
+                    v[r] = (lower == up) ? min(v[r], y) : max(v[r], y);
+                }
+            }
+        }
+    }
+}
+
+// One warp per listed row of length 33..32*E: sort in registers, pack the
+// distinct values (dedup) or all of them back in place, record the count.
+template <int E>
+__global__ void k_sort_warp(const int *__restrict__ row, const int *__restrict__ list, const unsigned *cnt,
+                            int *tmp, int dedup, int *ucnt)
+{
+    const int count = (int)*cnt;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int lane = (int)lane_id();
+    for (int64_t li = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; li < count; li += warps) {
+        const int r = list[li];
+        const int b = row[r], d = row[r + 1] - b;
+        int v[E];
+#pragma unroll
+        for (int k = 0; k < E; k++) {
+            const int i = k * 32 + lane;
+            v[k] = i < d ? tmp[b + i] : INT_MAX;
+        }
+        warp_bitonic_sort_regs<E>(v);
+        int base = 0;
+#pragma unroll
+        for (int k = 0; k < E; k++) {
+            const int i = k * 32 + lane;
+            int prev = __shfl_up_sync(FULL, v[k], 1);
+            if (k > 0) {
+                const int last = __shfl_sync(FULL, v[k - 1], 31);
+                if (lane == 0) prev = last;
+            }
+            const bool keep = i < d && (!dedup || i == 0 || v[k] != prev);
+            const unsigned mk = __ballot_sync(FULL, keep);
+            if (keep) tmp[b + base + __popc(mk & lanemask_lt())] = v[k];
+            base += __popc(mk);
+        }
+        if (lane == 0) ucnt[r] = base;
+    }
+}
+
+// One CTA per row of length W16_MAX+1..MED_MAX: bitonic sort in shared memory.
 __global__ void __launch_bounds__(MED_THREADS)
 k_sort_medium(const int *__restrict__ row, const int *__restrict__ list, const unsigned *cnt,
               int *tmp, int dedup, int *ucnt)
@@ -563,19 +642,25 @@ done:
 int sort_rows_inplace(const int *row, int *col, int32_t n, int64_t m, cudaStream_t st, std::string &err)
 {
     int rc = GBFS_OK;
-    int *ucnt = nullptr, *med = nullptr, *large = nullptr, *tmp2 = nullptr;
+    int *ucnt = nullptr, *med = nullptr, *large = nullptr, *tmp2 = nullptr, *w4 = nullptr, *w16 = nullptr;
     unsigned *lcnt = nullptr;
     int key_bits = 1;
     const int thr = 256;
     CK(cudaMalloc(&ucnt, sizeof(int) * ((size_t)n + 1)));
     CK(cudaMalloc(&med, sizeof(int) * (size_t)n));
     CK(cudaMalloc(&large, sizeof(int) * (size_t)n));
+    CK(cudaMalloc(&w4, sizeof(int) * (size_t)n));
+    CK(cudaMalloc(&w16, sizeof(int) * (size_t)n));
     CK(cudaMalloc(&lcnt, 16));
     CK(cudaMalloc(&tmp2, sizeof(int) * (size_t)std::max<int64_t>(m, 1)));
     CK(cudaMemsetAsync(lcnt, 0, 16, st));
-    k_bin<<<grid_for(n, BIN_THREADS, 152 * 4), BIN_THREADS, 0, st>>>(row, n, med, large, lcnt);
+    k_bin<<<grid_for(n, BIN_THREADS, 152 * 4), BIN_THREADS, 0, st>>>(row, n, med, large, w4, w16, lcnt);
     CK(cudaGetLastError());
     k_sort_small<<<grid_for((int64_t)n * 32, thr), thr, 0, st>>>(row, n, col, 0, ucnt);
+    CK(cudaGetLastError());
+    k_sort_warp<4><<<152 * 8, 256, 0, st>>>(row, w4, lcnt + 2, col, 0, ucnt);
+    CK(cudaGetLastError());
+    k_sort_warp<16><<<152 * 8, 256, 0, st>>>(row, w16, lcnt + 3, col, 0, ucnt);
     CK(cudaGetLastError());
     k_sort_medium<<<152 * 4, MED_THREADS, 0, st>>>(row, med, lcnt, col, 0, ucnt);
     CK(cudaGetLastError());
@@ -587,6 +672,8 @@ done:
     if (ucnt) cudaFree(ucnt);
     if (med) cudaFree(med);
     if (large) cudaFree(large);
+    if (w4) cudaFree(w4);
+    if (w16) cudaFree(w16);
     if (lcnt) cudaFree(lcnt);
     if (tmp2) cudaFree(tmp2);
     return rc;
@@ -655,7 +742,7 @@ int csr_build_from_edges(int32_t n, int64_t m, const int *d_src, const int *d_ds
     int rc = GBFS_OK;
     const bool sym = flags & GBFS_SYMMETRIZE, dedup = flags & GBFS_DEDUP;
     int *deg = nullptr, *cursor = nullptr, *tmp = nullptr, *tmp2 = nullptr, *ucnt = nullptr;
-    int *med = nullptr, *large = nullptr, *row2 = nullptr;
+    int *med = nullptr, *large = nullptr, *row2 = nullptr, *w4 = nullptr, *w16 = nullptr;
     unsigned *lcnt = nullptr;
     int *status = nullptr;
     unsigned long long *total = nullptr;
@@ -718,9 +805,15 @@ int csr_build_from_edges(int32_t n, int64_t m, const int *d_src, const int *d_ds
     CK(cudaMalloc(&ucnt, sizeof(int) * ((size_t)n + 1)));
     CK(cudaMalloc(&med, sizeof(int) * (size_t)n));
     CK(cudaMalloc(&large, sizeof(int) * (size_t)n));
-    k_bin<<<grid_for(n, BIN_THREADS, 152 * 4), BIN_THREADS, 0, st>>>(out.row, n, med, large, lcnt);
+    CK(cudaMalloc(&w4, sizeof(int) * (size_t)n));
+    CK(cudaMalloc(&w16, sizeof(int) * (size_t)n));
+    k_bin<<<grid_for(n, BIN_THREADS, 152 * 4), BIN_THREADS, 0, st>>>(out.row, n, med, large, w4, w16, lcnt);
     CK(cudaGetLastError());
     k_sort_small<<<grid_for((int64_t)n * 32, thr), thr, 0, st>>>(out.row, n, tmp, dedup, ucnt);
+    CK(cudaGetLastError());
+    k_sort_warp<4><<<152 * 8, 256, 0, st>>>(out.row, w4, lcnt + 2, tmp, dedup, ucnt);
+    CK(cudaGetLastError());
+    k_sort_warp<16><<<152 * 8, 256, 0, st>>>(out.row, w16, lcnt + 3, tmp, dedup, ucnt);
     CK(cudaGetLastError());
     k_sort_medium<<<152 * 4, MED_THREADS, 0, st>>>(out.row, med, lcnt, tmp, dedup, ucnt);
     CK(cudaGetLastError());
@@ -769,6 +862,8 @@ done:
     if (ucnt) cudaFree(ucnt);
     if (med) cudaFree(med);
     if (large) cudaFree(large);
+    if (w4) cudaFree(w4);
+    if (w16) cudaFree(w16);
     if (row2) cudaFree(row2);
     if (status) cudaFree(status);
     if (scan_mem) cudaFree(scan_mem);
