@@ -138,7 +138,7 @@ static int validate_params(const gbfs_params *p)
 extern "C" int gbfs_get_params(const gbfs_graph *g, gbfs_params *p)
 {
     if (!g || !p) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
-    *p = g->params;
+    *p = graph_params(g);
     return GBFS_OK;
 }
 
@@ -147,8 +147,7 @@ extern "C" int gbfs_set_params(gbfs_graph *g, const gbfs_params *p)
     if (!g) return fail(GBFS_ERR_INVALID_ARG, "graph is NULL");
     int rc = validate_params(p);
     if (rc) return rc;
-    std::lock_guard<std::mutex> lk(g->mu);
-    g->params = *p;
+    graph_set_params(g, *p);
     return GBFS_OK;
 }
 
@@ -311,7 +310,7 @@ static void fill_stats(gbfs_stats *s, const BfsResult &r, int64_t nsources)
 
 static gbfs_params effective_params(const gbfs_graph *g)
 {
-    gbfs_params p = g->params;
+    gbfs_params p = graph_params(g);
     if (!g->symmetric) p.direction = GBFS_DIR_TOPDOWN;
     return p;
 }
@@ -581,7 +580,7 @@ extern "C" int gbfs_bfs_multi(gbfs_graph *g, const int32_t *sources, int32_t k, 
     if (rc) return fail(rc, err);
     const bool dev_out = is_device_ptr(levels_out);
     const size_t n = (size_t)g->csr.n;
-    gbfs_params p = g->params;
+    gbfs_params p = graph_params(g);
     MsResult tot;
     g->last_multi = true;
     for (int32_t b0 = 0; b0 < k; b0 += MS_LANES) {

@@ -56,7 +56,7 @@ extern "C" int gbfs_autotune(gbfs_graph *g, const int32_t *sources, int32_t nsou
         auto it = g_cache.find(sig);
         if (it != g_cache.end()) {
             gbfs_params p = it->second;
-            p.timeout_ms = g->params.timeout_ms;
+            p.timeout_ms = graph_params(g).timeout_ms;
             gbfs_set_params(g, &p);
             if (best) *best = p;
             return GBFS_OK;
@@ -66,8 +66,8 @@ extern "C" int gbfs_autotune(gbfs_graph *g, const int32_t *sources, int32_t nsou
     const size_t n = (size_t)g->csr.n;
     gbfs_params base;
     gbfs_default_params(&base);
-    base.timeout_ms = g->params.timeout_ms;
-    const gbfs_params saved = g->params;
+    const gbfs_params saved = graph_params(g);
+    base.timeout_ms = saved.timeout_ms;
 
     int *ref = nullptr, *tmp = nullptr;
     unsigned *diff = nullptr;

@@ -585,22 +585,15 @@ size_t bfs_smem_bytes()
 template <int BLOCK, int MINB>
 cudaError_t bfs_launch(BfsArgs &args, int blocks_per_sm, cudaStream_t st, int max_ctas)
 {
-    static int sms = 0;
-    static bool attr_set = false;
+    static LaunchSetup setup;  // per template instance
     const size_t smem = bfs_smem_bytes<BLOCK>();
-    cudaError_t e;
-    if (!attr_set) {
-        e = cudaFuncSetAttribute(k_bfs<BLOCK, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
-    if (!sms) {
-        int dev = 0;
-        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    }
-    int occ = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bfs<BLOCK, MINB>, BLOCK, smem);
+    int sms = 0, occ = 0;
+    cudaError_t e = setup.get(sms, occ, [&](int dev, int &s_out, int &o_out) {
+        cudaError_t r = cudaFuncSetAttribute(k_bfs<BLOCK, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (r == cudaSuccess) r = cudaDeviceGetAttribute(&s_out, cudaDevAttrMultiProcessorCount, dev);
+        if (r == cudaSuccess) r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o_out, k_bfs<BLOCK, MINB>, BLOCK, smem);
+        return r;
+    });
     if (e != cudaSuccess) return e;
     if (occ < 1) return cudaErrorInvalidConfiguration;
     const int per = std::max(1, std::min(blocks_per_sm, occ));

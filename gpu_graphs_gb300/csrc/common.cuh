@@ -4,9 +4,41 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "../../include/gbfs.h"
 
 namespace gbfs {
+
+// Per-device facts a kernel's launcher computes on first use (its dynamic
+// shared-memory attribute, SM count, CTAs per SM), safe when several host
+// threads launch for the first time at once.
+struct LaunchSetup {
+    std::mutex mu;
+    bool done[64] = {};
+    cudaError_t err[64] = {};
+    int sms[64] = {};
+    int occ[64] = {};
+
+    // f(sms, occ) fills the facts for the current device once; returns its error.
+    template <typename F>
+    cudaError_t get(int &sms_out, int &occ_out, F f)
+    {
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return e;
+        if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+        std::lock_guard<std::mutex> lk(mu);
+        if (!done[dev]) {
+            err[dev] = f(dev, sms[dev], occ[dev]);
+            done[dev] = err[dev] == cudaSuccess;
+            if (!done[dev]) return err[dev];
+        }
+        sms_out = sms[dev];
+        occ_out = occ[dev];
+        return cudaSuccess;
+    }
+};
 
 constexpr unsigned FULL = 0xffffffffu;
 

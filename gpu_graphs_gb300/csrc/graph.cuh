@@ -17,7 +17,8 @@ struct gbfs_graphset;
 
 struct gbfs_graph {
     gbfs::DeviceCsr csr;
-    gbfs_params params{};
+    gbfs_params params{};        // read and written only under pmu (graph_params / set)
+    mutable std::mutex pmu;
     gbfs::BfsWork work;
     gbfs::MsWork ms;
     cudaStream_t stream = nullptr;
@@ -37,6 +38,19 @@ struct gbfs_graphset {
 };
 
 namespace gbfs {
+
+// A copy of the graph's traversal parameters (other threads may set them).
+inline gbfs_params graph_params(const gbfs_graph *g)
+{
+    std::lock_guard<std::mutex> lk(g->pmu);
+    return g->params;
+}
+
+inline void graph_set_params(gbfs_graph *g, const gbfs_params &p)
+{
+    std::lock_guard<std::mutex> lk(g->pmu);
+    g->params = p;
+}
 
 // thread-local error detail
 void set_error(const std::string &msg);

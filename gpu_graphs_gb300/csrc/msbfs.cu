@@ -735,24 +735,17 @@ cudaError_t msbfs_enqueue(const DeviceCsr &g, const gbfs_params &p, bool pull_al
     a.direction = p.direction;
     a.pull_div = 16;
     a.timeout_ns = (unsigned long long)std::max(1, p.timeout_ms) * 1000000ull;
-    static int sms = 0, occ = 0;
+    static LaunchSetup setup;
     const size_t smem = ms_smem_bytes();
-    cudaError_t e = cudaSuccess;
-    if (!sms) {
-        int dev = 0;
-        e = cudaFuncSetAttribute(k_msbfs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e == cudaSuccess) e = cudaGetDevice(&dev);
-        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_msbfs, MS_BLOCK, smem);
-        if (e != cudaSuccess) {
-            sms = 0;
-            return e;
-        }
-        if (occ < 1) {
-            sms = 0;
-            return cudaErrorInvalidConfiguration;
-        }
-    }
+    int sms = 0, occ = 0;
+    cudaError_t e = setup.get(sms, occ, [&](int dev, int &s_out, int &o_out) {
+        cudaError_t r = cudaFuncSetAttribute(k_msbfs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (r == cudaSuccess) r = cudaDeviceGetAttribute(&s_out, cudaDevAttrMultiProcessorCount, dev);
+        if (r == cudaSuccess) r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o_out, k_msbfs, MS_BLOCK, smem);
+        return r;
+    });
+    if (e != cudaSuccess) return e;
+    if (occ < 1) return cudaErrorInvalidConfiguration;
     const int per = std::max(1, std::min(occ, std::max(1, p.blocks_per_sm)));
     int grid = sms * per;
     if (max_ctas > 0) grid = std::max(1, std::min(grid, max_ctas));

@@ -152,15 +152,15 @@ cudaError_t launch_scan(const Tin *in, Tout *out, int64_t n, Tout *total_out, Sc
     if (ntiles > s.max_tiles || ntiles > 0x7fffffff) return cudaErrorInvalidValue;
     s.epoch = (s.epoch + 1) & 0x3fffffffu;
     if (s.epoch == 0) s.epoch = 1;
-    static bool attr_set = false;  // per template instance
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_scan_exclusive<Tin, Tout>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)scan_stage_bytes());
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    static LaunchSetup setup;  // per template instance
+    int unused_sms = 0, unused_occ = 0;
+    cudaError_t e = setup.get(unused_sms, unused_occ, [&](int, int &, int &) {
+        return cudaFuncSetAttribute(k_scan_exclusive<Tin, Tout>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)scan_stage_bytes());
+    });
+    if (e != cudaSuccess) return e;
     // the tile ticket starts at zero (flags carry the call number instead)
-    cudaError_t e = cudaMemsetAsync(s.ctl, 0, sizeof(unsigned), st);
+    e = cudaMemsetAsync(s.ctl, 0, sizeof(unsigned), st);
     if (e != cudaSuccess) return e;
     k_scan_exclusive<Tin, Tout><<<(unsigned)ntiles, SCAN_THREADS, scan_stage_bytes(), st>>>(
         in, out, n, total_out, s.flags, s.agg, s.inc, s.ctl, s.epoch, ntiles);

@@ -171,7 +171,7 @@ void gbfs_server::worker(int idx)
         const auto t_launch = Clock::now();
         const size_t n = (size_t)g->csr.n;
         int status = GBFS_OK;
-        gbfs_params p = g->params;
+        gbfs_params p = graph_params(g);
         p.timeout_ms = cfg.timeout_ms;
         if (!g->symmetric) p.direction = GBFS_DIR_TOPDOWN;
         cudaError_t e = cudaSuccess;

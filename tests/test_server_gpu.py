@@ -102,3 +102,33 @@ def test_bounded_wait_reports_timeout_and_context_survives(gb, orc):
     s, d = gb.gen_er(1000, 3000, 1)
     g = gb.Graph.from_edges(1000, s, d)
     assert np.array_equal(g.bfs(0), orc.bfs_queue(orc.csr_build(1000, s, d, orc.UNDIRECTED), 0))
+
+
+def test_server_with_concurrent_param_changes(gb, orc):
+    """Parameters changed from another thread while the server runs: results stay exact."""
+    graphs = _graphs(gb, orc)
+    stop = threading.Event()
+
+    def toggler():
+        i = 0
+        while not stop.is_set():
+            for g, _ in graphs:
+                g.set_params(alpha=8 if i % 2 else 14, direction=i % 3)
+            i += 1
+
+    th = threading.Thread(target=toggler)
+    th.start()
+    try:
+        with gb.Server(mem_budget_bytes=8 << 30, num_slots=3, max_lanes=64, batch_window_us=200) as srv:
+            gids = [srv.add_graph(g) for g, _ in graphs]
+            rng = np.random.default_rng(9)
+            plan = [(int(rng.integers(len(graphs))), 0) for _ in range(150)]
+            plan = [(gi, int(rng.integers(graphs[gi][0].n))) for gi, _ in plan]
+            tickets = [srv.submit(gids[gi], s) for gi, s in plan]
+            for t, (gi, s) in zip(tickets, plan):
+                got, info = srv.wait(t)
+                assert info.status == 0
+                assert np.array_equal(got, orc.bfs_queue(graphs[gi][1], s)), (gi, s)
+    finally:
+        stop.set()
+        th.join()
