@@ -260,7 +260,8 @@ def config_block(args, n: int, m: int) -> dict:
 # ---- the other configurations (extra objects on the same line) --------------------
 
 def measure_grid(side: int, torch) -> dict:
-    """High-diameter grid: one persistent launch vs one launch per level."""
+    """High-diameter grid: one persistent launch vs one launch per level (host
+    loop, the reference's shape) vs the same launches replayed by a CUDA graph."""
     import gpu_graphs_gb300 as gb
     src, dst = gb.gen_grid(side, 0.1, 0.001, 8, seed=1)
     n = side * side
@@ -279,9 +280,17 @@ def measure_grid(side: int, torch) -> dict:
     runs_l = [g.bfs(source, out=out, stats=True)[1] for _ in range(2)]
     same = bool(torch.equal(out, ref))
     t_l = float(np.mean([r.ms for r in runs_l]))
+    # the same launches per level, replayed by a CUDA graph (device-side loop)
+    g.set_params(per_level_launch=2)
+    g.bfs(source, out=out)
+    runs_g = [g.bfs(source, out=out, stats=True)[1] for _ in range(2)]
+    same = same and bool(torch.equal(out, ref))
+    t_g = float(np.mean([r.ms for r in runs_g]))
+    g.set_params(per_level_launch=0)
     return {"workload": f"grid {side}x{side}, 10% edges dropped, 0.1% extra edges within radius 8",
             "vertices": n, "directed_edges": int(g.m), "source": source, "levels": int(st.levels),
             "persistent_ms": round(t_p, 3), "per_level_launch_ms": round(t_l, 3),
+            "per_level_graph_ms": round(t_g, 3),
             "per_level_launches": int(runs_l[-1].launches), "speedup_vs_per_level": round(t_l / t_p, 2),
             "gteps_persistent": round(st.edges_in_component / 2 / (t_p / 1e3) / 1e9, 3),
             "us_per_level_persistent": round(1e3 * t_p / max(1, st.levels), 3),

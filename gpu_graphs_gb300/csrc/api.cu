@@ -129,8 +129,8 @@ static int validate_params(const gbfs_params *p)
     if (p->alpha < 1 || p->beta < 1) return fail(GBFS_ERR_INVALID_ARG, "alpha and beta must be >= 1");
     if (p->big_degree < 32) return fail(GBFS_ERR_INVALID_ARG, "big_degree must be >= 32");
     if (p->direction < 0 || p->direction > 2) return fail(GBFS_ERR_INVALID_ARG, "bad direction");
-    if (p->per_level_launch != 0 && p->per_level_launch != 1)
-        return fail(GBFS_ERR_INVALID_ARG, "per_level_launch must be 0 or 1");
+    if (p->per_level_launch < 0 || p->per_level_launch > 2)
+        return fail(GBFS_ERR_INVALID_ARG, "per_level_launch must be 0, 1 or 2");
     if (p->timeout_ms < 1) return fail(GBFS_ERR_INVALID_ARG, "timeout_ms must be >= 1");
     return GBFS_OK;
 }

@@ -694,6 +694,7 @@ void bfs_work_free(BfsWork &w)
     if (w.h_ctrl) cudaFreeHost(w.h_ctrl);
     if (w.ev0) cudaEventDestroy(w.ev0);
     if (w.ev1) cudaEventDestroy(w.ev1);
+    bfs_graph_free(w);
     if (w.level2) cudaFree(w.level2);
     if (w.copy_st) cudaStreamDestroy(w.copy_st);
     for (int i = 0; i < 2; i++) {
@@ -726,11 +727,12 @@ int bfs_work_reserve_overlap(BfsWork &w, std::string &err)
     return GBFS_OK;
 }
 
-cudaError_t bfs_enqueue(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_roots, int k,
-                        int single_root, int *d_level, BfsOut *slot, cudaStream_t st, bool symmetric, int resume,
-                        int max_steps, int max_ctas)
+namespace {
+
+BfsArgs make_args(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_roots, int k, int single_root,
+                  int *d_level, BfsOut *slot, bool symmetric, int resume, int max_steps)
 {
-    BfsArgs a;
+    BfsArgs a{};
     a.n = g.n;
     a.n_active = (int)std::max<int64_t>(1, g.nonisolated);
     a.m = g.m;
@@ -757,7 +759,160 @@ cudaError_t bfs_enqueue(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, co
     a.big_degree = std::max(32, p.big_degree);
     a.direction = p.direction;
     a.timeout_ns = (unsigned long long)std::max(1, p.timeout_ms) * 1000000ull;
+    return a;
+}
+
+// Kernel, block, grid and shared memory of a launch with these parameters.
+template <int BLOCK, int MINB>
+cudaError_t bfs_shape(int blocks_per_sm, int max_ctas, const void **func, int *block, int *grid, size_t *smem)
+{
+    static LaunchSetup setup;  // per template instance
+    const size_t sm = bfs_smem_bytes<BLOCK>();
+    int sms = 0, occ = 0;
+    cudaError_t e = setup.get(sms, occ, [&](int dev, int &s_out, int &o_out) {
+        cudaError_t r = cudaFuncSetAttribute(k_bfs<BLOCK, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        if (r == cudaSuccess) r = cudaDeviceGetAttribute(&s_out, cudaDevAttrMultiProcessorCount, dev);
+        if (r == cudaSuccess) r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o_out, k_bfs<BLOCK, MINB>, BLOCK, sm);
+        return r;
+    });
+    if (e != cudaSuccess) return e;
+    if (occ < 1) return cudaErrorInvalidConfiguration;
+    int gr = sms * std::max(1, std::min(blocks_per_sm, occ));
+    if (max_ctas > 0) gr = std::max(1, std::min(gr, max_ctas));
+    *func = (const void *)k_bfs<BLOCK, MINB>;
+    *block = BLOCK;
+    *grid = gr;
+    *smem = sm;
+    return cudaSuccess;
+}
+
+cudaError_t bfs_shape_any(int threads, int bps, int max_ctas, const void **func, int *block, int *grid, size_t *smem)
+{
+    switch (threads) {
+    case 256:
+        return bps <= 4 ? bfs_shape<256, 4>(bps, max_ctas, func, block, grid, smem)
+                        : bfs_shape<256, 8>(bps, max_ctas, func, block, grid, smem);
+    case 1024:
+        return bps <= 1 ? bfs_shape<1024, 1>(bps, max_ctas, func, block, grid, smem)
+                        : bfs_shape<1024, 2>(bps, max_ctas, func, block, grid, smem);
+    default:
+        if (bps <= 2) return bfs_shape<512, 2>(bps, max_ctas, func, block, grid, smem);
+        if (bps == 3) return bfs_shape<512, 3>(bps, max_ctas, func, block, grid, smem);
+        return bfs_shape<512, 4>(bps, max_ctas, func, block, grid, smem);
+    }
+}
+
+// The while-loop condition of a graph-captured search: run another level
+// launch while the last one parked its state without a device error.
+__global__ void k_set_loop(BfsCtrl *ctrl, cudaGraphConditionalHandle h)
+{
+    const int st = ld_relaxed_i32(&ctrl->status);
+    const unsigned go = st == DEV_OK && !ctrl->rs.done ? 1u : 0u;
+    cudaGraphSetConditional(h, go);
+}
+
+cudaError_t add_set_loop_node(cudaGraph_t g, const cudaGraphNode_t *dep, size_t ndep, BfsCtrl *ctrl,
+                              cudaGraphConditionalHandle h, cudaGraphNode_t *node)
+{
+    void *kargs[] = {&ctrl, &h};
+    cudaGraphNodeParams kp = {};
+    kp.type = cudaGraphNodeTypeKernel;
+    kp.kernel.func = (void *)k_set_loop;
+    kp.kernel.gridDim = dim3(1);
+    kp.kernel.blockDim = dim3(1);
+    kp.kernel.kernelParams = kargs;
+    return cudaGraphAddNode(node, g, dep, nullptr, ndep, &kp);
+}
+
+// One cooperative kernel node for args `a` in graph g (after `dep`, if any).
+cudaError_t add_bfs_node(cudaGraph_t g, const cudaGraphNode_t *dep, size_t ndep, BfsArgs &a, const void *func,
+                         int block, int grid, size_t smem, cudaGraphNode_t *node)
+{
+    void *kargs[] = {&a};
+    cudaGraphNodeParams kp = {};
+    kp.type = cudaGraphNodeTypeKernel;
+    kp.kernel.func = const_cast<void *>(func);
+    kp.kernel.gridDim = dim3(grid);
+    kp.kernel.blockDim = dim3(block);
+    kp.kernel.sharedMemBytes = (unsigned)smem;
+    kp.kernel.kernelParams = kargs;
+    cudaError_t e = cudaGraphAddNode(node, g, dep, nullptr, ndep, &kp);
+    if (e != cudaSuccess) return e;
+    cudaLaunchAttributeValue v = {};
+    v.cooperative = 1;
+    return cudaGraphKernelNodeSetAttribute(*node, cudaLaunchAttributeCooperative, &v);
+}
+
+}  // namespace
+
+cudaError_t bfs_enqueue(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_roots, int k,
+                        int single_root, int *d_level, BfsOut *slot, cudaStream_t st, bool symmetric, int resume,
+                        int max_steps, int max_ctas)
+{
+    BfsArgs a = make_args(g, p, w, d_roots, k, single_root, d_level, slot, symmetric, resume, max_steps);
     return bfs_launch_any(a, p.threads_per_block, p.blocks_per_sm, st, max_ctas);
+}
+
+void bfs_graph_free(BfsWork &w)
+{
+    if (w.gexec) cudaGraphExecDestroy(w.gexec);
+    if (w.graph) cudaGraphDestroy(w.graph);
+    w.gexec = nullptr;
+    w.graph = nullptr;
+}
+
+// Graph-captured per-level launches: an init launch (initialisation and
+// level 0), then a while-loop node whose body is one per-level launch and a
+// one-thread node that keeps the loop going while the launch parked its
+// state for another level (and stops it on a device error).  The roots are
+// read from w.roots, so one instantiated graph serves every query with the
+// same shape; it is rebuilt when the arguments change.
+cudaError_t bfs_graph_launch(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, int k, int *d_level,
+                             cudaStream_t st, bool symmetric)
+{
+    BfsArgs a0 = make_args(g, p, w, w.roots, k, -1, d_level, &w.ctrl->out, symmetric, 0, 1);
+    const void *func = nullptr;
+    int block = 0, grid = 0;
+    size_t smem = 0;
+    cudaError_t e = bfs_shape_any(p.threads_per_block, p.blocks_per_sm, 0, &func, &block, &grid, &smem);
+    if (e != cudaSuccess) return e;
+    static_assert(sizeof(BfsArgs) <= sizeof(w.graph_key), "graph key holds the launch arguments");
+    unsigned char key[sizeof(w.graph_key)] = {};
+    memcpy(key, &a0, sizeof(BfsArgs));
+    const int shape[3] = {block, grid, (int)smem};
+    if (!w.gexec || memcmp(key, w.graph_key, sizeof(key)) != 0 || memcmp(shape, w.graph_shape, sizeof(shape)) != 0) {
+        bfs_graph_free(w);
+        cudaGraph_t gr = nullptr;
+        e = cudaGraphCreate(&gr, 0);
+        cudaGraphConditionalHandle h = 0;
+        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, gr, 0u, cudaGraphCondAssignDefault);
+        BfsArgs ai = a0, al = a0;
+        al.resume = 1;
+        // init launch -> condition -> while (condition) { level launch -> condition }
+        cudaGraphNode_t n0 = nullptr, n1 = nullptr, nc = nullptr, nb = nullptr, nb2 = nullptr;
+        if (e == cudaSuccess) e = add_bfs_node(gr, nullptr, 0, ai, func, block, grid, smem, &n0);
+        if (e == cudaSuccess) e = add_set_loop_node(gr, &n0, 1, w.ctrl, h, &n1);
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        if (e == cudaSuccess) e = cudaGraphAddNode(&nc, gr, &n1, nullptr, 1, &cp);
+        cudaGraph_t body = e == cudaSuccess ? cp.conditional.phGraph_out[0] : nullptr;
+        if (e == cudaSuccess) e = add_bfs_node(body, nullptr, 0, al, func, block, grid, smem, &nb);
+        if (e == cudaSuccess) e = add_set_loop_node(body, &nb, 1, w.ctrl, h, &nb2);
+        cudaGraphExec_t ex = nullptr;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&ex, gr, 0);
+        if (e != cudaSuccess) {
+            if (gr) cudaGraphDestroy(gr);
+            return e;
+        }
+        w.graph = gr;
+        w.gexec = ex;
+        memcpy(w.graph_key, key, sizeof(key));
+        memcpy(w.graph_shape, shape, sizeof(shape));
+    }
+    return cudaGraphLaunch(w.gexec, st);
 }
 
 int bfs_work_reserve_many(BfsWork &w, int k, std::string &err)
@@ -792,9 +947,19 @@ int bfs_work_reserve_many(BfsWork &w, int k, std::string &err)
 int bfs_run(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_roots, int k,
             int single_root, int *d_level, cudaStream_t st, BfsResult &res, std::string &err, bool symmetric)
 {
-    cudaError_t e = cudaEventRecord(w.ev0, st);
+    cudaError_t e = cudaSuccess;
+    if (p.per_level_launch == 2) {
+        // the graph reads its roots from w.roots
+        if (d_roots) e = cudaMemcpyAsync(w.roots, d_roots, sizeof(int) * (size_t)k, cudaMemcpyDeviceToDevice, st);
+        else e = cudaMemcpyAsync(w.roots, &single_root, sizeof(int), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // single_root lives on this stack frame
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(w.ev0, st);
     int launches = 1;
-    if (!p.per_level_launch) {
+    if (p.per_level_launch == 2) {
+        if (e == cudaSuccess) e = bfs_graph_launch(g, p, w, d_roots ? k : 1, d_level, st, symmetric);
+        launches = -1;  // the graph's own launches: levels + 1, filled in below
+    } else if (!p.per_level_launch) {
         if (e == cudaSuccess) e = bfs_enqueue(g, p, w, d_roots, k, single_root, d_level, &w.ctrl->out, st, symmetric);
     } else {
         // The reference's shape: one launch per level, then a device->host
@@ -832,7 +997,7 @@ int bfs_run(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_r
     res.levels = h.out.levels;
     res.td_levels = h.out.td_levels;
     res.bu_levels = h.out.bu_levels;
-    res.launches = launches;
+    res.launches = launches >= 0 ? launches : h.out.levels + 1;
     res.roots = h.out.roots;
     res.reached = (int64_t)h.out.reached;
     res.edges_c = (int64_t)h.out.edges_c;

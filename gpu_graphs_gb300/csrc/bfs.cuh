@@ -82,8 +82,16 @@ struct BfsWork {
     int *level2 = nullptr;
     cudaStream_t copy_st = nullptr;
     cudaEvent_t ev_ready[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
+    // graph-captured per-level launches (per_level_launch == 2): the
+    // instantiated graph and the launch arguments / shape it was built for
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    unsigned char graph_key[256] = {};
+    int graph_shape[3] = {0, 0, 0};
     int64_t bytes = 0;
 };
+
+void bfs_graph_free(BfsWork &w);
 
 // Allocate the second level buffer, the copy stream and its events.
 int bfs_work_reserve_overlap(BfsWork &w, std::string &err);

@@ -117,8 +117,12 @@ typedef struct gbfs_params {
     int32_t beta;               /* BU->TD when frontier vertices < n/beta    */
     int32_t big_degree;         /* TD rows >= this are split across the grid */
     int32_t direction;          /* GBFS_DIR_*                               */
-    int32_t per_level_launch;   /* 1: one launch per level with a host loop
-                                   (the reference's shape), 0: persistent   */
+    int32_t per_level_launch;   /* 0: one persistent launch per search;
+                                   1: one launch per level with a host loop
+                                   (the reference's shape); 2: one launch per
+                                   level replayed by a CUDA graph with a
+                                   device-side while loop (no host round
+                                   trip between levels)                     */
     int32_t timeout_ms;         /* bound on every device-side wait          */
 } gbfs_params;
 

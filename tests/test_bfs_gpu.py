@@ -42,6 +42,10 @@ def test_reference_fixtures(gb, orc, name):
         g2 = gb.Graph.from_csr(d["ref_row"], d["ref_col"])
         for s, want in zip(d["sources"], d["levels"]):
             assert np.array_equal(g2.bfs(int(s)), want)
+    for mode in (1, 2):  # a launch per level: host loop, then a CUDA graph
+        g.set_params(per_level_launch=mode)
+        for s, want in zip(d["sources"], d["levels"]):
+            assert np.array_equal(g.bfs(int(s)), want), (name, int(s), mode)
 
 
 @pytest.mark.parametrize("name", golden_names("syn_"))
@@ -81,7 +85,8 @@ def _check_against_oracle(gb, orc, n, src, dst, sources, flags=None, params=None
 @pytest.mark.parametrize("params", [
     {}, {"threads_per_block": 256, "blocks_per_sm": 4}, {"threads_per_block": 1024, "blocks_per_sm": 1},
     {"alpha": 2, "beta": 4}, {"alpha": 96, "beta": 96}, {"big_degree": 32}, {"big_degree": 4096},
-    {"direction": 1}, {"direction": 2}, {"per_level_launch": 1},
+    {"direction": 1}, {"direction": 2}, {"per_level_launch": 1}, {"per_level_launch": 2},
+    {"per_level_launch": 2, "direction": 2},
 ])
 def test_rmat18_param_grid(gb, orc, params):
     src, dst = gb.gen_rmat(18, 16, seed=2)
@@ -102,6 +107,15 @@ def test_grid_high_diameter(gb, orc):
     got, st2 = g.bfs(0, stats=True)
     assert np.array_equal(got, want)
     assert st2.launches == st.levels + 1 and st2.levels == st.levels
+    g.set_params(per_level_launch=2)  # the same launches replayed by a CUDA graph
+    for s0 in (0, side * side // 2 + 7, 0):  # the second query of the same shape reuses the graph
+        got3, st3 = g.bfs(s0, stats=True)
+        assert np.array_equal(got3, orc.bfs_queue(o, s0))
+        assert st3.launches == st3.levels + 1
+    # multi-root through the graph (roots from device memory)
+    mr = g.bfs_multiroot([0, side * side - 1])
+    g.set_params(per_level_launch=0)
+    assert np.array_equal(mr, g.bfs_multiroot([0, side * side - 1]))
 
 
 def test_er_and_directed(gb, orc):
