@@ -55,7 +55,7 @@ SOURCE_SEED = 1
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gbfs", "reference"], default="gbfs")
     ap.add_argument("--scale", type=int, default=22)
@@ -121,7 +121,11 @@ def pick_sources(deg: np.ndarray, k: int) -> np.ndarray:
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms in the background."""
+    """nvidia-smi clocks / throttle reasons sampled every 100 ms in the background.
+
+    Started before the warm-up (nvidia-smi takes a moment to start); each
+    sample is stamped on arrival and summary() keeps those inside the window
+    set by mark_start() / mark_end() around the timed steps."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -130,13 +134,21 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.lines: list[str] = []
+        self.lines: list[tuple[float, str]] = []
+        self.t0 = None
+        self.t1 = None
+
+    def mark_start(self):
+        self.t0 = time.perf_counter()
+
+    def mark_end(self):
+        self.t1 = time.perf_counter()
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
         except (OSError, FileNotFoundError):
@@ -145,7 +157,7 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
 
     def __exit__(self, *exc):
         if self.proc:
@@ -158,7 +170,12 @@ class ClockSampler:
 
     def summary(self) -> dict:
         sm, mx, reasons = [], [], set()
-        for ln in self.lines:
+        # a sample printed within 100 ms after the window still describes it
+        lo = self.t0 if self.t0 is not None else float("-inf")
+        hi = self.t1 + 0.1 if self.t1 is not None else float("inf")
+        for t, ln in self.lines:
+            if not lo <= t <= hi:
+                continue
             p = [x.strip() for x in ln.split(",")]
             if len(p) < 9:
                 continue
@@ -550,12 +567,13 @@ def main():
     g.bfs_many(sources[:2], out=out[:2])
     parity = all(np.array_equal(out[i].cpu().numpy(), oracle.bfs_queue(og, int(s))) for i, s in enumerate(sources[:2]))
 
-    for _ in range(args.warmup):
-        g.bfs_many(sources, out=out)
-    torch.cuda.synchronize()
-    dist.barrier()
     launch_ms, launch_ec, edges_c, verts, lvls = [], [], 0, 0, []
     with ClockSampler(local) as clk:
+        for _ in range(args.warmup):
+            g.bfs_many(sources, out=out)
+        torch.cuda.synchronize()
+        dist.barrier()
+        clk.mark_start()
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
         ev0.record(stream)
@@ -568,6 +586,7 @@ def main():
             lvls += [(s.levels, s.td_levels, s.bu_levels) for s in sts]
         ev1.record(stream)
         torch.cuda.synchronize()
+        clk.mark_end()
     dist.barrier()
     ms = ev0.elapsed_time(ev1)
     ms_max = dist.reduce(ms, "max")
