@@ -7,6 +7,13 @@ namespace gbfs {
 namespace {
 
 constexpr unsigned ST_AGG = 1, ST_INC = 2;
+constexpr int LB_WARPS = 4;  // warps of the look-back: 32 * LB_WARPS predecessors per step
+
+// Barrier 1 over the look-back warps only (threads 0 .. 32 * LB_WARPS - 1).
+__device__ __forceinline__ void lb_sync()
+{
+    asm volatile("bar.sync 1, %0;" ::"n"(32 * LB_WARPS) : "memory");
+}
 constexpr unsigned long long LOOKBACK_TIMEOUT_NS = 2000000000ULL;  // 2 s
 
 // Shared-memory index of tile element i with one pad word per 32 words, so
@@ -28,8 +35,11 @@ k_scan_exclusive(const Tin *__restrict__ in, Tout *__restrict__ out, int64_t n,
     // written coalesced (striped), used blocked by the scan
     extern __shared__ __align__(16) int s_stage[];
     __shared__ long long s_warp[SCAN_THREADS / 32];
-    __shared__ long long s_prefix;
+    __shared__ long long s_prefix, s_tile_sum;
     __shared__ unsigned s_tile;
+    __shared__ unsigned s_okm[LB_WARPS], s_incm[LB_WARPS];
+    __shared__ long long s_part[LB_WARPS];
+    __shared__ bool s_abort;
 
     if (threadIdx.x == 0) s_tile = atomicAdd(&ctl[0], 1u);
     __syncthreads();
@@ -61,62 +71,94 @@ k_scan_exclusive(const Tin *__restrict__ in, Tout *__restrict__ out, int64_t n,
         const long long wi = warp_incl_scan(w);
         if (lane < SCAN_THREADS / 32) s_warp[lane] = wi - w;  // exclusive warp offsets
         const long long tile_sum = __shfl_sync(FULL, wi, SCAN_THREADS / 32 - 1);
-        const unsigned tag = epoch << 2;
-        long long prefix = 0;
-        if (tile == 0) {
-            if (lane == 0) {
+        if (lane == 0) {
+            s_tile_sum = tile_sum;
+            if (tile == 0) {
                 inc[0] = tile_sum;
                 __threadfence();
-                st_release_gpu(&flags[0], tag | ST_INC);
-            }
-        } else {
-            if (lane == 0) {
+                st_release_gpu(&flags[0], (epoch << 2) | ST_INC);
+                s_prefix = 0;
+                if (ntiles == 1 && total_out) *total_out = (Tout)tile_sum;
+            } else {
                 agg[tile] = tile_sum;
                 __threadfence();
-                st_release_gpu(&flags[tile], tag | ST_AGG);
-            }
-            // Warp-wide look-back: lane l reads predecessor p - l.  The window
-            // is usable once every lane up to the nearest inclusive prefix
-            // has published; then the aggregates before it and that prefix
-            // are summed, else all 32 aggregates are and the window moves on.
-            int64_t p = tile - 1;
-            const unsigned long long t0 = globaltimer_ns();
-            unsigned spins = 0;
-            for (;;) {
-                const int64_t idx = p - (int64_t)lane;
-                unsigned f = tag | ST_INC;  // before tile 0: an inclusive prefix of 0
-                if (idx >= 0) f = ld_relaxed_u32(&flags[idx]);
-                const bool ok = (f >> 2) == (epoch & 0x3fffffffu) && (f & 3u) != 0;
-                const unsigned okm = __ballot_sync(FULL, ok);
-                const unsigned incm = __ballot_sync(FULL, ok && (f & 3u) == ST_INC);
-                const int first_inc = incm ? __ffs(incm) - 1 : 32;
-                const unsigned need = first_inc < 31 ? ((2u << first_inc) - 1u) : FULL;
-                if ((okm & need) == need) {
-                    __threadfence();  // acquire: the values published with those flags
-                    long long val = 0;
-                    if ((int)lane <= first_inc && idx >= 0)
-                        val = (int)lane == first_inc ? (long long)ld_relaxed_u64((const unsigned long long *)&inc[idx])
-                                                     : (long long)ld_relaxed_u64((const unsigned long long *)&agg[idx]);
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(FULL, val, o);
-                    prefix += val;
-                    if (first_inc < 32) break;
-                    p -= 32;
-                    continue;
-                }
-                if ((++spins & 31u) == 0 && globaltimer_ns() - t0 > LOOKBACK_TIMEOUT_NS) {
-                    if (lane == 0) atomicExch(&ctl[2], (unsigned)DEV_TIMEOUT);
-                    prefix = 0;
-                    break;
-                }
-            }
-            if (lane == 0) {
-                inc[tile] = prefix + tile_sum;
-                __threadfence();
-                st_release_gpu(&flags[tile], tag | ST_INC);
+                st_release_gpu(&flags[tile], (epoch << 2) | ST_AGG);
             }
         }
-        if (lane == 0) {
+    }
+    __syncthreads();
+    if (tile > 0 && warp < LB_WARPS) {
+        // Look-back by LB_WARPS warps: thread t of them reads predecessor
+        // p - t.  The window is usable once every predecessor up to the
+        // nearest inclusive prefix has published; then the aggregates before
+        // it and that prefix are summed, else all of the window's aggregates
+        // are and it moves on.  Decisions come from shared memory, so the
+        // warps take them together (named barrier 1 over LB_WARPS warps).
+        const unsigned tag = epoch << 2;
+        const int t = (int)threadIdx.x;  // 0 .. 32 * LB_WARPS - 1
+        long long prefix = 0;
+        int64_t p = tile - 1;
+        const unsigned long long t0 = globaltimer_ns();
+        unsigned spins = 0;
+        for (;;) {
+            const int64_t idx = p - (int64_t)t;
+            unsigned f = tag | ST_INC;  // before tile 0: an inclusive prefix of 0
+            if (idx >= 0) f = ld_relaxed_u32(&flags[idx]);
+            const bool ok = (f >> 2) == (epoch & 0x3fffffffu) && (f & 3u) != 0;
+            const unsigned okm = __ballot_sync(FULL, ok);
+            const unsigned incm = __ballot_sync(FULL, ok && (f & 3u) == ST_INC);
+            if (lane == 0) {
+                s_okm[warp] = okm;
+                s_incm[warp] = incm;
+            }
+            lb_sync();
+            int fi = 32 * LB_WARPS;  // window position of the nearest inclusive prefix
+            bool valid = true;
+#pragma unroll
+            for (int w2 = 0; w2 < LB_WARPS; w2++) {
+                if (fi < 32 * LB_WARPS) break;
+                const unsigned im = s_incm[w2], om = s_okm[w2];
+                if (im) {
+                    const int l = __ffs(im) - 1;
+                    const unsigned need = l < 31 ? ((2u << l) - 1u) : FULL;
+                    valid = valid && (om & need) == need;
+                    fi = w2 * 32 + l;
+                } else {
+                    valid = valid && om == FULL;
+                }
+            }
+            if (valid) {
+                __threadfence();  // acquire: the values published with those flags
+                long long val = 0;
+                if (t <= fi && idx >= 0)
+                    val = t == fi ? (long long)ld_relaxed_u64((const unsigned long long *)&inc[idx])
+                                  : (long long)ld_relaxed_u64((const unsigned long long *)&agg[idx]);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(FULL, val, o);
+                if (lane == 0) s_part[warp] = val;
+                lb_sync();
+#pragma unroll
+                for (int w2 = 0; w2 < LB_WARPS; w2++) prefix += s_part[w2];
+                lb_sync();  // before the next window reuses the shared words
+                if (fi < 32 * LB_WARPS) break;
+                p -= 32 * LB_WARPS;
+                continue;
+            }
+            if (t == 0) s_abort = (++spins & 31u) == 0 && globaltimer_ns() - t0 > LOOKBACK_TIMEOUT_NS;
+            lb_sync();
+            const bool abort = s_abort;
+            lb_sync();
+            if (abort) {
+                if (t == 0) atomicExch(&ctl[2], (unsigned)DEV_TIMEOUT);
+                prefix = 0;
+                break;
+            }
+        }
+        if (t == 0) {
+            const long long tile_sum = s_tile_sum;
+            inc[tile] = prefix + tile_sum;
+            __threadfence();
+            st_release_gpu(&flags[tile], tag | ST_INC);
             s_prefix = prefix;
             if (tile == ntiles - 1 && total_out) *total_out = (Tout)(prefix + tile_sum);
         }
