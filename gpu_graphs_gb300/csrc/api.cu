@@ -308,10 +308,18 @@ static void fill_stats(gbfs_stats *s, const BfsResult &r, int64_t nsources)
     s->edges_traversed = r.reached - nsources;
 }
 
-static gbfs_params effective_params(const gbfs_graph *g)
+// Parameters for a traversal of g: bottom-up steps need in-edges, so a
+// graph whose in-edges differ from its out-edges gets its transpose built
+// here on first use (top-down only if that fails for lack of memory).
+// Caller holds g->mu.
+static gbfs_params effective_params(gbfs_graph *g)
 {
     gbfs_params p = graph_params(g);
-    if (!g->symmetric) p.direction = GBFS_DIR_TOPDOWN;
+    if (!g->symmetric && p.direction != GBFS_DIR_TOPDOWN && !g->csr.trow) {
+        std::string err;
+        if (csr_build_transpose(g->csr, g->stream, err) != GBFS_OK) cudaGetLastError();
+    }
+    if (!g->symmetric && !g->csr.trow) p.direction = GBFS_DIR_TOPDOWN;
     return p;
 }
 

@@ -30,8 +30,8 @@
 //                   frontier has fewer than (non-isolated vertices)/beta
 //                   vertices and is shrinking.  A queue <-> bitmap
 //                   conversion phase runs at each switch.
-// Bottom-up needs in-edges == out-edges, so it is used on symmetric graphs
-// only; other graphs run top-down at every level.
+// Bottom-up probes in-edges: the graph itself when symmetric, else its
+// transpose (built on demand); without either, every level is top-down.
 #include <algorithm>
 #include <cstddef>
 #include <cstring>
@@ -54,6 +54,7 @@ struct BfsArgs {
     long long m;
     const int *row;
     const int *col;
+    const int *brow, *bcol;  // bottom-up adjacency: in-edges (row/col when symmetric)
     const unsigned *zmask;   // out-degree-0 bitmap, or NULL (directed graphs:
                              // a sink still has in-edges, so it stays claimable)
     int *level;
@@ -327,7 +328,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
         edges_c += mf;
         m_u -= (long long)mf;
         bool bu;
-        if (a.direction == GBFS_DIR_TOPDOWN) bu = false;
+        if (a.direction == GBFS_DIR_TOPDOWN || a.brow == nullptr) bu = false;
         else if (a.direction == GBFS_DIR_BOTTOMUP) bu = true;
         else if (td) bu = (long long)mf * a.alpha > m_u;
         else bu = !((long long)nf * a.beta < a.n_active && nf < prev_nf);
@@ -489,8 +490,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                     }
                     const int va = vv[0], vb = vv[1];
                     int ia = 0, ea = 0, ib = 0, eb = 0;
-                    if (va >= 0) { ia = __ldg(a.row + va); ea = __ldg(a.row + va + 1); }
-                    if (vb >= 0) { ib = __ldg(a.row + vb); eb = __ldg(a.row + vb + 1); }
+                    if (va >= 0) { ia = __ldg(a.brow + va); ea = __ldg(a.brow + va + 1); }
+                    if (vb >= 0) { ib = __ldg(a.brow + vb); eb = __ldg(a.brow + vb + 1); }
                     const int da = ea - ia, db = eb - ib;
                     bool fa = false, fb = false;
                     // First step: FIRST_PROBE neighbours (most vertices find their
@@ -501,8 +502,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                         int ua[PROBE], ub[PROBE];
 #pragma unroll
                         for (int t = 0; t < PROBE; t++) {
-                            ua[t] = (t < width && !fa && ia + t < ea) ? __ldg(a.col + ia + t) : -1;
-                            ub[t] = (t < width && !fb && ib + t < eb) ? __ldg(a.col + ib + t) : -1;
+                            ua[t] = (t < width && !fa && ia + t < ea) ? __ldg(a.bcol + ia + t) : -1;
+                            ub[t] = (t < width && !fb && ib + t < eb) ? __ldg(a.bcol + ib + t) : -1;
                         }
                         unsigned ga = 0, gb = 0;
 #pragma unroll
@@ -514,17 +515,19 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                         if (!fb && ib < eb) { if (gb & 1u) fb = true; else ib += width; }
                         width = PROBE;
                     }
+                    // the next frontier's out-edges (for the direction rule): the
+                    // probed in-degree when in-edges are the out-edges
                     if (fa) {
                         a.level[va] = nl;
                         atomicOr(&my_found[(va >> 5) - w0], 1u << (va & 31));
                         ++my_cnt;
-                        my_deg += (unsigned long long)da;
+                        my_deg += (unsigned long long)(a.brow == a.row ? da : __ldg(a.row + va + 1) - __ldg(a.row + va));
                     }
                     if (fb) {
                         a.level[vb] = nl;
                         atomicOr(&my_found[(vb >> 5) - w0], 1u << (vb & 31));
                         ++my_cnt;
-                        my_deg += (unsigned long long)db;
+                        my_deg += (unsigned long long)(a.brow == a.row ? db : __ldg(a.row + vb + 1) - __ldg(a.row + vb));
                     }
                 }
                 __syncwarp();
@@ -738,6 +741,11 @@ BfsArgs make_args(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const in
     a.m = g.m;
     a.row = g.row;
     a.col = g.col;
+    // in-edges for bottom-up steps; null when neither (then every level is
+    // top-down); the transpose is read only when bottom-up may run
+    const bool bu_possible = p.direction != GBFS_DIR_TOPDOWN;
+    a.brow = symmetric ? g.row : bu_possible ? g.trow : nullptr;
+    a.bcol = symmetric ? g.col : bu_possible ? g.tcol : nullptr;
     a.zmask = symmetric ? g.zmask : nullptr;
     a.level = d_level;
     a.visited = w.visited;

@@ -726,8 +726,78 @@ done:
     return rc;
 }
 
+namespace {
+
+__global__ void k_in_count(const int *__restrict__ col, int64_t m, int *indeg)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd(&indeg[col[i]], 1);
+}
+
+// One warp per row u: every out-edge u -> v lands in v's in-row.
+__global__ void k_in_scatter(const int *__restrict__ row, const int *__restrict__ col, int n, int *cursor, int *tcol)
+{
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < n; u += warps)
+        for (int i = row[u] + (int)lane_id(); i < row[u + 1]; i += 32) tcol[atomicAdd(&cursor[col[i]], 1)] = (int)u;
+}
+
+}  // namespace
+
+int csr_build_transpose(DeviceCsr &c, cudaStream_t st, std::string &err)
+{
+    if (c.trow) return GBFS_OK;
+    int rc = GBFS_OK;
+    const int n = c.n;
+    const int64_t m = c.m;
+    int *indeg = nullptr, *cursor = nullptr, *trow = nullptr, *tcol = nullptr;
+    void *scan_mem = nullptr;
+    ScanScratch ss;
+    const int64_t tiles = scan_tiles((int64_t)n + 1);
+    CK(cudaMalloc(&indeg, sizeof(int) * ((size_t)n + 1)));
+    CK(cudaMalloc(&trow, sizeof(int) * ((size_t)n + 1)));
+    CK(cudaMalloc(&cursor, sizeof(int) * ((size_t)n + 1)));
+    CK(cudaMalloc(&tcol, sizeof(int) * (size_t)std::max<int64_t>(m, 1)));
+    CK(cudaMalloc(&scan_mem, scan_scratch_bytes(tiles)));
+    CK(cudaMemsetAsync(scan_mem, 0, scan_scratch_bytes(tiles), st));
+    scan_scratch_carve(scan_mem, tiles, ss);
+    CK(cudaMemsetAsync(indeg, 0, sizeof(int) * ((size_t)n + 1), st));
+    if (m > 0) {
+        k_in_count<<<grid_for(m, 256), 256, 0, st>>>(c.col, m, indeg);
+        CK(cudaGetLastError());
+    }
+    CK(scan_exclusive_i32_i32(indeg, trow, n, trow + n, ss, st));
+    CK(cudaMemcpyAsync(cursor, trow, sizeof(int) * ((size_t)n + 1), cudaMemcpyDeviceToDevice, st));
+    if (m > 0) {
+        k_in_scatter<<<grid_for((int64_t)n * 32, 256), 256, 0, st>>>(c.row, c.col, n, cursor, tcol);
+        CK(cudaGetLastError());
+    }
+    CK(cudaStreamSynchronize(st));
+    {
+        unsigned h_scan_status[3] = {0, 0, 0};
+        CK(cudaMemcpy(h_scan_status, ss.ctl, 12, cudaMemcpyDeviceToHost));
+        if (h_scan_status[2] != 0) {
+            err = "scan look-back timed out";
+            rc = GBFS_ERR_TIMEOUT;
+            goto done;
+        }
+    }
+    c.trow = trow;
+    c.tcol = tcol;
+    trow = tcol = nullptr;
+done:
+    if (indeg) cudaFree(indeg);
+    if (cursor) cudaFree(cursor);
+    if (trow) cudaFree(trow);
+    if (tcol) cudaFree(tcol);
+    if (scan_mem) cudaFree(scan_mem);
+    return rc;
+}
+
 void csr_free(DeviceCsr &c)
 {
+    if (c.trow) cudaFree(c.trow);
+    if (c.tcol) cudaFree(c.tcol);
     if (c.heavy) cudaFree(c.heavy);
     if (c.pieces) cudaFree(c.pieces);
     if (c.row) cudaFree(c.row);

@@ -25,6 +25,10 @@ struct DeviceCsr {
     int2 *pieces = nullptr;
     int32_t npieces = 0;
     bool pieces_built = false;
+    // transpose (in-edges), built on demand for bottom-up steps on graphs
+    // whose in-edges differ from their out-edges; rows unsorted
+    int *trow = nullptr;       // n+1
+    int *tcol = nullptr;       // m
 };
 
 // Rows longer than this are walked by a whole warp in multi-source passes.
@@ -46,6 +50,9 @@ int csr_check_symmetric(const DeviceCsr &c, cudaStream_t st, bool &sym, std::str
 
 // Move each row's highest-degree neighbour to the row's front.
 int csr_hub_first(DeviceCsr &c, cudaStream_t st, std::string &err);
+
+// Build c.trow / c.tcol (the in-edge CSR); a no-op once built.  Synchronises st.
+int csr_build_transpose(DeviceCsr &c, cudaStream_t st, std::string &err);
 
 void csr_free(DeviceCsr &c);
 

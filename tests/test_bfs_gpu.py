@@ -121,12 +121,36 @@ def test_grid_high_diameter(gb, orc):
 def test_er_and_directed(gb, orc):
     src, dst = gb.gen_er(200000, 800000, seed=4)
     _check_against_oracle(gb, orc, 200000, src, dst, [0, 5, 199999])
-    # directed as stored: bottom-up must not be used (no reverse edges)
+    # directed as stored: bottom-up steps probe the transpose (in-edges)
     src, dst = gb.gen_er(50000, 150000, seed=5)
     g, _ = _check_against_oracle(gb, orc, 50000, src, dst, [0, 1, 2], flags=0)
     g.set_params(direction=2)
     o = orc.csr_build(50000, src, dst, 0)
     assert np.array_equal(g.bfs(3), orc.bfs_queue(o, 3))
+
+
+@pytest.mark.parametrize("direction", [0, 1, 2])
+def test_directed_rmat_direction_optimising(gb, orc, direction):
+    """Directed power-law graph: top-down, bottom-up over the transpose, and
+    the switching rule between them all give the oracle's levels."""
+    n = 1 << 17
+    src, dst = gb.gen_rmat(17, 16, seed=71)
+    flags = gb.DEDUP | gb.DROP_SELF_LOOPS
+    o = orc.csr_build(n, src, dst, flags)
+    g = gb.Graph.from_edges(n, src, dst, flags)
+    g.set_params(direction=direction)
+    outdeg = np.diff(o.row_offset)
+    sources = [int(np.argmax(outdeg)), int(np.flatnonzero(outdeg > 0)[7]), 5]
+    for s0 in sources:
+        got, st = g.bfs(s0, stats=True)
+        want = orc.bfs_queue(o, s0)
+        assert np.array_equal(got, want), (direction, s0)
+        if direction == 1:
+            assert st.bu_levels == 0
+    lv, par = g.bfs_parents(sources[0])
+    assert np.array_equal(par, orc.min_parents(o, lv))
+    gs = g.bfs_multiroot(sources)
+    assert gs.shape == (n,)
 
 
 def test_edge_cases(gb, orc):
