@@ -23,7 +23,9 @@ Extra objects on the same line (rank 0, skipped with --no-extra): grid
 (7000 x 7000, persistent vs one launch per level), batched (64-lane
 multi-source on RMAT-20; 512 small graphs in one launch), primitives (CSR
 build, exclusive scan) and serving (32 resident graphs, Poisson arrivals;
---no-serving skips it).
+--no-serving skips it).  The batched and serving objects carry a
+cpu_parallel throughput: the same queries through the oracle's queue BFS,
+one query per host core at a time.
 
 --impl reference times that CPU path alone (the reference's own code cannot
 be compiled on the GPU host: its sources are not shipped there).
@@ -229,6 +231,20 @@ def cpu_bfs_sample(n: int, row: np.ndarray, col: np.ndarray, sources, threads: i
     return wall, edges, levels
 
 
+def cpu_parallel_queries(tasks, threads: int = 0) -> dict:
+    """Embarrassingly parallel CPU throughput: the oracle's queue BFS (the
+    reference's CPU algorithm), one query per host core at a time.  `tasks`
+    is a list of (oracle CSR, source); returns queries/s and the levels."""
+    import oracle
+    threads = threads or (os.cpu_count() or 1)
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(threads) as ex:
+        levels = list(ex.map(lambda t: oracle.bfs_queue(t[0], int(t[1])), tasks))
+    wall = time.perf_counter() - t0
+    return {"queries_per_s": round(len(tasks) / wall, 1), "cores": threads, "queries": len(tasks),
+            "seconds": round(wall, 3)}, levels
+
+
 def run_reference(args, rank: int, world: int) -> None:
     """--impl reference: the reference's CPU BFS (oracle port) on the host cores."""
     if rank != 0:
@@ -323,7 +339,7 @@ def measure_batched(torch) -> dict:
     src, dst = gb.gen_rmat(20, 16, 0.57, 0.19, 0.19, seed=1)
     g = gb.Graph.from_edges(n20, src, dst, gb.UNDIRECTED | gb.HUB_FIRST)
     del src, dst
-    row, _ = g.csr()
+    row, col = g.csr()
     sources = pick_sources(np.diff(row), 64)
     plain_out = torch.empty((64, n20), dtype=torch.int32, device="cuda")
     multi_out = torch.empty((64, n20), dtype=torch.int32, device="cuda")
@@ -344,7 +360,17 @@ def measure_batched(torch) -> dict:
         "plain_queries_per_s": round(64 / (t_plain / 1e3), 1), "batched_queries_per_s": round(64 / (t_multi / 1e3), 1),
         "speedup": round(t_plain / t_multi, 2), "speedup_vs_topdown": round(t_plain_td / t_multi, 2),
         "levels_identical": same}
-    del plain_out, multi_out, g
+    # the same 64 queries on the host cores, one per core at a time
+    import oracle
+    og = oracle.CSR(n20, row.astype(np.int64), col)
+    cpu, lv = cpu_parallel_queries([(og, s0) for s0 in sources])
+    mo = multi_out.cpu().numpy()
+    cpu["levels_identical"] = all(np.array_equal(a, b) for a, b in zip(lv, mo))
+    cpu["kind"] = "port"
+    res["multi_source"]["cpu_parallel"] = cpu
+    res["multi_source"]["speedup_vs_cpu_parallel"] = round(res["multi_source"]["batched_queries_per_s"] /
+                                                           cpu["queries_per_s"], 1)
+    del plain_out, multi_out, g, og, row, col, mo, lv
 
     rng = np.random.default_rng(1)
     sizes = np.exp(rng.uniform(np.log(256), np.log(65536), 512)).astype(np.int64)
@@ -363,12 +389,20 @@ def measure_batched(torch) -> dict:
         h.bfs(s0, out=o)
     t_plain = min(sum(h.bfs(s0, out=o, stats=True)[1].ms for h, o, s0 in zip(handles, douts, srcs)) for _ in range(2))
     same = all(np.array_equal(f, o.cpu().numpy()) for f, o in zip(fused, douts))
+    ocsr = []
+    for h in handles:
+        r_, c_ = h.csr()
+        ocsr.append(oracle.CSR(h.n, r_.astype(np.int64), c_))
+    cpu, lv = cpu_parallel_queries(list(zip(ocsr, srcs)))
+    cpu["levels_identical"] = all(np.array_equal(a, b) for a, b in zip(lv, fused))
+    cpu["kind"] = "port"
     res["many_graphs"] = {
         "workload": f"512 ER graphs, n log-uniform in [256, 65536] (total {int(sizes.sum())} vertices), avg degree 8, "
                     "one source each, one fused launch",
         "plain_ms": round(t_plain, 3), "fused_ms": round(t_fused, 3),
         "plain_queries_per_s": round(512 / (t_plain / 1e3), 1), "fused_queries_per_s": round(512 / (t_fused / 1e3), 1),
-        "speedup": round(t_plain / t_fused, 2), "levels_identical": bool(same)}
+        "speedup": round(t_plain / t_fused, 2), "levels_identical": bool(same),
+        "cpu_parallel": cpu, "speedup_vs_cpu_parallel": round(512 / (t_fused / 1e3) / cpu["queries_per_s"], 1)}
     return res
 
 
@@ -467,6 +501,20 @@ def measure_serving(torch, seconds: float = 2.0, fractions=(0.25, 0.5, 0.75, 1.0
                                           "p99_ms": round(plain_ms[int(0.99 * (len(plain_ms) - 1))], 3)},
            "plain_topdown_queries_per_s": round(len(draws) / (plain_td_ms / 1e3), 1)}
     log("serving: plain baseline done")
+    # the first 32 of the same queries on the host cores, one per core at a time
+    import oracle
+    cpu_draws = draws[:32]
+    ocsr = {}
+    for gi, _ in cpu_draws:
+        if gi not in ocsr:
+            r_, c_ = graphs[gi].csr()
+            ocsr[gi] = oracle.CSR(graphs[gi].n, r_.astype(np.int64), c_)
+    cpu, lv = cpu_parallel_queries([(ocsr[gi], s0) for gi, s0 in cpu_draws])
+    cpu["kind"] = "port"
+    cpu["levels_identical"] = all(np.array_equal(a, graphs[gi].bfs(s0)) for a, (gi, s0) in zip(lv, cpu_draws))
+    out["cpu_parallel"] = cpu
+    del ocsr, lv
+    log(f"serving: cpu parallel {cpu}")
     sweep = []
     # pinned result buffers (8 per graph, reused round robin: contents are not
     # checked here, the serving tests do that)
@@ -532,6 +580,7 @@ def measure_serving(torch, seconds: float = 2.0, fractions=(0.25, 0.5, 0.75, 1.0
     out["sweep"] = sweep
     out["capacity_vs_plain"] = round(capacity / out["plain_one_query_per_launch"]["queries_per_s"], 2)
     out["capacity_vs_plain_topdown"] = round(capacity / out["plain_topdown_queries_per_s"], 2)
+    out["capacity_vs_cpu_parallel"] = round(capacity / out["cpu_parallel"]["queries_per_s"], 1)
     return out
 
 def main():

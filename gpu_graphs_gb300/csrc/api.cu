@@ -584,11 +584,11 @@ extern "C" int gbfs_bfs_multi(gbfs_graph *g, const int32_t *sources, int32_t k, 
     std::string err;
     int rc = ms_work_alloc(g->ms, g->csr.n, err);
     if (rc) return fail(rc, err);
+    const gbfs_params p = effective_params(g);  // builds the transpose a directed graph's pull steps need
     rc = ms_prepare(g->csr, g->stream, err);
     if (rc) return fail(rc, err);
     const bool dev_out = is_device_ptr(levels_out);
     const size_t n = (size_t)g->csr.n;
-    gbfs_params p = graph_params(g);
     MsResult tot;
     g->last_multi = true;
     for (int32_t b0 = 0; b0 < k; b0 += MS_LANES) {

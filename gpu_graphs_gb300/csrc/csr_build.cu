@@ -750,7 +750,8 @@ int csr_build_transpose(DeviceCsr &c, cudaStream_t st, std::string &err)
     int rc = GBFS_OK;
     const int n = c.n;
     const int64_t m = c.m;
-    int *indeg = nullptr, *cursor = nullptr, *trow = nullptr, *tcol = nullptr;
+    int *indeg = nullptr, *cursor = nullptr, *trow = nullptr, *tcol = nullptr, *theavy = nullptr;
+    unsigned *d_nheavy = nullptr, h_nheavy = 0;
     void *scan_mem = nullptr;
     ScanScratch ss;
     const int64_t tiles = scan_tiles((int64_t)n + 1);
@@ -758,6 +759,9 @@ int csr_build_transpose(DeviceCsr &c, cudaStream_t st, std::string &err)
     CK(cudaMalloc(&trow, sizeof(int) * ((size_t)n + 1)));
     CK(cudaMalloc(&cursor, sizeof(int) * ((size_t)n + 1)));
     CK(cudaMalloc(&tcol, sizeof(int) * (size_t)std::max<int64_t>(m, 1)));
+    CK(cudaMalloc(&theavy, sizeof(int) * (size_t)std::max(1, n)));
+    CK(cudaMalloc(&d_nheavy, sizeof(unsigned)));
+    CK(cudaMemsetAsync(d_nheavy, 0, sizeof(unsigned), st));
     CK(cudaMalloc(&scan_mem, scan_scratch_bytes(tiles)));
     CK(cudaMemsetAsync(scan_mem, 0, scan_scratch_bytes(tiles), st));
     scan_scratch_carve(scan_mem, tiles, ss);
@@ -772,6 +776,9 @@ int csr_build_transpose(DeviceCsr &c, cudaStream_t st, std::string &err)
         k_in_scatter<<<grid_for((int64_t)n * 32, 256), 256, 0, st>>>(c.row, c.col, n, cursor, tcol);
         CK(cudaGetLastError());
     }
+    k_heavy_list<<<grid_for(n, 256), 256, 0, st>>>(trow, n, theavy, d_nheavy);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(&h_nheavy, d_nheavy, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     {
         unsigned h_scan_status[3] = {0, 0, 0};
@@ -784,8 +791,12 @@ int csr_build_transpose(DeviceCsr &c, cudaStream_t st, std::string &err)
     }
     c.trow = trow;
     c.tcol = tcol;
-    trow = tcol = nullptr;
+    c.theavy = theavy;
+    c.ntheavy = (int32_t)h_nheavy;
+    trow = tcol = theavy = nullptr;
 done:
+    if (theavy) cudaFree(theavy);
+    if (d_nheavy) cudaFree(d_nheavy);
     if (indeg) cudaFree(indeg);
     if (cursor) cudaFree(cursor);
     if (trow) cudaFree(trow);
@@ -798,6 +809,8 @@ void csr_free(DeviceCsr &c)
 {
     if (c.trow) cudaFree(c.trow);
     if (c.tcol) cudaFree(c.tcol);
+    if (c.theavy) cudaFree(c.theavy);
+    if (c.tpieces) cudaFree(c.tpieces);
     if (c.heavy) cudaFree(c.heavy);
     if (c.pieces) cudaFree(c.pieces);
     if (c.row) cudaFree(c.row);

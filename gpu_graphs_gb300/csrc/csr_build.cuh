@@ -29,6 +29,12 @@ struct DeviceCsr {
     // whose in-edges differ from their out-edges; rows unsorted
     int *trow = nullptr;       // n+1
     int *tcol = nullptr;       // m
+    int *theavy = nullptr;     // vertices of in-degree > HEAVY_DEGREE (built with the transpose)
+    int32_t ntheavy = 0;
+    // multi-source pull pieces over the transpose (ms_prepare, once trow exists)
+    int2 *tpieces = nullptr;
+    int32_t ntpieces = 0;
+    bool tpieces_built = false;
 };
 
 // Rows longer than this are walked by a whole warp in multi-source passes.

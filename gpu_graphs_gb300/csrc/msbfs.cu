@@ -14,8 +14,9 @@
 //     memory); each edge claims its lanes at the neighbour with one atomicOr
 //     on vis, the claimed lanes go into the next frontier mask with a second
 //     atomicOr, whose first writer appends the neighbour to the next queue;
-//   * pull step (dense frontiers, symmetric graphs): every vertex with
-//     unreached lanes ORs F over its row until those lanes are covered --
+//   * pull step (dense frontiers): every vertex with unreached lanes ORs F
+//     over its in-edges (its own row on a symmetric graph, its row of the
+//     transpose on a directed one) until those lanes are covered --
 //     one thread per light row, a whole warp per row of degree > 64;
 //   * frontier masks and queues rotate by level, and the masks of level L-1
 //     are cleared through their queue during level L, so no pass touches all
@@ -39,7 +40,8 @@ constexpr int MS_BIG = 256;                  // push rows this long go to a grid
 
 struct MsArgs {
     int n, n_active, k;
-    const int *row, *col;
+    const int *row, *col;     // out-edges: push steps
+    const int *prow, *pcol;   // in-edges: pull steps (row/col on a symmetric graph)
     const int *heavy;
     int nheavy;
     const int2 *pieces;
@@ -313,17 +315,17 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
                 const long long u = base + lane;
                 unsigned long long nw = 0;
                 if (u < n) {
-                    const int b = __ldg(a.row + u), e = __ldg(a.row + u + 1);
+                    const int b = __ldg(a.prow + u), e = __ldg(a.prow + u + 1);
                     if (e > b && e - b <= HEAVY_DEGREE) {
                         const unsigned long long vu = __ldcg(a.vis + u);
                         const unsigned long long need = ~vu & live;
                         if (need) {
                             unsigned long long acc = 0;
                             for (int i = b; i < e; i += 4) {
-                                const int v0 = __ldg(a.col + i);
-                                const int v1 = i + 1 < e ? __ldg(a.col + i + 1) : v0;
-                                const int v2 = i + 2 < e ? __ldg(a.col + i + 2) : v0;
-                                const int v3 = i + 3 < e ? __ldg(a.col + i + 3) : v0;
+                                const int v0 = __ldg(a.pcol + i);
+                                const int v1 = i + 1 < e ? __ldg(a.pcol + i + 1) : v0;
+                                const int v2 = i + 2 < e ? __ldg(a.pcol + i + 2) : v0;
+                                const int v3 = i + 3 < e ? __ldg(a.pcol + i + 3) : v0;
                                 acc |= __ldcg(Fc + v0) | __ldcg(Fc + v1) | __ldcg(Fc + v2) | __ldcg(Fc + v3);
                                 if ((acc & need) == need) break;
                             }
@@ -350,8 +352,8 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
                 unsigned long long vu = 0, need = 0;
                 if (h < a.nheavy) {
                     u = __ldg(a.heavy + h);
-                    b = __ldg(a.row + u);
-                    e = __ldg(a.row + u + 1);
+                    b = __ldg(a.prow + u);
+                    e = __ldg(a.prow + u + 1);
                     if (e - b <= MS_HUGE) {  // longer rows: split into pieces below
                         vu = __ldcg(a.vis + u);
                         need = ~vu & live;
@@ -371,7 +373,7 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
 #pragma unroll
                         for (int t = 0; t < 4; t++) {
                             const int i = i0 + t * 32 + (int)lane;
-                            if (i < re) x |= __ldcg(Fc + __ldg(a.col + i));
+                            if (i < re) x |= __ldcg(Fc + __ldg(a.pcol + i));
                         }
                         acc |= warp_or64(x);
                         if ((acc & rneed) == rneed) break;
@@ -412,7 +414,7 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
                     const int u = __shfl_sync(FULL, pc.x, sl), j = __shfl_sync(FULL, pc.y, sl);
                     const unsigned long long rvu = __shfl_sync(FULL, vu, sl);
                     const unsigned long long rneed = __shfl_sync(FULL, need, sl);
-                    const int rb = __ldg(a.row + u), re = __ldg(a.row + u + 1);
+                    const int rb = __ldg(a.prow + u), re = __ldg(a.prow + u + 1);
                     const unsigned pn = (unsigned)((re - rb + MS_PIECE - 1) / MS_PIECE);
                     const int b = rb + j * MS_PIECE;
                     const int e = min(re, b + MS_PIECE);
@@ -427,7 +429,7 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
 #pragma unroll
                             for (int t = 0; t < 4; t++) {
                                 const int i = i0 + t * 32 + (int)lane;
-                                if (i < e) x |= __ldcg(Fc + __ldg(a.col + i));
+                                if (i < e) x |= __ldcg(Fc + __ldg(a.pcol + i));
                             }
                             acc |= warp_or64(x);
                             if ((acc & rneed) == rneed) break;
@@ -606,34 +608,40 @@ size_t ms_smem_bytes()
 
 }  // namespace
 
-int64_t ms_prepare_bytes(const DeviceCsr &g)
+int64_t ms_prepare_bytes(const DeviceCsr &g, bool transpose)
 {
     // rows of degree d > 2 * MS_PIECE give ceil(d / MS_PIECE) < 1.5 d / MS_PIECE pieces
-    return g.pieces_built ? 0 : (int64_t)sizeof(int2) * (3 * g.m / (2 * MS_PIECE) + 1);
+    const int64_t one = (int64_t)sizeof(int2) * (3 * g.m / (2 * MS_PIECE) + 1);
+    return (g.pieces_built ? 0 : one) + (transpose && !g.tpieces_built ? one : 0);
 }
 
-int ms_prepare(DeviceCsr &g, cudaStream_t st, std::string &err)
+namespace {
+
+// The pull pieces of one adjacency (out-edge rows, or the transpose's
+// in-edge rows): {vertex, j} for the j-th MS_PIECE edges of every heavy row
+// longer than MS_HUGE.
+int build_pieces(const int *row, const int *heavy, int nheavy, cudaStream_t st, int2 *&out, int32_t &count,
+                 std::string &err)
 {
-    if (g.pieces_built) return GBFS_OK;
     std::vector<int2> h_pieces;
-    if (g.nheavy > 0 && g.max_degree > MS_HUGE) {
+    if (nheavy > 0) {
         int *deg = nullptr;
-        std::vector<int> h_heavy(g.nheavy), h_deg(g.nheavy);
-        cudaError_t e = cudaMalloc(&deg, sizeof(int) * (size_t)g.nheavy);
+        std::vector<int> h_heavy(nheavy), h_deg(nheavy);
+        cudaError_t e = cudaMalloc(&deg, sizeof(int) * (size_t)nheavy);
         if (e == cudaSuccess) {
-            k_heavy_degrees<<<std::max(1, std::min(1216, (g.nheavy + 255) / 256)), 256, 0, st>>>(g.row, g.heavy,
-                                                                                               g.nheavy, deg);
-            e = cudaMemcpyAsync(h_deg.data(), deg, sizeof(int) * (size_t)g.nheavy, cudaMemcpyDeviceToHost, st);
+            k_heavy_degrees<<<std::max(1, std::min(1216, (nheavy + 255) / 256)), 256, 0, st>>>(row, heavy, nheavy,
+                                                                                             deg);
+            e = cudaMemcpyAsync(h_deg.data(), deg, sizeof(int) * (size_t)nheavy, cudaMemcpyDeviceToHost, st);
         }
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(h_heavy.data(), g.heavy, sizeof(int) * (size_t)g.nheavy, cudaMemcpyDeviceToHost, st);
+            e = cudaMemcpyAsync(h_heavy.data(), heavy, sizeof(int) * (size_t)nheavy, cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         cudaFree(deg);
         if (e != cudaSuccess) {
             err = std::string("pull pieces: ") + cudaGetErrorString(e);
             return GBFS_ERR_CUDA;
         }
-        for (int i = 0; i < g.nheavy; i++)
+        for (int i = 0; i < nheavy; i++)
             if (h_deg[i] > MS_HUGE)
                 for (int j = 0; j * MS_PIECE < h_deg[i]; j++) h_pieces.push_back(make_int2(h_heavy[i], j));
     }
@@ -649,9 +657,26 @@ int ms_prepare(DeviceCsr &g, cudaStream_t st, std::string &err)
             return e == cudaErrorMemoryAllocation ? GBFS_ERR_OOM : GBFS_ERR_CUDA;
         }
     }
-    g.pieces = d;
-    g.npieces = (int32_t)h_pieces.size();
-    g.pieces_built = true;
+    out = d;
+    count = (int32_t)h_pieces.size();
+    return GBFS_OK;
+}
+
+}  // namespace
+
+int ms_prepare(DeviceCsr &g, cudaStream_t st, std::string &err)
+{
+    if (!g.pieces_built) {
+        const int nh = g.max_degree > MS_HUGE ? g.nheavy : 0;
+        const int rc = build_pieces(g.row, g.heavy, nh, st, g.pieces, g.npieces, err);
+        if (rc) return rc;
+        g.pieces_built = true;
+    }
+    if (g.trow && !g.tpieces_built) {
+        const int rc = build_pieces(g.trow, g.theavy, g.ntheavy, st, g.tpieces, g.ntpieces, err);
+        if (rc) return rc;
+        g.tpieces_built = true;
+    }
     return GBFS_OK;
 }
 
@@ -707,7 +732,7 @@ int64_t ms_work_bytes(int64_t n)
     return n > 0 ? (int64_t)(8 * 5 + 4 * 6 + 5 * MS_LANES) * n + 4096 : 0;
 }
 
-cudaError_t msbfs_enqueue(const DeviceCsr &g, const gbfs_params &p, bool pull_allowed, MsWork &w,
+cudaError_t msbfs_enqueue(const DeviceCsr &g, const gbfs_params &p, bool symmetric, MsWork &w,
                           const int *d_src, int k, int *d_out, cudaStream_t st, int max_ctas)
 {
     MsArgs a;
@@ -716,11 +741,17 @@ cudaError_t msbfs_enqueue(const DeviceCsr &g, const gbfs_params &p, bool pull_al
     a.k = k;
     a.row = g.row;
     a.col = g.col;
-    a.heavy = g.heavy;
-    a.nheavy = g.nheavy;
-    if (!g.pieces_built) return cudaErrorInvalidValue;  // ms_prepare not run
-    a.pieces = g.pieces;
-    a.npieces = g.npieces;
+    if (!g.pieces_built || (g.trow && !g.tpieces_built)) return cudaErrorInvalidValue;  // ms_prepare not run
+    // pull steps gather over in-edges: the rows themselves on a symmetric
+    // graph, the transpose on a directed one (no pull steps without it)
+    const bool pull_allowed = symmetric || g.trow != nullptr;
+    const bool tr = !symmetric && g.trow != nullptr;
+    a.prow = tr ? g.trow : g.row;
+    a.pcol = tr ? g.tcol : g.col;
+    a.heavy = tr ? g.theavy : g.heavy;
+    a.nheavy = tr ? g.ntheavy : g.nheavy;
+    a.pieces = tr ? g.tpieces : g.pieces;
+    a.npieces = tr ? g.ntpieces : g.npieces;
     a.hacc = w.hacc;
     a.hcnt = w.hcnt;
     a.vis = w.vis;
@@ -764,11 +795,11 @@ int ms_max_ctas()
     return sms * occ;
 }
 
-int msbfs_run(const DeviceCsr &g, const gbfs_params &p, bool pull_allowed, MsWork &w, const int *d_src, int k,
+int msbfs_run(const DeviceCsr &g, const gbfs_params &p, bool symmetric, MsWork &w, const int *d_src, int k,
               int *d_out, cudaStream_t st, MsResult &res, std::string &err)
 {
     cudaError_t e = cudaEventRecord(w.ev0, st);
-    if (e == cudaSuccess) e = msbfs_enqueue(g, p, pull_allowed, w, d_src, k, d_out, st, 0);
+    if (e == cudaSuccess) e = msbfs_enqueue(g, p, symmetric, w, d_src, k, d_out, st, 0);
     if (e == cudaSuccess) e = cudaEventRecord(w.ev1, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(w.h_ctrl, w.ctrl, offsetof(MsCtrl, t_entry), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);

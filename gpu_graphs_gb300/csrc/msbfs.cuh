@@ -47,11 +47,12 @@ struct MsWork {
     int64_t bytes = 0;
 };
 
-// Split the huge rows into pull pieces (DeviceCsr::pieces); a no-op once
-// built.  Synchronises st.
+// Split the huge rows into pull pieces (DeviceCsr::pieces, and tpieces for
+// the transpose once it exists); a no-op once built.  Synchronises st.
 int ms_prepare(DeviceCsr &g, cudaStream_t st, std::string &err);
-// Device bytes ms_prepare adds to a graph.
-int64_t ms_prepare_bytes(const DeviceCsr &g);
+// Device bytes ms_prepare adds to a graph (`transpose`: count the pieces of
+// the transpose too, built or about to be).
+int64_t ms_prepare_bytes(const DeviceCsr &g, bool transpose);
 
 // Device bytes ms_work_alloc takes for n vertices.
 int64_t ms_work_bytes(int64_t n);
@@ -68,16 +69,17 @@ struct MsResult {
 // Enqueue one launch: k <= 64 sources (device array d_src); d_out: k*n
 // int32, row i = levels of source i; results land in w.ctrl.  max_ctas > 0
 // caps the grid (concurrent launches on several streams must fit on the GPU
-// together, since every launch waits on all of its own CTAs).  No sync.
-cudaError_t msbfs_enqueue(const DeviceCsr &g, const gbfs_params &p, bool pull_allowed, MsWork &w,
+// together, since every launch waits on all of its own CTAs).  Pull steps
+// gather over in-edges: the rows themselves when `symmetric`, else the
+// transpose if it has been built (top-down only without it).  No sync.
+cudaError_t msbfs_enqueue(const DeviceCsr &g, const gbfs_params &p, bool symmetric, MsWork &w,
                           const int *d_src, int k, int *d_out, cudaStream_t st, int max_ctas);
 
 // CTAs of one full-GPU multi-source launch (0 on error).
 int ms_max_ctas();
 
-// msbfs_enqueue + read-back; pull_allowed: the graph is symmetric.
-// Synchronises `st`.
-int msbfs_run(const DeviceCsr &g, const gbfs_params &p, bool pull_allowed, MsWork &w,
+// msbfs_enqueue + read-back.  Synchronises `st`.
+int msbfs_run(const DeviceCsr &g, const gbfs_params &p, bool symmetric, MsWork &w,
               const int *d_src, int k, int *d_out, cudaStream_t st, MsResult &res,
               std::string &err);
 

@@ -51,6 +51,10 @@ struct SrvQuery {
 
 struct SrvGraph {
     gbfs_graph *g = nullptr;
+    // the graph's device buffers as admitted (out-edges, pull pieces and, for
+    // a directed graph, its transpose); none of them moves or is freed while
+    // the graph is resident, so workers launch on this copy without g->mu
+    DeviceCsr csr;
     int64_t bytes = 0;
     std::deque<std::shared_ptr<SrvQuery>> pending;
     int inflight = 0;
@@ -169,16 +173,17 @@ void gbfs_server::worker(int idx)
         gbfs_graph *g = sg->g;
         const int k = (int)batch.size();
         const auto t_launch = Clock::now();
-        const size_t n = (size_t)g->csr.n;
+        const DeviceCsr &csr = sg->csr;
+        const size_t n = (size_t)csr.n;
         int status = GBFS_OK;
         gbfs_params p = graph_params(g);
         p.timeout_ms = cfg.timeout_ms;
-        if (!g->symmetric) p.direction = GBFS_DIR_TOPDOWN;
+        if (!g->symmetric && !csr.trow) p.direction = GBFS_DIR_TOPDOWN;  // bottom-up needs in-edges
         cudaError_t e = cudaSuccess;
         int dev_status = DEV_OK;
         if (k == 1) {
             // one query: the single-source direction-optimising kernel
-            e = bfs_enqueue(g->csr, p, slot.bw, nullptr, 1, srcs[0], slot.bw.level, &slot.bw.ctrl->out, slot.st,
+            e = bfs_enqueue(csr, p, slot.bw, nullptr, 1, srcs[0], slot.bw.level, &slot.bw.ctrl->out, slot.st,
                             g->symmetric, 0, 0, bfs_ctas);
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync(&slot.bw.h_ctrl->status, &slot.bw.ctrl->status, sizeof(int),
@@ -196,7 +201,7 @@ void gbfs_server::worker(int idx)
         } else {
             e = cudaMemcpyAsync(slot.w.src, srcs.data(), sizeof(int32_t) * k, cudaMemcpyHostToDevice, slot.st);
             if (e == cudaSuccess)
-                e = msbfs_enqueue(g->csr, p, g->symmetric, slot.w, slot.w.src, k, slot.w.out, slot.st, max_ctas);
+                e = msbfs_enqueue(csr, p, g->symmetric, slot.w, slot.w.src, k, slot.w.out, slot.st, max_ctas);
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync(slot.w.h_ctrl, slot.w.ctrl, offsetof(MsCtrl, t_entry), cudaMemcpyDeviceToHost, slot.st);
             if (e == cudaSuccess) e = cudaStreamSynchronize(slot.st);
@@ -309,8 +314,13 @@ extern "C" int gbfs_server_add_graph(gbfs_server *s, gbfs_graph *g, int32_t *gra
 {
     if (!s || !g || !graph_id) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
     std::unique_lock<std::mutex> lk(s->mu);
+    // a directed graph that may step bottom-up gets its transpose (in-edge
+    // rows plus their heavy-row list) built here, inside the budget
+    const bool want_t = !g->symmetric && graph_params(g).direction != GBFS_DIR_TOPDOWN;
+    const bool has_t = want_t || g->csr.trow != nullptr;
+    const int64_t tbytes = has_t ? (int64_t)sizeof(int) * (2 * (int64_t)g->csr.n + 1 + g->csr.m) : 0;
     const int64_t gbytes = (int64_t)sizeof(int) * ((int64_t)g->csr.n + 1 + g->csr.m) + 4 * (((int64_t)g->csr.n + 31) / 32) +
-                           ms_prepare_bytes(g->csr);
+                           tbytes + ms_prepare_bytes(g->csr, has_t);
     const int64_t new_cap = std::max<int64_t>(s->n_cap, g->csr.n);
     const int64_t need = s->resident + gbytes + s->slots_total(new_cap);
     if (need > s->cfg.mem_budget_bytes) {
@@ -318,6 +328,7 @@ extern "C" int gbfs_server_add_graph(gbfs_server *s, gbfs_graph *g, int32_t *gra
         return fail(GBFS_ERR_BUDGET, "graph plus slot workspaces exceed the memory budget (" + std::to_string(need) +
                                          " > " + std::to_string(s->cfg.mem_budget_bytes) + " bytes)");
     }
+    DeviceCsr csr_snapshot;
     if (new_cap > s->n_cap) {
         // grow every slot's workspace once the slots are idle
         s->resizing = true;
@@ -355,12 +366,15 @@ extern "C" int gbfs_server_add_graph(gbfs_server *s, gbfs_graph *g, int32_t *gra
     {
         std::lock_guard<std::mutex> glk(g->mu);
         std::string err;
-        const int rc = ms_prepare(g->csr, g->stream, err);
+        int rc = want_t ? csr_build_transpose(g->csr, g->stream, err) : GBFS_OK;
+        if (!rc) rc = ms_prepare(g->csr, g->stream, err);
         if (rc) return fail(rc, err);
+        csr_snapshot = g->csr;
     }
     const int32_t gid = s->next_gid++;
     SrvGraph sg;
     sg.g = g;
+    sg.csr = csr_snapshot;
     sg.bytes = gbytes;
     s->graphs.emplace(gid, std::move(sg));
     s->resident += gbytes;

@@ -106,6 +106,9 @@ int gbfs_graph_get_csr(const gbfs_graph *g, int32_t *row_offset,
                        int32_t *col_idx);
 
 /* ---- traversal parameters (autotuned) --------------------------------- */
+/* Bottom-up steps probe in-edges: on a directed graph the first traversal
+ * that may take one builds the transpose (4(2n+1) + 4m device bytes) and
+ * keeps it with the graph; if that allocation fails the search is top-down. */
 #define GBFS_DIR_OPTIMIZING   0   /* Beamer top-down / bottom-up switching  */
 #define GBFS_DIR_TOPDOWN      1
 #define GBFS_DIR_BOTTOMUP     2
@@ -383,7 +386,10 @@ int gbfs_server_create(const gbfs_server_config *cfg, gbfs_server **out);
 /* Stops admission, drains in-flight work, frees slots (not the graphs). */
 void gbfs_server_destroy(gbfs_server *s);
 /* Admit a resident graph (borrowed; must outlive the server or be removed).
- * GBFS_ERR_BUDGET if its CSR plus one slot's workspace does not fit. */
+ * A directed graph whose direction is not GBFS_DIR_TOPDOWN gets its
+ * transpose (in-edge rows, for bottom-up and pull steps) built here and
+ * counted in the budget.  GBFS_ERR_BUDGET if its CSR plus one slot's
+ * workspace does not fit. */
 int gbfs_server_add_graph(gbfs_server *s, gbfs_graph *g, int32_t *graph_id);
 int gbfs_server_remove_graph(gbfs_server *s, int32_t graph_id);
 /* Queue one query; levels_out (host, n int32) is written before completion

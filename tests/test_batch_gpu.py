@@ -147,3 +147,29 @@ def test_multi_source_huge_rows(gb, orc):
         got = g.bfs_multi(sources)
         for i, s in enumerate(sources):
             assert np.array_equal(got[i], orc.bfs_queue(o, int(s))), (direction, i)
+
+
+def test_multi_source_directed_huge_in_rows(gb, orc):
+    """Directed graph whose pull steps gather over the transpose: vertex 7 has
+    30000 in-edges (a huge row of the transpose, scanned in pieces) and
+    vertex 11 9000 out-edges (a huge out-row, push only)."""
+    n = 60000
+    s1, d1 = gb.gen_er(n, 240000, seed=53)
+    rng = np.random.default_rng(54)
+    hub_in = rng.choice(n, 30000, replace=False).astype(np.int32)
+    hub_out = rng.choice(n, 9000, replace=False).astype(np.int32)
+    src = np.concatenate([s1, hub_in, np.full(9000, 11, np.int32)])
+    dst = np.concatenate([d1, np.full(30000, 7, np.int32), hub_out])
+    flags = gb.DEDUP | gb.DROP_SELF_LOOPS
+    o = orc.csr_build(n, src, dst, flags)
+    g = gb.Graph.from_edges(n, src, dst, flags)
+    outdeg = np.diff(o.row_offset)
+    assert np.bincount(o.col_idx, minlength=n)[7] > 4 * 2048
+    sources = list(rng.choice(np.flatnonzero(outdeg > 0), 64, replace=False))
+    for direction in (0, 1, 2):
+        g.set_params(direction=direction)
+        got, st = g.bfs_multi(sources, stats=True)
+        for i, s in enumerate(sources):
+            assert np.array_equal(got[i], orc.bfs_queue(o, int(s))), (direction, i)
+        if direction == 2:
+            assert st.bu_levels > 0

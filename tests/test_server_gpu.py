@@ -132,3 +132,31 @@ def test_server_with_concurrent_param_changes(gb, orc):
     finally:
         stop.set()
         th.join()
+
+
+def test_server_directed_graphs(gb, orc):
+    """Directed graphs in the server: single queries and batches step
+    bottom-up / pull over the transpose built at admission."""
+    graphs = []
+    for scale, seed in ((13, 21), (11, 22)):
+        s, d = gb.gen_rmat(scale, 16, seed=seed)
+        n = 1 << scale
+        flags = gb.DEDUP | gb.DROP_SELF_LOOPS
+        graphs.append((gb.Graph.from_edges(n, s, d, flags), orc.csr_build(n, s, d, flags)))
+    s, d = gb.gen_er(5000, 20000, 23)
+    graphs.append((gb.Graph.from_edges(5000, s, d, 0), orc.csr_build(5000, s, d, 0)))
+    graphs[2][0].set_params(direction=1)  # stays top-down: no transpose
+    with gb.Server(mem_budget_bytes=4 << 30, num_slots=2, max_lanes=64, batch_window_us=300) as srv:
+        gids = [srv.add_graph(g) for g, _ in graphs]
+        rng = np.random.default_rng(24)
+        plan = [int(rng.integers(len(graphs))) for _ in range(300)]
+        plan = [(gi, int(rng.integers(graphs[gi][0].n))) for gi in plan]
+        tickets = [srv.submit(gids[gi], s0) for gi, s0 in plan]
+        for t, (gi, s0) in zip(tickets, plan):
+            got, info = srv.wait(t)
+            assert info.status == 0
+            assert np.array_equal(got, orc.bfs_queue(graphs[gi][1], s0)), (gi, s0)
+        for gi, (g, o) in enumerate(graphs):  # one query alone (single-source kernel)
+            t = srv.submit(gids[gi], 0)
+            got, info = srv.wait(t)
+            assert info.batch_lanes == 1 and np.array_equal(got, orc.bfs_queue(o, 0))
