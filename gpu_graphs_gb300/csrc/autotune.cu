@@ -135,7 +135,10 @@ extern "C" int gbfs_autotune(gbfs_graph *g, const int32_t *sources, int32_t nsou
             c.blocks_per_sm = bl;
             try_set(c);
         }
-    if (g->symmetric) {
+    // the switch thresholds matter once bottom-up steps can run: always on a
+    // symmetric graph, on a directed one once the reference runs above built
+    // its transpose
+    if (g->symmetric || g->csr.trow) {
         start = cur;
         for (int al : {2, 4, 8, 14, 24, 48, 96}) {
             gbfs_params c = start;

@@ -126,6 +126,23 @@ def test_autotune_keeps_levels_and_caches(gb, orc):
     assert p2.as_dict() == p.as_dict()
 
 
+def test_autotune_directed(gb, orc):
+    """A directed graph is tuned over its switch thresholds too (bottom-up
+    steps run on its transpose); the tuned parameters keep every level."""
+    n = 1 << 15
+    src, dst = gb.gen_rmat(15, 16, seed=32)
+    flags = gb.DEDUP | gb.DROP_SELF_LOOPS
+    o = orc.csr_build(n, src, dst, flags)
+    g = gb.Graph.from_edges(n, src, dst, flags)
+    outdeg = np.diff(o.row_offset)
+    sources = [int(x) for x in np.flatnonzero(outdeg > 0)[:3]]
+    p = g.autotune(sources)
+    assert p.direction == 0 and p.alpha >= 1 and p.beta >= 1
+    for s in sources + [int(np.argmax(outdeg))]:
+        got, st = g.bfs(s, stats=True)
+        assert np.array_equal(got, orc.bfs_queue(o, s))
+
+
 def test_multi_source_huge_rows(gb, orc):
     """Rows far above the pull piece size (hubs of degree 30000 and 9000) are
     scanned in pieces by many warps and settled by the last one (pull), or
