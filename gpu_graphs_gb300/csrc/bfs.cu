@@ -437,16 +437,20 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
         } else {
             ++bu_levels;
             unsigned long long my_cnt = 0, my_deg = 0;
-            // cw bitmap words per warp iteration, cw chosen so a chunk holds
-            // about 64 unvisited vertices (dense levels: small chunks keep
-            // every warp busy; sparse levels: large chunks avoid empty round
-            // trips).  A chunk's unvisited vertices are dealt two per lane
-            // and probed in interleaved steps; the warp owns the chunk's
-            // words, so fn / visited words are written without atomics.
+            // A warp takes chunks of cw bitmap words; a chunk's unvisited
+            // vertices are dealt two per lane (64 per round) and probed in
+            // interleaved steps; the warp owns the chunk's words, so fn /
+            // visited words are written without atomics.  cw aims a chunk at
+            // about 120 unvisited vertices (two nearly full rounds: about 64
+            // left half the chunks with a second round of a few vertices)
+            // when that still gives every warp two chunks, else at about 56
+            // (one round; small graphs and dense levels keep every warp
+            // busy), up to 32 words on sparse levels.
             long long unv_est = (long long)a.n_active - (long long)reached;
             if (unv_est < 1) unv_est = 1;
-            int cw = 2;
-            while (cw < 32 && (long long)cw * 32 * unv_est < 64LL * n) cw <<= 1;
+            long long cwl = (120LL * n) / (32LL * unv_est);
+            if (cwl < 1 || (long long)W < 2 * nwarps * cwl) cwl = (56LL * n) / (32LL * unv_est);
+            const int cw = (int)min(32LL, max(1LL, cwl));
             unsigned *my_found = (unsigned *)(s_beg) + (threadIdx.x >> 5) * 32;  // s_beg is free here
             my_found[lane] = 0;
             __syncwarp();

@@ -136,10 +136,12 @@ int gbfs_set_params(gbfs_graph *g, const gbfs_params *p);
 
 /*
  * Autotuner: times a grid of candidate parameters (block size, CTAs per SM,
- * alpha, beta, big_degree) on `nsources` sources of this graph, keeps the
- * fastest whose levels equal the default's, stores it in the graph and
- * returns it in *best (nullable).  A process-wide cache keyed by the
- * graph's size/degree signature makes repeated calls cheap.
+ * alpha, beta, big_degree) on up to 16 of `nsources` sources of this graph
+ * (pass 16 or more: per-source times vary widely), keeps a candidate only
+ * if it is more than 2 % faster than the best so far and its levels equal
+ * the default's, stores the result in the graph and returns it in *best
+ * (nullable).  A process-wide cache keyed by the graph's size/degree
+ * signature makes repeated calls cheap.
  */
 int gbfs_autotune(gbfs_graph *g, const int32_t *sources, int32_t nsources,
                   gbfs_params *best);
