@@ -58,6 +58,14 @@ int graph_wrap(DeviceCsr &csr, bool symmetric_known, bool symmetric, cudaStream_
     g->stream = st;
     cudaGetDevice(&g->device);
     gbfs_default_params(&g->params);
+    {
+        std::string err;
+        const int rc = csr_build_first(g->csr, st, err);  // after any row reordering
+        if (rc != GBFS_OK) {
+            gbfs_graph_destroy(g);
+            return fail(rc, err);
+        }
+    }
     if (symmetric_known) {
         g->symmetric = symmetric;
     } else {
@@ -273,8 +281,7 @@ extern "C" int gbfs_graph_get_info(const gbfs_graph *g, gbfs_graph_info *info)
     info->m = g->csr.m;
     info->max_degree = g->csr.max_degree;
     info->nonisolated = g->csr.nonisolated;
-    info->device_bytes = (int64_t)sizeof(int) * ((int64_t)g->csr.n + 1 + g->csr.m) +
-                         4 * (((int64_t)g->csr.n + 31) / 32) + g->work.bytes + g->ms.bytes;
+    info->device_bytes = csr_device_bytes(g->csr) + g->work.bytes + g->ms.bytes;
     return GBFS_OK;
 }
 

@@ -46,7 +46,6 @@ namespace {
 constexpr int SEG = 2048;    // frontier rows expanded edge-balanced per pass
 constexpr int ILP = 4;       // edges in flight per lane in top-down passes
 constexpr int PROBE = 8;     // neighbours probed per step in bottom-up
-constexpr int FIRST_PROBE = 2;  // neighbours probed by the first bottom-up step
 
 struct BfsArgs {
     int n;
@@ -55,6 +54,8 @@ struct BfsArgs {
     const int *row;
     const int *col;
     const int *brow, *bcol;  // bottom-up adjacency: in-edges (row/col when symmetric)
+    const int *bfirst;       // first entry of each brow row (-1: empty row)
+    const int *bsecond;      // second entries (-1 past the end); null: probe the first alone
     const unsigned *zmask;   // out-degree-0 bitmap, or NULL (directed graphs:
                              // a sink still has in-edges, so it stays claimable)
     int *level;
@@ -493,15 +494,36 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                         vv[h] = slot < U ? (int)((w0 + owner) * 32 + pos) : -1;
                     }
                     const int va = vv[0], vb = vv[1];
-                    int ia = 0, ea = 0, ib = 0, eb = 0;
-                    if (va >= 0) { ia = __ldg(a.brow + va); ea = __ldg(a.brow + va + 1); }
-                    if (vb >= 0) { ib = __ldg(a.brow + vb); eb = __ldg(a.brow + vb + 1); }
+                    const bool two = a.bsecond != nullptr;
+                    int ia = 0, ea = 0, ib = 0, eb = 0, pa = -1, pb = -1, qa = -1, qb = -1;
+                    if (va >= 0) {
+                        pa = __ldg(a.bfirst + va);
+                        if (two) qa = __ldg(a.bsecond + va);
+                        ia = __ldg(a.brow + va);
+                        ea = __ldg(a.brow + va + 1);
+                    }
+                    if (vb >= 0) {
+                        pb = __ldg(a.bfirst + vb);
+                        if (two) qb = __ldg(a.bsecond + vb);
+                        ib = __ldg(a.brow + vb);
+                        eb = __ldg(a.brow + vb + 1);
+                    }
                     const int da = ea - ia, db = eb - ib;
-                    bool fa = false, fb = false;
-                    // First step: FIRST_PROBE neighbours (most vertices find their
-                    // parent there); later steps PROBE wide.  Narrow first steps
-                    // keep the frontier-bitmap sector reads near one per vertex.
-                    int width = FIRST_PROBE;
+                    // First step: each row's first entry (hub-first rows: the
+                    // highest-degree neighbour, where most vertices find their
+                    // parent), with its second on other rows, from the compact
+                    // first-entry arrays, read coalesced with the row offsets
+                    // instead of one col_idx sector per row.  Later steps walk
+                    // the rest of the row, PROBE wide.
+                    unsigned ha = 0, hb = 0;  // the entries' bits loaded at once
+                    if (pa >= 0) ha |= __ldcg(fc + (pa >> 5)) >> (pa & 31);
+                    if (qa >= 0) ha |= __ldcg(fc + (qa >> 5)) >> (qa & 31);
+                    if (pb >= 0) hb |= __ldcg(fc + (pb >> 5)) >> (pb & 31);
+                    if (qb >= 0) hb |= __ldcg(fc + (qb >> 5)) >> (qb & 31);
+                    bool fa = ha & 1u, fb = hb & 1u;
+                    ia += two ? 2 : 1;
+                    ib += two ? 2 : 1;
+                    const int width = PROBE;
                     while ((ia < ea && !fa) || (ib < eb && !fb)) {
                         int ua[PROBE], ub[PROBE];
 #pragma unroll
@@ -517,7 +539,6 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                         }
                         if (!fa && ia < ea) { if (ga & 1u) fa = true; else ia += width; }
                         if (!fb && ib < eb) { if (gb & 1u) fb = true; else ib += width; }
-                        width = PROBE;
                     }
                     // the next frontier's out-edges (for the direction rule): the
                     // probed in-degree when in-edges are the out-edges
@@ -750,6 +771,12 @@ BfsArgs make_args(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const in
     const bool bu_possible = p.direction != GBFS_DIR_TOPDOWN;
     a.brow = symmetric ? g.row : bu_possible ? g.trow : nullptr;
     a.bcol = symmetric ? g.col : bu_possible ? g.tcol : nullptr;
+    a.bfirst = symmetric ? g.first : bu_possible ? g.tfirst : nullptr;
+    if (!a.bfirst) a.brow = a.bcol = nullptr;
+    // hub-first rows (the transpose's always are): most vertices find their
+    // parent at the first entry, and a second lookup per vertex costs more
+    // than it saves; other rows probe their first two entries at once
+    a.bsecond = symmetric && !g.hub_rows ? g.second : nullptr;
     a.zmask = symmetric ? g.zmask : nullptr;
     a.level = d_level;
     a.visited = w.visited;

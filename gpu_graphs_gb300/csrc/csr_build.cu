@@ -722,6 +722,7 @@ int csr_hub_first(DeviceCsr &c, cudaStream_t st, std::string &err)
     k_hub_first_cta<<<152 * 2, 512, 0, st>>>(c.row, c.n, c.col);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
+    c.hub_rows = true;
 done:
     return rc;
 }
@@ -732,6 +733,17 @@ __global__ void k_in_count(const int *__restrict__ col, int64_t m, int *indeg)
 {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
         atomicAdd(&indeg[col[i]], 1);
+}
+
+// first[v] / second[v]: row v's first / second entry, -1 past its end
+// (second may be null).
+__global__ void k_first(const int *__restrict__ row, const int *__restrict__ col, int n, int *first, int *second)
+{
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const int b = row[v], d = row[v + 1] - b;
+        first[v] = d > 0 ? col[b] : -1;
+        if (second) second[v] = d > 1 ? col[b + 1] : -1;
+    }
 }
 
 // One warp per row u: every out-edge u -> v lands in v's in-row.
@@ -750,7 +762,7 @@ int csr_build_transpose(DeviceCsr &c, cudaStream_t st, std::string &err)
     int rc = GBFS_OK;
     const int n = c.n;
     const int64_t m = c.m;
-    int *indeg = nullptr, *cursor = nullptr, *trow = nullptr, *tcol = nullptr, *theavy = nullptr;
+    int *indeg = nullptr, *cursor = nullptr, *trow = nullptr, *tcol = nullptr, *theavy = nullptr, *tfirst = nullptr;
     unsigned *d_nheavy = nullptr, h_nheavy = 0;
     void *scan_mem = nullptr;
     ScanScratch ss;
@@ -760,6 +772,7 @@ int csr_build_transpose(DeviceCsr &c, cudaStream_t st, std::string &err)
     CK(cudaMalloc(&cursor, sizeof(int) * ((size_t)n + 1)));
     CK(cudaMalloc(&tcol, sizeof(int) * (size_t)std::max<int64_t>(m, 1)));
     CK(cudaMalloc(&theavy, sizeof(int) * (size_t)std::max(1, n)));
+    CK(cudaMalloc(&tfirst, sizeof(int) * (size_t)std::max(1, n)));
     CK(cudaMalloc(&d_nheavy, sizeof(unsigned)));
     CK(cudaMemsetAsync(d_nheavy, 0, sizeof(unsigned), st));
     CK(cudaMalloc(&scan_mem, scan_scratch_bytes(tiles)));
@@ -778,6 +791,14 @@ int csr_build_transpose(DeviceCsr &c, cudaStream_t st, std::string &err)
     }
     k_heavy_list<<<grid_for(n, 256), 256, 0, st>>>(trow, n, theavy, d_nheavy);
     CK(cudaGetLastError());
+    // in-rows hub-first (the in-neighbour of highest in-degree, the likeliest
+    // to be reached early, is probed first), then their first entries
+    k_hub_first_warp<<<grid_for((int64_t)n * 32, 256), 256, 0, st>>>(trow, n, tcol);
+    CK(cudaGetLastError());
+    k_hub_first_cta<<<152 * 2, 512, 0, st>>>(trow, n, tcol);
+    CK(cudaGetLastError());
+    k_first<<<grid_for(n, 256), 256, 0, st>>>(trow, tcol, n, tfirst, nullptr);
+    CK(cudaGetLastError());
     CK(cudaMemcpyAsync(&h_nheavy, d_nheavy, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     {
@@ -793,9 +814,11 @@ int csr_build_transpose(DeviceCsr &c, cudaStream_t st, std::string &err)
     c.tcol = tcol;
     c.theavy = theavy;
     c.ntheavy = (int32_t)h_nheavy;
-    trow = tcol = theavy = nullptr;
+    c.tfirst = tfirst;
+    trow = tcol = theavy = tfirst = nullptr;
 done:
     if (theavy) cudaFree(theavy);
+    if (tfirst) cudaFree(tfirst);
     if (d_nheavy) cudaFree(d_nheavy);
     if (indeg) cudaFree(indeg);
     if (cursor) cudaFree(cursor);
@@ -805,11 +828,41 @@ done:
     return rc;
 }
 
+int csr_build_first(DeviceCsr &c, cudaStream_t st, std::string &err)
+{
+    int rc = GBFS_OK;
+    if (!c.first) CK(cudaMalloc(&c.first, sizeof(int) * (size_t)std::max(1, c.n)));
+    if (!c.second) CK(cudaMalloc(&c.second, sizeof(int) * (size_t)std::max(1, c.n)));
+    if (c.n > 0) {
+        k_first<<<grid_for(c.n, 256), 256, 0, st>>>(c.row, c.col, c.n, c.first, c.second);
+        CK(cudaGetLastError());
+    }
+    CK(cudaStreamSynchronize(st));
+done:
+    return rc;
+}
+
+int64_t csr_device_bytes(const DeviceCsr &c)
+{
+    const int64_t n = c.n, m = c.m;
+    int64_t b = 4 * (n + 1 + m) + 4 * ((n + 31) / 32) + 4 * n;  // row, col, zmask, heavy list
+    if (c.first) b += 4 * n;
+    if (c.second) b += 4 * n;
+    if (c.pieces) b += 8 * (int64_t)c.npieces;
+    if (c.trow) b += 4 * (n + 1 + m) + 4 * n;                    // trow, tcol, theavy
+    if (c.tfirst) b += 4 * n;
+    if (c.tpieces) b += 8 * (int64_t)c.ntpieces;
+    return b;
+}
+
 void csr_free(DeviceCsr &c)
 {
     if (c.trow) cudaFree(c.trow);
     if (c.tcol) cudaFree(c.tcol);
     if (c.theavy) cudaFree(c.theavy);
+    if (c.tfirst) cudaFree(c.tfirst);
+    if (c.first) cudaFree(c.first);
+    if (c.second) cudaFree(c.second);
     if (c.tpieces) cudaFree(c.tpieces);
     if (c.heavy) cudaFree(c.heavy);
     if (c.pieces) cudaFree(c.pieces);

@@ -20,6 +20,12 @@ struct DeviceCsr {
     int64_t nonisolated = 0;
     int *heavy = nullptr;      // vertices of out-degree > HEAVY_DEGREE (any order)
     int32_t nheavy = 0;
+    // each row's first and second entries, -1 where the row is shorter (with
+    // hub-first rows, the first is the highest-degree neighbour): bottom-up's
+    // first probe, read coalesced
+    int *first = nullptr;      // n
+    int *second = nullptr;     // n
+    bool hub_rows = false;     // rows are hub-first (csr_hub_first ran)
     // multi-source pull pieces (built on demand by ms_prepare): every row of
     // degree > 2 * MS_PIECE contributes {vertex, j} for its j-th MS_PIECE edges
     int2 *pieces = nullptr;
@@ -29,6 +35,7 @@ struct DeviceCsr {
     // whose in-edges differ from their out-edges; rows unsorted
     int *trow = nullptr;       // n+1
     int *tcol = nullptr;       // m
+    int *tfirst = nullptr;     // n: the transpose's first entries (its rows are hub-first)
     int *theavy = nullptr;     // vertices of in-degree > HEAVY_DEGREE (built with the transpose)
     int32_t ntheavy = 0;
     // multi-source pull pieces over the transpose (ms_prepare, once trow exists)
@@ -57,8 +64,15 @@ int csr_check_symmetric(const DeviceCsr &c, cudaStream_t st, bool &sym, std::str
 // Move each row's highest-degree neighbour to the row's front.
 int csr_hub_first(DeviceCsr &c, cudaStream_t st, std::string &err);
 
-// Build c.trow / c.tcol (the in-edge CSR); a no-op once built.  Synchronises st.
+// Build c.trow / c.tcol (the in-edge CSR, rows hub-first) with c.tfirst and
+// c.theavy; a no-op once built.  Synchronises st.
 int csr_build_transpose(DeviceCsr &c, cudaStream_t st, std::string &err);
+
+// (Re)compute c.first / c.second from the rows as they are now.  Synchronises st.
+int csr_build_first(DeviceCsr &c, cudaStream_t st, std::string &err);
+
+// Device bytes held by the CSR and everything built on it.
+int64_t csr_device_bytes(const DeviceCsr &c);
 
 void csr_free(DeviceCsr &c);
 

@@ -318,9 +318,9 @@ extern "C" int gbfs_server_add_graph(gbfs_server *s, gbfs_graph *g, int32_t *gra
     // rows plus their heavy-row list) built here, inside the budget
     const bool want_t = !g->symmetric && graph_params(g).direction != GBFS_DIR_TOPDOWN;
     const bool has_t = want_t || g->csr.trow != nullptr;
-    const int64_t tbytes = has_t ? (int64_t)sizeof(int) * (2 * (int64_t)g->csr.n + 1 + g->csr.m) : 0;
-    const int64_t gbytes = (int64_t)sizeof(int) * ((int64_t)g->csr.n + 1 + g->csr.m) + 4 * (((int64_t)g->csr.n + 31) / 32) +
-                           tbytes + ms_prepare_bytes(g->csr, has_t);
+    const int64_t tbytes =  // trow, tcol, theavy, tfirst still to build
+        want_t && !g->csr.trow ? (int64_t)sizeof(int) * (3 * (int64_t)g->csr.n + 1 + g->csr.m) : 0;
+    const int64_t gbytes = csr_device_bytes(g->csr) + tbytes + ms_prepare_bytes(g->csr, has_t);
     const int64_t new_cap = std::max<int64_t>(s->n_cap, g->csr.n);
     const int64_t need = s->resident + gbytes + s->slots_total(new_cap);
     if (need > s->cfg.mem_budget_bytes) {

@@ -96,7 +96,9 @@ typedef struct gbfs_graph_info {
     int32_t max_degree;
     int64_t m;                  /* stored directed edges                     */
     int64_t nonisolated;        /* vertices with out-degree > 0              */
-    int64_t device_bytes;       /* CSR + per-graph search workspace          */
+    int64_t device_bytes;       /* CSR and what is built on it (first-entry
+                                   arrays, pull pieces, transpose) + per-graph
+                                   search workspace                          */
 } gbfs_graph_info;
 
 int gbfs_graph_get_info(const gbfs_graph *g, gbfs_graph_info *info);
@@ -107,7 +109,7 @@ int gbfs_graph_get_csr(const gbfs_graph *g, int32_t *row_offset,
 
 /* ---- traversal parameters (autotuned) --------------------------------- */
 /* Bottom-up steps probe in-edges: on a directed graph the first traversal
- * that may take one builds the transpose (4(2n+1) + 4m device bytes) and
+ * that may take one builds the transpose (4(3n+1) + 4m device bytes) and
  * keeps it with the graph; if that allocation fails the search is top-down. */
 #define GBFS_DIR_OPTIMIZING   0   /* Beamer top-down / bottom-up switching  */
 #define GBFS_DIR_TOPDOWN      1
