@@ -46,6 +46,7 @@ namespace {
 constexpr int SEG = 2048;    // frontier rows expanded edge-balanced per pass
 constexpr int ILP = 4;       // edges in flight per lane in top-down passes
 constexpr int PROBE = 8;     // neighbours probed per step in bottom-up
+constexpr unsigned long long BMTD_EDGES = 65536;  // top-down from the bitmap up to this many frontier edges
 
 struct BfsArgs {
     int n;
@@ -210,6 +211,95 @@ __device__ void bitmap_to_list(const unsigned *bm, bool complement, int n, int W
     }
 }
 
+// Top-down expansion of one row per lane (d = 0: none) as one concatenated
+// edge range over the warp, ILP edges per lane in flight; rows of
+// big_degree or more go to bigl (counted in *bigcnt) for a grid-wide pass.
+__device__ __forceinline__ void expand_lane_rows(int v, int b, int d, const BfsArgs &a, int nl, WarpQ &q,
+                                                 unsigned long long *cnt, int *qn, unsigned long long &my_deg,
+                                                 unsigned *bigcnt, unsigned lane)
+{
+    const bool isbig = d >= a.big_degree;
+    const unsigned bm = __ballot_sync(FULL, isbig);
+    if (bm) {
+        unsigned pos = 0;
+        const int leader = __ffs(bm) - 1;
+        if ((int)lane == leader) pos = atomicAdd(bigcnt, (unsigned)__popc(bm));
+        pos = __shfl_sync(FULL, pos, leader);
+        if (isbig) a.bigl[pos + __popc(bm & lanemask_lt())] = v;
+        if (isbig) d = 0;
+    }
+    const int incl = warp_incl_scan(d);
+    const int excl = incl - d;
+    const int T = __shfl_sync(FULL, incl, 31);
+    for (int e0 = 0; e0 < T; e0 += 32 * ILP) {
+        int w[ILP];
+#pragma unroll
+        for (int j = 0; j < ILP; j++) {
+            const int k = e0 + j * 32 + (int)lane;
+            const int kk = min(k, T - 1);
+            int lo = 0;
+#pragma unroll
+            for (int s = 16; s > 0; s >>= 1) {
+                const int c = lo + s;
+                if (__shfl_sync(FULL, excl, c) <= kk) lo = c;
+            }
+            const int ob = __shfl_sync(FULL, b, lo);
+            const int oe = __shfl_sync(FULL, excl, lo);
+            w[j] = k < T ? __ldg(a.col + ob + (kk - oe)) : -1;
+        }
+        claim_batch(w, a, nl, q, cnt, qn, my_deg);
+    }
+}
+
+// Top-down step over a frontier given as a bitmap (few edges, right after
+// bottom-up steps), with no bitmap -> queue pass: a warp takes cw words at a
+// time, deals their frontier vertices one per lane, and expands those rows
+// with expand_lane_rows.  cw aims a chunk at about 32 frontier vertices.
+__device__ __forceinline__ void bitmap_expand(const unsigned *fb, int W, long long nf, const BfsArgs &a, int nl,
+                                              WarpQ &q, unsigned long long *cnt, int *qn,
+                                              unsigned long long &my_deg, unsigned *bigcnt, long long gwarp,
+                                              long long nwarps, unsigned lane)
+{
+    const int cw = (int)min(32LL, max(1LL, (32LL * W) / max(1LL, nf)));
+    for (long long w0 = gwarp * cw; w0 < W; w0 += nwarps * cw) {
+        const long long wl = w0 + lane;
+        const unsigned bits = ((int)lane < cw && wl < W) ? __ldcg(fb + wl) : 0u;
+        const int c = __popc(bits);
+        const int incl = warp_incl_scan(c);
+        const int excl = incl - c;
+        const int U = __shfl_sync(FULL, incl, 31);
+        for (int r0 = 0; r0 < U; r0 += 32) {
+            const int slot = r0 + (int)lane;
+            const int jj = min(slot, U - 1);
+            int owner = 0;
+#pragma unroll
+            for (int s = 16; s > 0; s >>= 1) {
+                const int cand = owner + s;
+                if (__shfl_sync(FULL, excl, cand) <= jj) owner = cand;
+            }
+            unsigned um = __shfl_sync(FULL, bits, owner);
+            int k = jj - __shfl_sync(FULL, excl, owner);
+            int pos = 0;  // position of the k-th set bit of um
+#pragma unroll
+            for (int s = 16; s > 0; s >>= 1) {
+                const int lowc = __popc(um & ((1u << s) - 1u));
+                if (k >= lowc) {
+                    k -= lowc;
+                    um >>= s;
+                    pos += s;
+                }
+            }
+            int v = 0, b = 0, d = 0;
+            if (slot < U) {
+                v = (int)((w0 + owner) * 32 + pos);
+                b = __ldg(a.row + v);
+                d = __ldg(a.row + v + 1) - b;
+            }
+            expand_lane_rows(v, b, d, a, nl, q, cnt, qn, my_deg, bigcnt, lane);
+        }
+    }
+}
+
 // MINB (CTAs per SM the register budget is sized for) only shapes register
 // allocation; the launch decides the actual grid.
 template <int BLOCK, int MINB>
@@ -359,7 +449,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                 atomicOr(&fc[v >> 5], 1u << (v & 31));
             }
             if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
-        } else if (!bu && !td) {
+        }
+        // back to top-down with few frontier edges: expand the frontier
+        // straight from its bitmap (no bitmap -> queue pass and barrier)
+        const bool from_bitmap = !bu && !td && mf <= BMTD_EDGES;
+        if (!bu && !td && !from_bitmap) {
             // bitmap -> queue
             bitmap_to_list<BLOCK>(fc, false, n, W, qc, &ctrl->fill, s_warp, &s_base);
             if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
@@ -371,7 +465,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
             ++td_levels;
             if (gtid == 0) ctrl->fill = 0;
             unsigned long long my_deg = 0;
-            if (nf <= (unsigned long long)SEG) {
+            if (from_bitmap) {
+                bitmap_expand(fc, W, (long long)nf, a, nl, q, cnt_next, qn, my_deg, &ctrl->big[L % 3], gwarp, nwarps,
+                              lane);
+            } else if (nf <= (unsigned long long)SEG) {
                 // small frontier: every edge of it balanced over the whole grid
                 grid_expand_list<BLOCK>(qc, (int)nf, a, nl, q, cnt_next, qn, my_deg, s_pre, s_beg, s_warp);
             } else {
@@ -385,37 +482,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                         b = __ldg(a.row + v);
                         d = __ldg(a.row + v + 1) - b;
                     }
-                    const bool isbig = d >= a.big_degree;
-                    const unsigned bm = __ballot_sync(FULL, isbig);
-                    if (bm) {
-                        unsigned pos = 0;
-                        const int leader = __ffs(bm) - 1;
-                        if ((int)lane == leader) pos = atomicAdd(&ctrl->big[L % 3], (unsigned)__popc(bm));
-                        pos = __shfl_sync(FULL, pos, leader);
-                        if (isbig) a.bigl[pos + __popc(bm & lanemask_lt())] = v;
-                        if (isbig) d = 0;
-                    }
-                    const int incl = warp_incl_scan(d);
-                    const int excl = incl - d;
-                    const int T = __shfl_sync(FULL, incl, 31);
-                    for (int e0 = 0; e0 < T; e0 += 32 * ILP) {
-                        int w[ILP];
-#pragma unroll
-                        for (int j = 0; j < ILP; j++) {
-                            const int k = e0 + j * 32 + (int)lane;
-                            const int kk = min(k, T - 1);
-                            int lo = 0;
-#pragma unroll
-                            for (int s = 16; s > 0; s >>= 1) {
-                                const int c = lo + s;
-                                if (__shfl_sync(FULL, excl, c) <= kk) lo = c;
-                            }
-                            const int ob = __shfl_sync(FULL, b, lo);
-                            const int oe = __shfl_sync(FULL, excl, lo);
-                            w[j] = k < T ? __ldg(a.col + ob + (kk - oe)) : -1;
-                        }
-                        claim_batch(w, a, nl, q, cnt_next, qn, my_deg);
-                    }
+                    expand_lane_rows(v, b, d, a, nl, q, cnt_next, qn, my_deg, &ctrl->big[L % 3], lane);
                 }
             }
             block_flush(q, cnt_next, qn, s_wq, &s_base);
@@ -425,7 +492,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
             }
             if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
 
-            const int nb = nf > (unsigned long long)SEG ? (int)__ldcg(&ctrl->big[L % 3]) : 0;
+            const int nb = nf > (unsigned long long)SEG || from_bitmap ? (int)__ldcg(&ctrl->big[L % 3]) : 0;
             traced_big = nb > 0;
             if (nb > 0) {
                 my_deg = 0;

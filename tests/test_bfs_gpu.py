@@ -244,6 +244,33 @@ def test_reference_interface_mirror(gb, orc, tmp_path):
         assert b.exec_time > 0
 
 
+@pytest.mark.parametrize("flags_name", ["UNDIRECTED", "UNDIRECTED|HUB_FIRST", "DIRECTED"])
+def test_bottom_up_short_rows(gb, orc, flags_name):
+    """Bottom-up on rows of 0, 1, 2 and 3 entries (the first probe reads the
+    compact first / second entries, then the rest of the row)."""
+    flags = {"UNDIRECTED": gb.UNDIRECTED, "UNDIRECTED|HUB_FIRST": gb.UNDIRECTED | gb.HUB_FIRST,
+             "DIRECTED": gb.DEDUP | gb.DROP_SELF_LOOPS}[flags_name]
+    rng = np.random.default_rng(77)
+    cases = []
+    n = 41
+    cases.append((n, np.arange(n - 1), np.arange(1, n)))                        # a path (rows of 1-2)
+    cases.append((n, np.zeros(n - 1, np.int64), np.arange(1, n)))               # a star
+    tri = [(i, i + 1) for i in range(0, 30, 3)] + [(i, i + 2) for i in range(0, 30, 3)]
+    cases.append((n, np.array([a for a, _ in tri]), np.array([b for _, b in tri])))  # rows of 2-3, isolated tail
+    for _ in range(3):
+        m = int(rng.integers(40, 120))
+        cases.append((200, rng.integers(0, 200, m), rng.integers(0, 200, m)))
+    for nn, s, d in cases:
+        s = np.asarray(s, np.int32)
+        d = np.asarray(d, np.int32)
+        o = orc.csr_build(nn, s, d, flags & 7)
+        g = gb.Graph.from_edges(nn, s, d, flags)
+        for direction in (0, 2):
+            g.set_params(direction=direction)
+            for s0 in range(0, nn, 7):
+                assert np.array_equal(g.bfs(s0), orc.bfs_queue(o, s0)), (flags_name, direction, s0)
+
+
 def test_hub_first_layout(gb, orc):
     n = 1 << 16
     src, dst = gb.gen_rmat(16, 16, seed=21)
