@@ -78,9 +78,11 @@ struct BfsArgs {
 // Top-down claim of ILP neighbours per lane, all loads and atomics issued
 // before any result is used.  w[j] < 0 means "no edge".  A vertex is won by
 // the atomicOr that sets its visited bit; the winner writes its level,
-// adds its out-degree to my_deg and appends it to the warp queue.
+// adds its out-degree to my_deg, appends it to the warp queue and, with fnw
+// given, marks it in the next frontier's bitmap too.
 __device__ __forceinline__ void claim_batch(const int (&w)[ILP], const BfsArgs &a, int nl, WarpQ &q,
-                                            unsigned long long *cnt, int *qn, unsigned long long &my_deg)
+                                            unsigned long long *cnt, int *qn, unsigned long long &my_deg,
+                                            unsigned *fnw)
 {
     unsigned word[ILP];
 #pragma unroll
@@ -109,6 +111,11 @@ __device__ __forceinline__ void claim_batch(const int (&w)[ILP], const BfsArgs &
         my_deg += (unsigned long long)(d1[j] - d0[j]);
         wq_push(q, won[j], w[j], cnt, qn);
     }
+    if (fnw) {  // one branch, taken on whole levels or not at all
+#pragma unroll
+        for (int j = 0; j < ILP; j++)
+            if (won[j]) atomicOr(&fnw[w[j] >> 5], 1u << (w[j] & 31));
+    }
 }
 
 // Expand the rows of list[0, cnt) with the edges split evenly: each CTA
@@ -120,7 +127,7 @@ __device__ __forceinline__ void claim_batch(const int (&w)[ILP], const BfsArgs &
 template <int BLOCK>
 __device__ void grid_expand_list(const int *list, int cnt, const BfsArgs &a, int nl, WarpQ &q,
                                  unsigned long long *cnt_next, int *qn, unsigned long long &my_deg, int *s_pre,
-                                 int *s_beg, int *s_warp, bool heavy = false)
+                                 int *s_beg, int *s_warp, unsigned *fnw, bool heavy = false)
 {
     constexpr int PER = SEG / BLOCK;
     const int lane = (int)lane_id();
@@ -174,7 +181,7 @@ __device__ void grid_expand_list(const int *list, int cnt, const BfsArgs &a, int
                     w[j] = __ldg(a.col + s_beg[l] + (int)(e - s_pre[l]));
                 }
             }
-            claim_batch(w, a, nl, q, cnt_next, qn, my_deg);
+            claim_batch(w, a, nl, q, cnt_next, qn, my_deg, fnw);
         }
         __syncthreads();
     }
@@ -216,7 +223,7 @@ __device__ void bitmap_to_list(const unsigned *bm, bool complement, int n, int W
 // big_degree or more go to bigl (counted in *bigcnt) for a grid-wide pass.
 __device__ __forceinline__ void expand_lane_rows(int v, int b, int d, const BfsArgs &a, int nl, WarpQ &q,
                                                  unsigned long long *cnt, int *qn, unsigned long long &my_deg,
-                                                 unsigned *bigcnt, unsigned lane)
+                                                 unsigned *bigcnt, unsigned lane, unsigned *fnw)
 {
     const bool isbig = d >= a.big_degree;
     const unsigned bm = __ballot_sync(FULL, isbig);
@@ -247,7 +254,7 @@ __device__ __forceinline__ void expand_lane_rows(int v, int b, int d, const BfsA
             const int oe = __shfl_sync(FULL, excl, lo);
             w[j] = k < T ? __ldg(a.col + ob + (kk - oe)) : -1;
         }
-        claim_batch(w, a, nl, q, cnt, qn, my_deg);
+        claim_batch(w, a, nl, q, cnt, qn, my_deg, fnw);
     }
 }
 
@@ -258,7 +265,7 @@ __device__ __forceinline__ void expand_lane_rows(int v, int b, int d, const BfsA
 __device__ __forceinline__ void bitmap_expand(const unsigned *fb, int W, long long nf, const BfsArgs &a, int nl,
                                               WarpQ &q, unsigned long long *cnt, int *qn,
                                               unsigned long long &my_deg, unsigned *bigcnt, long long gwarp,
-                                              long long nwarps, unsigned lane)
+                                              long long nwarps, unsigned lane, unsigned *fnw)
 {
     const int cw = (int)min(32LL, max(1LL, (32LL * W) / max(1LL, nf)));
     for (long long w0 = gwarp * cw; w0 < W; w0 += nwarps * cw) {
@@ -295,7 +302,7 @@ __device__ __forceinline__ void bitmap_expand(const unsigned *fb, int W, long lo
                 b = __ldg(a.row + v);
                 d = __ldg(a.row + v + 1) - b;
             }
-            expand_lane_rows(v, b, d, a, nl, q, cnt, qn, my_deg, bigcnt, lane);
+            expand_lane_rows(v, b, d, a, nl, q, cnt, qn, my_deg, bigcnt, lane, fnw);
         }
     }
 }
@@ -378,6 +385,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
     unsigned long long prev_nf = 0, reached = 0, edges_c = 0, roots = 0;
     int L = 0, td_levels = 0, bu_levels = 0;
     bool td = true;
+    bool fn_set = false;  // the last top-down step marked its finds in fn
+    unsigned long long prev_mf = 0;  // the last level's frontier edges
     if (a.resume) {
         const BfsResume r = ctrl->rs;
         m_u = r.m_u;
@@ -441,9 +450,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
             ctrl->big[(L + 1) % 3] = 0;
         }
 
-        if (bu && td) {
+        if (bu && td && !fn_set) {
             // queue -> bitmap (fc is zero: fb[L%3] was cleared two levels
-            // ago and top-down steps do not write it)
+            // ago and top-down steps that did not mark it do not write it)
             for (long long i = gtid; i < (long long)nf; i += gthreads) {
                 const int v = __ldcg(qc + i);
                 atomicOr(&fc[v >> 5], 1u << (v & 31));
@@ -465,12 +474,19 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
             ++td_levels;
             if (gtid == 0) ctrl->fill = 0;
             unsigned long long my_deg = 0;
+            // direction-optimising, with the next level likely bottom-up
+            // (this frontier's edges times their growth from the last level
+            // past the switching rule): also mark the next frontier in its
+            // bitmap, so the switch needs no queue -> bitmap pass
+            const float growth = fmaxf(1.f, (float)mf / (float)(prev_mf ? prev_mf : 1ull));
+            const bool likely_bu = (float)mf * growth * (float)a.alpha > (float)m_u;
+            unsigned *fnw = a.direction == GBFS_DIR_OPTIMIZING && a.brow && likely_bu ? fn : nullptr;
             if (from_bitmap) {
                 bitmap_expand(fc, W, (long long)nf, a, nl, q, cnt_next, qn, my_deg, &ctrl->big[L % 3], gwarp, nwarps,
-                              lane);
+                              lane, fnw);
             } else if (nf <= (unsigned long long)SEG) {
                 // small frontier: every edge of it balanced over the whole grid
-                grid_expand_list<BLOCK>(qc, (int)nf, a, nl, q, cnt_next, qn, my_deg, s_pre, s_beg, s_warp);
+                grid_expand_list<BLOCK>(qc, (int)nf, a, nl, q, cnt_next, qn, my_deg, s_pre, s_beg, s_warp, fnw);
             } else {
                 // large frontier: 32 rows per warp as one concatenated edge
                 // range, rows of degree >= big_degree deferred to a grid pass
@@ -482,7 +498,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                         b = __ldg(a.row + v);
                         d = __ldg(a.row + v + 1) - b;
                     }
-                    expand_lane_rows(v, b, d, a, nl, q, cnt_next, qn, my_deg, &ctrl->big[L % 3], lane);
+                    expand_lane_rows(v, b, d, a, nl, q, cnt_next, qn, my_deg, &ctrl->big[L % 3], lane, fnw);
                 }
             }
             block_flush(q, cnt_next, qn, s_wq, &s_base);
@@ -496,13 +512,15 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
             traced_big = nb > 0;
             if (nb > 0) {
                 my_deg = 0;
-                grid_expand_list<BLOCK>(a.bigl, nb, a, nl, q, cnt_next, qn, my_deg, s_pre, s_beg, s_warp, true);
+                grid_expand_list<BLOCK>(a.bigl, nb, a, nl, q, cnt_next, qn, my_deg, s_pre, s_beg, s_warp, fnw, true);
                 block_flush(q, cnt_next, qn, s_wq, &s_base);
                 const unsigned long long bd = block_reduce_sum(my_deg, s_red);
                 if (threadIdx.x == 0 && bd) atomicAdd(deg_next, bd);
                 if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
             }
+            fn_set = fnw != nullptr;
         } else {
+            fn_set = false;
             ++bu_levels;
             unsigned long long my_cnt = 0, my_deg = 0;
             // A warp takes chunks of cw bitmap words; a chunk's unvisited
@@ -637,6 +655,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
             if (threadIdx.x == 0 && bd) atomicAdd(deg_next, bd);
             if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
         }
+        prev_mf = mf;
         if (gtid == 0) {
             LevelTrace t;
             t.level = L;
