@@ -46,6 +46,7 @@ namespace {
 constexpr int SEG = 2048;    // frontier rows expanded edge-balanced per pass
 constexpr int ILP = 4;       // edges in flight per lane in top-down passes
 constexpr int PROBE = 8;     // neighbours probed per step in bottom-up
+constexpr int BU_DEF = 192;  // deferred bottom-up rows per warp: under 64 left plus a 128-vertex round (<= QCAP)
 constexpr unsigned long long BMTD_EDGES = 65536;  // top-down from the bitmap up to this many frontier edges
 
 struct BfsArgs {
@@ -321,6 +322,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
     int *s_q = smem;                           // NW * QCAP warp queues
     int *s_pre = s_q + NW * QCAP;              // SEG degree prefix
     int *s_beg = s_pre + SEG;                  // SEG row begins
+    int2 *s_def = (int2 *)(s_beg + SEG);       // NW * BU_DEF deferred bottom-up rows
 
     const int n = a.n;
     const int W = (n + 31) >> 5;
@@ -523,98 +525,49 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
             fn_set = false;
             ++bu_levels;
             unsigned long long my_cnt = 0, my_deg = 0;
-            // A warp takes chunks of cw bitmap words; a chunk's unvisited
-            // vertices are dealt two per lane (64 per round) and probed in
-            // interleaved steps; the warp owns the chunk's words, so fn /
-            // visited words are written without atomics.  cw aims a chunk at
-            // about 120 unvisited vertices (two nearly full rounds: about 64
-            // left half the chunks with a second round of a few vertices)
-            // when that still gives every warp two chunks, else at about 56
-            // (one round; small graphs and dense levels keep every warp
-            // busy), up to 32 words on sparse levels.
+            // A warp takes chunks of cw bitmap words and probes the chunk's
+            // unvisited vertices (the two branches below).  cw aims a chunk
+            // at about 120 unvisited vertices when that still gives every
+            // warp two chunks, else at about 56 (small graphs and dense
+            // levels keep every warp busy), up to 32 words on sparse levels.
             long long unv_est = (long long)a.n_active - (long long)reached;
             if (unv_est < 1) unv_est = 1;
             long long cwl = (120LL * n) / (32LL * unv_est);
             if (cwl < 1 || (long long)W < 2 * nwarps * cwl) cwl = (56LL * n) / (32LL * unv_est);
             const int cw = (int)min(32LL, max(1LL, cwl));
             unsigned *my_found = (unsigned *)(s_beg) + (threadIdx.x >> 5) * 32;  // s_beg is free here
+            int *def_v = q.buf;  // the warp's queue is idle in bottom-up steps
+            int2 *def_b = s_def + (threadIdx.x >> 5) * BU_DEF;
             my_found[lane] = 0;
             __syncwarp();
-            for (long long w0 = gwarp * cw; w0 < W; w0 += nwarps * cw) {
-                const long long wl = w0 + lane;
-                unsigned vis = FULL, valid = 0;
-                if ((int)lane < cw && wl < W) {
-                    vis = __ldcg(a.visited + wl);
-                    valid = (wl == W - 1 && (n & 31)) ? ((1u << (n & 31)) - 1u) : FULL;
-                }
-                const unsigned unv = ~vis & valid;
-                const int c = __popc(unv);
-                const int incl = warp_incl_scan(c);
-                const int excl = incl - c;
-                const int U = __shfl_sync(FULL, incl, 31);
-                for (int r0 = 0; r0 < U; r0 += 64) {
-                    int vv[2];
-#pragma unroll
-                    for (int h = 0; h < 2; h++) {
-                        const int slot = r0 + (int)lane + 32 * h;
-                        const int jj = min(slot, U - 1);
-                        int owner = 0;
-#pragma unroll
-                        for (int s = 16; s > 0; s >>= 1) {
-                            const int cand = owner + s;
-                            if (__shfl_sync(FULL, excl, cand) <= jj) owner = cand;
-                        }
-                        unsigned um = __shfl_sync(FULL, unv, owner);
-                        int k = jj - __shfl_sync(FULL, excl, owner);
-                        int pos = 0;  // position of the k-th set bit of um
-#pragma unroll
-                        for (int s = 16; s > 0; s >>= 1) {
-                            const int lowc = __popc(um & ((1u << s) - 1u));
-                            if (k >= lowc) {
-                                k -= lowc;
-                                um >>= s;
-                                pos += s;
-                            }
-                        }
-                        vv[h] = slot < U ? (int)((w0 + owner) * 32 + pos) : -1;
-                    }
-                    const int va = vv[0], vb = vv[1];
-                    const bool two = a.bsecond != nullptr;
-                    int ia = 0, ea = 0, ib = 0, eb = 0, pa = -1, pb = -1, qa = -1, qb = -1;
-                    if (va >= 0) {
-                        pa = __ldg(a.bfirst + va);
-                        if (two) qa = __ldg(a.bsecond + va);
-                        ia = __ldg(a.brow + va);
-                        ea = __ldg(a.brow + va + 1);
-                    }
-                    if (vb >= 0) {
-                        pb = __ldg(a.bfirst + vb);
-                        if (two) qb = __ldg(a.bsecond + vb);
-                        ib = __ldg(a.brow + vb);
-                        eb = __ldg(a.brow + vb + 1);
-                    }
-                    const int da = ea - ia, db = eb - ib;
-                    // First step: each row's first entry (hub-first rows: the
-                    // highest-degree neighbour, where most vertices find their
-                    // parent), with its second on other rows, from the compact
-                    // first-entry arrays, read coalesced with the row offsets
-                    // instead of one col_idx sector per row.  Later steps walk
-                    // the rest of the row, PROBE wide.
-                    unsigned ha = 0, hb = 0;  // the entries' bits loaded at once
-                    if (pa >= 0) ha |= __ldcg(fc + (pa >> 5)) >> (pa & 31);
-                    if (qa >= 0) ha |= __ldcg(fc + (qa >> 5)) >> (qa & 31);
-                    if (pb >= 0) hb |= __ldcg(fc + (pb >> 5)) >> (pb & 31);
-                    if (qb >= 0) hb |= __ldcg(fc + (qb >> 5)) >> (qb & 31);
-                    bool fa = ha & 1u, fb = hb & 1u;
-                    ia += two ? 2 : 1;
-                    ib += two ? 2 : 1;
-                    const int width = PROBE;
+            if (a.bsecond == nullptr) {
+                // Hub-first rows (other rows probe in place, below).  Phase A,
+                // 128 vertices a round (four per lane): each row's first
+                // entry, its highest-degree neighbour, from the compact
+                // first-entry array, read coalesced with the row offsets;
+                // most vertices settle here.
+                // Rows left with entries to probe go on the warp's deferred
+                // stack (shared memory); phase B walks them 64 at a time, two
+                // per lane, PROBE entries per step.  The stack empties after
+                // the warp's last chunk is done; it carries over chunks, so its
+                // finds and the chunk's own go to fn / visited by atomicOr
+                // (the words are this warp's alone in this step).
+                constexpr int skip = 1;  // entries the first probe covers
+                int dn = 0;  // deferred rows on the stack
+                auto phase_b = [&](int cntb) {
+                    const int base = dn - cntb;
+                    const int ka = base + (int)lane, kb = base + 32 + (int)lane;
+                    int va = -1, vb = -1, ia = 0, ea = 0, ib = 0, eb = 0;
+                    if (ka < dn) { va = def_v[ka]; ia = def_b[ka].x; ea = def_b[ka].y; }
+                    if (kb < dn) { vb = def_v[kb]; ib = def_b[kb].x; eb = def_b[kb].y; }
+                    const int da = ea - ia + skip, db = eb - ib + skip;
+                    bool fa = false, fb = false;
                     while ((ia < ea && !fa) || (ib < eb && !fb)) {
                         int ua[PROBE], ub[PROBE];
 #pragma unroll
                         for (int t = 0; t < PROBE; t++) {
-                            ua[t] = (t < width && !fa && ia + t < ea) ? __ldg(a.bcol + ia + t) : -1;
-                            ub[t] = (t < width && !fb && ib + t < eb) ? __ldg(a.bcol + ib + t) : -1;
+                            ua[t] = (!fa && ia + t < ea) ? __ldg(a.bcol + ia + t) : -1;
+                            ub[t] = (!fb && ib + t < eb) ? __ldg(a.bcol + ib + t) : -1;
                         }
                         unsigned ga = 0, gb = 0;
 #pragma unroll
@@ -622,32 +575,233 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                             if (ua[t] >= 0) ga |= __ldcg(fc + (ua[t] >> 5)) >> (ua[t] & 31);
                             if (ub[t] >= 0) gb |= __ldcg(fc + (ub[t] >> 5)) >> (ub[t] & 31);
                         }
-                        if (!fa && ia < ea) { if (ga & 1u) fa = true; else ia += width; }
-                        if (!fb && ib < eb) { if (gb & 1u) fb = true; else ib += width; }
+                        if (!fa && ia < ea) { if (ga & 1u) fa = true; else ia += PROBE; }
+                        if (!fb && ib < eb) { if (gb & 1u) fb = true; else ib += PROBE; }
                     }
-                    // the next frontier's out-edges (for the direction rule): the
-                    // probed in-degree when in-edges are the out-edges
                     if (fa) {
                         a.level[va] = nl;
-                        atomicOr(&my_found[(va >> 5) - w0], 1u << (va & 31));
+                        atomicOr(fn + (va >> 5), 1u << (va & 31));
+                        atomicOr(a.visited + (va >> 5), 1u << (va & 31));
                         ++my_cnt;
                         my_deg += (unsigned long long)(a.brow == a.row ? da : __ldg(a.row + va + 1) - __ldg(a.row + va));
                     }
                     if (fb) {
                         a.level[vb] = nl;
-                        atomicOr(&my_found[(vb >> 5) - w0], 1u << (vb & 31));
+                        atomicOr(fn + (vb >> 5), 1u << (vb & 31));
+                        atomicOr(a.visited + (vb >> 5), 1u << (vb & 31));
                         ++my_cnt;
                         my_deg += (unsigned long long)(a.brow == a.row ? db : __ldg(a.row + vb + 1) - __ldg(a.row + vb));
                     }
+                    __syncwarp();
+                    dn = base;
+                };
+                for (long long w0 = gwarp * cw; w0 < W; w0 += nwarps * cw) {
+                    const long long wl = w0 + lane;
+                    unsigned vis = FULL, valid = 0;
+                    if ((int)lane < cw && wl < W) {
+                        vis = __ldcg(a.visited + wl);
+                        valid = (wl == W - 1 && (n & 31)) ? ((1u << (n & 31)) - 1u) : FULL;
+                    }
+                    const unsigned unv = ~vis & valid;
+                    const int c = __popc(unv);
+                    const int incl = warp_incl_scan(c);
+                    const int excl = incl - c;
+                    const int U = __shfl_sync(FULL, incl, 31);
+                    for (int r0 = 0; r0 < U; r0 += 128) {
+                        int vv[4];
+                        const int hn = U - r0 > 64 ? 4 : 2;  // a round's upper half only when it has vertices
+#pragma unroll
+                        for (int h = 0; h < 4; h++) {
+                            vv[h] = -1;
+                            if (h >= hn) continue;
+                            const int slot = r0 + (int)lane + 32 * h;
+                            const int jj = min(slot, U - 1);
+                            int owner = 0;
+#pragma unroll
+                            for (int s = 16; s > 0; s >>= 1) {
+                                const int cand = owner + s;
+                                if (__shfl_sync(FULL, excl, cand) <= jj) owner = cand;
+                            }
+                            unsigned um = __shfl_sync(FULL, unv, owner);
+                            int k = jj - __shfl_sync(FULL, excl, owner);
+                            int pos = 0;  // position of the k-th set bit of um
+#pragma unroll
+                            for (int s = 16; s > 0; s >>= 1) {
+                                const int lowc = __popc(um & ((1u << s) - 1u));
+                                if (k >= lowc) {
+                                    k -= lowc;
+                                    um >>= s;
+                                    pos += s;
+                                }
+                            }
+                            vv[h] = slot < U ? (int)((w0 + owner) * 32 + pos) : -1;
+                        }
+                        int pf[4], rb[4], re[4];
+#pragma unroll
+                        for (int h = 0; h < 4; h++) {
+                            pf[h] = -1;
+                            rb[h] = re[h] = 0;
+                            if (vv[h] >= 0) {
+                                pf[h] = __ldg(a.bfirst + vv[h]);
+                                rb[h] = __ldg(a.brow + vv[h]);
+                                re[h] = __ldg(a.brow + vv[h] + 1);
+                            }
+                        }
+                        unsigned hit[4];
+#pragma unroll
+                        for (int h = 0; h < 4; h++) {
+                            hit[h] = 0;
+                            if (pf[h] >= 0) hit[h] |= __ldcg(fc + (pf[h] >> 5)) >> (pf[h] & 31);
+                        }
+#pragma unroll
+                        for (int h = 0; h < 4; h++) {
+                            const int v = vv[h];
+                            const bool f = hit[h] & 1u;
+                            if (f) {
+                                a.level[v] = nl;
+                                atomicOr(&my_found[(v >> 5) - w0], 1u << (v & 31));
+                                ++my_cnt;
+                                my_deg += (unsigned long long)(a.brow == a.row ? re[h] - rb[h]
+                                                                               : __ldg(a.row + v + 1) - __ldg(a.row + v));
+                            }
+                            const bool defer = v >= 0 && !f && rb[h] + skip < re[h];
+                            const unsigned dm = __ballot_sync(FULL, defer);
+                            if (defer) {
+                                const int slotd = dn + __popc(dm & lanemask_lt());
+                                def_v[slotd] = v;
+                                def_b[slotd] = make_int2(rb[h] + skip, re[h]);
+                            }
+                            dn += __popc(dm);
+                        }
+                        __syncwarp();
+                        while (dn >= 64) phase_b(64);
+                    }
+                    __syncwarp();
+                    if ((int)lane < cw && wl < W) {
+                        const unsigned fw = my_found[lane];
+                        if (fw) {
+                            atomicOr(fn + wl, fw);
+                            atomicOr(a.visited + wl, fw);
+                        }
+                        my_found[lane] = 0;
+                    }
+                    __syncwarp();
                 }
-                __syncwarp();
-                if ((int)lane < cw && wl < W) {
-                    const unsigned fw = my_found[lane];
-                    fn[wl] = fw;
-                    if (fw) a.visited[wl] = vis | fw;
-                    my_found[lane] = 0;
+                while (dn > 0) phase_b(min(64, dn));
+            } else {
+                // Rows that are not hub-first: two vertices per lane (64 per
+                // round), each probed in place until it settles; the warp
+                // owns the chunk's words, so fn / visited words are written
+                // without atomics.
+                for (long long w0 = gwarp * cw; w0 < W; w0 += nwarps * cw) {
+                    const long long wl = w0 + lane;
+                    unsigned vis = FULL, valid = 0;
+                    if ((int)lane < cw && wl < W) {
+                        vis = __ldcg(a.visited + wl);
+                        valid = (wl == W - 1 && (n & 31)) ? ((1u << (n & 31)) - 1u) : FULL;
+                    }
+                    const unsigned unv = ~vis & valid;
+                    const int c = __popc(unv);
+                    const int incl = warp_incl_scan(c);
+                    const int excl = incl - c;
+                    const int U = __shfl_sync(FULL, incl, 31);
+                    for (int r0 = 0; r0 < U; r0 += 64) {
+                        int vv[2];
+#pragma unroll
+                        for (int h = 0; h < 2; h++) {
+                            const int slot = r0 + (int)lane + 32 * h;
+                            const int jj = min(slot, U - 1);
+                            int owner = 0;
+#pragma unroll
+                            for (int s = 16; s > 0; s >>= 1) {
+                                const int cand = owner + s;
+                                if (__shfl_sync(FULL, excl, cand) <= jj) owner = cand;
+                            }
+                            unsigned um = __shfl_sync(FULL, unv, owner);
+                            int k = jj - __shfl_sync(FULL, excl, owner);
+                            int pos = 0;  // position of the k-th set bit of um
+#pragma unroll
+                            for (int s = 16; s > 0; s >>= 1) {
+                                const int lowc = __popc(um & ((1u << s) - 1u));
+                                if (k >= lowc) {
+                                    k -= lowc;
+                                    um >>= s;
+                                    pos += s;
+                                }
+                            }
+                            vv[h] = slot < U ? (int)((w0 + owner) * 32 + pos) : -1;
+                        }
+                        const int va = vv[0], vb = vv[1];
+                        const bool two = a.bsecond != nullptr;
+                        int ia = 0, ea = 0, ib = 0, eb = 0, pa = -1, pb = -1, qa = -1, qb = -1;
+                        if (va >= 0) {
+                            pa = __ldg(a.bfirst + va);
+                            if (two) qa = __ldg(a.bsecond + va);
+                            ia = __ldg(a.brow + va);
+                            ea = __ldg(a.brow + va + 1);
+                        }
+                        if (vb >= 0) {
+                            pb = __ldg(a.bfirst + vb);
+                            if (two) qb = __ldg(a.bsecond + vb);
+                            ib = __ldg(a.brow + vb);
+                            eb = __ldg(a.brow + vb + 1);
+                        }
+                        const int da = ea - ia, db = eb - ib;
+                        // First step: each row's first entry (hub-first rows: the
+                        // highest-degree neighbour, where most vertices find their
+                        // parent), with its second on other rows, from the compact
+                        // first-entry arrays, read coalesced with the row offsets
+                        // instead of one col_idx sector per row.  Later steps walk
+                        // the rest of the row, PROBE wide.
+                        unsigned ha = 0, hb = 0;  // the entries' bits loaded at once
+                        if (pa >= 0) ha |= __ldcg(fc + (pa >> 5)) >> (pa & 31);
+                        if (qa >= 0) ha |= __ldcg(fc + (qa >> 5)) >> (qa & 31);
+                        if (pb >= 0) hb |= __ldcg(fc + (pb >> 5)) >> (pb & 31);
+                        if (qb >= 0) hb |= __ldcg(fc + (qb >> 5)) >> (qb & 31);
+                        bool fa = ha & 1u, fb = hb & 1u;
+                        ia += two ? 2 : 1;
+                        ib += two ? 2 : 1;
+                        const int width = PROBE;
+                        while ((ia < ea && !fa) || (ib < eb && !fb)) {
+                            int ua[PROBE], ub[PROBE];
+#pragma unroll
+                            for (int t = 0; t < PROBE; t++) {
+                                ua[t] = (t < width && !fa && ia + t < ea) ? __ldg(a.bcol + ia + t) : -1;
+                                ub[t] = (t < width && !fb && ib + t < eb) ? __ldg(a.bcol + ib + t) : -1;
+                            }
+                            unsigned ga = 0, gb = 0;
+#pragma unroll
+                            for (int t = 0; t < PROBE; t++) {
+                                if (ua[t] >= 0) ga |= __ldcg(fc + (ua[t] >> 5)) >> (ua[t] & 31);
+                                if (ub[t] >= 0) gb |= __ldcg(fc + (ub[t] >> 5)) >> (ub[t] & 31);
+                            }
+                            if (!fa && ia < ea) { if (ga & 1u) fa = true; else ia += width; }
+                            if (!fb && ib < eb) { if (gb & 1u) fb = true; else ib += width; }
+                        }
+                        // the next frontier's out-edges (for the direction rule): the
+                        // probed in-degree when in-edges are the out-edges
+                        if (fa) {
+                            a.level[va] = nl;
+                            atomicOr(&my_found[(va >> 5) - w0], 1u << (va & 31));
+                            ++my_cnt;
+                            my_deg += (unsigned long long)(a.brow == a.row ? da : __ldg(a.row + va + 1) - __ldg(a.row + va));
+                        }
+                        if (fb) {
+                            a.level[vb] = nl;
+                            atomicOr(&my_found[(vb >> 5) - w0], 1u << (vb & 31));
+                            ++my_cnt;
+                            my_deg += (unsigned long long)(a.brow == a.row ? db : __ldg(a.row + vb + 1) - __ldg(a.row + vb));
+                        }
+                    }
+                    __syncwarp();
+                    if ((int)lane < cw && wl < W) {
+                        const unsigned fw = my_found[lane];
+                        fn[wl] = fw;
+                        if (fw) a.visited[wl] = vis | fw;
+                        my_found[lane] = 0;
+                    }
+                    __syncwarp();
                 }
-                __syncwarp();
             }
             const unsigned long long bc = block_reduce_sum(my_cnt, s_red);
             if (threadIdx.x == 0 && bc) atomicAdd(cnt_next, bc);
@@ -693,7 +847,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
 template <int BLOCK>
 size_t bfs_smem_bytes()
 {
-    return sizeof(int) * ((size_t)(BLOCK / 32) * QCAP + 2 * (size_t)SEG);
+    return sizeof(int) * ((size_t)(BLOCK / 32) * QCAP + 2 * (size_t)SEG) + sizeof(int2) * (size_t)(BLOCK / 32) * BU_DEF;
 }
 
 template <int BLOCK, int MINB>
