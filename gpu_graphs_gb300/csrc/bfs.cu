@@ -9,27 +9,31 @@
 // Here one cooperative launch runs the whole traversal.  Levels are
 // separated by a bounded grid barrier and every CTA takes the same
 // direction decision from the same counters:
-//   top-down step   frontier queue -> next queue.  Each warp takes 32
-//                   frontier vertices; their rows (below big_degree) are
-//                   walked as one concatenated edge range (shuffle binary
-//                   search per edge, coalesced col_idx reads); rows of
-//                   degree >= big_degree are deferred and then split into
-//                   512-edge chunks over every warp of the grid, read with
-//                   16-byte vector loads.  A vertex is claimed with an
-//                   atomicOr on the visited bitmap (after a plain-load
-//                   filter), its level written once, and it is appended
-//                   through a per-warp shared-memory queue (one global
-//                   atomic per flush instead of one per edge).
-//   bottom-up step  every unvisited vertex scans its row for a parent in
-//                   the frontier bitmap, 4 probes in flight per lane,
-//                   stopping at the first hit; each warp owns whole bitmap
-//                   words, so visited / next-frontier words are written
-//                   without atomics.
+//   top-down step   frontier queue -> next queue.  Small frontiers: every
+//                   edge balanced over the whole grid (degree prefix in
+//                   shared memory).  Large ones: each warp takes 32
+//                   frontier vertices and walks their rows (below
+//                   big_degree) as one concatenated edge range; rows of
+//                   degree >= big_degree are deferred to a grid-wide pass.
+//                   A vertex is claimed with an atomicOr on the visited
+//                   bitmap (after a plain-load filter), its level written
+//                   once, and it is appended through a per-warp
+//                   shared-memory queue (one global atomic per flush).
+//   bottom-up step  every unvisited vertex looks for a parent in the
+//                   frontier bitmap, stopping at the first hit.  The first
+//                   probe reads the row's first entry from a compact array
+//                   (coalesced, beside the row offsets); on hub-first rows
+//                   four vertices per lane take it and the rows left over
+//                   are walked from a per-warp stack, on other rows two per
+//                   lane probe in place.
 //   switching       Beamer's rule: top-down -> bottom-up when the frontier's
 //                   out-edges exceed (unexplored edges)/alpha, back when the
 //                   frontier has fewer than (non-isolated vertices)/beta
-//                   vertices and is shrinking.  A queue <-> bitmap
-//                   conversion phase runs at each switch.
+//                   vertices and is shrinking.  A top-down step likely to
+//                   hand over marks its finds in the next frontier bitmap;
+//                   a small frontier handed back to top-down is read from
+//                   its bitmap directly; otherwise a queue <-> bitmap
+//                   conversion phase runs at the switch.
 // Bottom-up probes in-edges: the graph itself when symmetric, else its
 // transpose (built on demand); without either, every level is top-down.
 #include <algorithm>
