@@ -271,6 +271,56 @@ def test_bottom_up_short_rows(gb, orc, flags_name):
                 assert np.array_equal(g.bfs(s0), orc.bfs_queue(o, s0)), (flags_name, direction, s0)
 
 
+@pytest.mark.parametrize("seed", range(6))
+def test_random_graphs_all_paths(gb, orc, seed):
+    """Randomised parity sweep over graph shapes (power-law with assorted
+    skew, uniform, stars and chains glued together), row layouts (sorted,
+    hub-first), directed or symmetrised storage, the three directions and
+    small/large deferral thresholds: every level array equals the oracle's."""
+    rng = np.random.default_rng(1000 + seed)
+    for case in range(5):
+        kind = rng.integers(4)
+        if kind == 0:
+            scale = int(rng.integers(8, 15))
+            a_ = float(rng.uniform(0.45, 0.7))
+            b_ = c_ = (1 - a_) * 0.4
+            src, dst = gb.gen_rmat(scale, int(rng.integers(2, 20)), a_, b_, c_, seed=int(rng.integers(1 << 30)))
+            n = 1 << scale
+        elif kind == 1:
+            n = int(rng.integers(100, 50000))
+            src, dst = gb.gen_er(n, int(n * rng.uniform(0.5, 12)), int(rng.integers(1 << 30)))
+        elif kind == 2:  # a few stars joined by a chain, plus noise
+            n = int(rng.integers(2000, 30000))
+            hubs = rng.choice(n, 4, replace=False)
+            leaves = [rng.choice(n, int(rng.integers(50, n // 2)), replace=False) for _ in hubs]
+            src = np.concatenate([np.full(len(l), h) for h, l in zip(hubs, leaves)] + [hubs[:-1]])
+            dst = np.concatenate(leaves + [hubs[1:]])
+            noise = rng.integers(0, n, (2, n // 10))
+            src, dst = np.concatenate([src, noise[0]]), np.concatenate([dst, noise[1]])
+        else:  # long chains with shortcuts (many small levels)
+            n = int(rng.integers(1000, 20000))
+            perm = rng.permutation(n)
+            src, dst = perm[:-1], perm[1:]
+            extra = rng.integers(0, n, (2, n // 50))
+            src, dst = np.concatenate([src, extra[0]]), np.concatenate([dst, extra[1]])
+        src = np.asarray(src, np.int32)
+        dst = np.asarray(dst, np.int32)
+        base = [gb.UNDIRECTED, gb.DEDUP | gb.DROP_SELF_LOOPS, 0][int(rng.integers(3))]
+        flags = base | (gb.HUB_FIRST if rng.random() < 0.5 else 0)
+        o = orc.csr_build(n, src, dst, base & 7)
+        g = gb.Graph.from_edges(n, src, dst, flags)
+        deg = np.diff(o.row_offset)
+        cand = np.flatnonzero(deg > 0)
+        sources = [int(x) for x in rng.choice(cand if len(cand) else np.arange(n), 3)]
+        for direction in (0, 1, 2):
+            g.set_params(direction=direction, big_degree=int(rng.choice([32, 256, 4096])))
+            for s0 in sources:
+                assert np.array_equal(g.bfs(s0), orc.bfs_queue(o, s0)), (seed, case, kind, flags, direction, s0)
+        got = g.bfs_multi(sources)  # the 64-lane kernel on the same graph (last direction set)
+        for i, s0 in enumerate(sources):
+            assert np.array_equal(got[i], orc.bfs_queue(o, s0)), (seed, case, "multi", s0)
+
+
 def test_hub_first_layout(gb, orc):
     n = 1 << 16
     src, dst = gb.gen_rmat(16, 16, seed=21)
