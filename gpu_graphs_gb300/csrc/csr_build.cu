@@ -876,7 +876,7 @@ int csr_build_from_edges(int32_t n, int64_t m, const int *d_src, const int *d_ds
                          cudaStream_t st, DeviceCsr &out, std::string &err)
 {
     int rc = GBFS_OK;
-    const bool sym = flags & GBFS_SYMMETRIZE, dedup = flags & GBFS_DEDUP;
+    const bool dedup = flags & GBFS_DEDUP;
     int *deg = nullptr, *cursor = nullptr, *tmp = nullptr, *tmp2 = nullptr, *ucnt = nullptr;
     int *med = nullptr, *large = nullptr, *row2 = nullptr, *w4 = nullptr, *w16 = nullptr;
     unsigned *lcnt = nullptr;
