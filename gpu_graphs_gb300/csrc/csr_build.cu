@@ -832,7 +832,8 @@ int csr_build_first(DeviceCsr &c, cudaStream_t st, std::string &err)
 {
     int rc = GBFS_OK;
     if (!c.first) CK(cudaMalloc(&c.first, sizeof(int) * (size_t)std::max(1, c.n)));
-    if (!c.second) CK(cudaMalloc(&c.second, sizeof(int) * (size_t)std::max(1, c.n)));
+    // hub-first rows are probed at their first entry alone: no second array
+    if (!c.hub_rows && !c.second) CK(cudaMalloc(&c.second, sizeof(int) * (size_t)std::max(1, c.n)));
     if (c.n > 0) {
         k_first<<<grid_for(c.n, 256), 256, 0, st>>>(c.row, c.col, c.n, c.first, c.second);
         CK(cudaGetLastError());

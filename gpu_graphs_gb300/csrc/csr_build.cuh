@@ -24,7 +24,7 @@ struct DeviceCsr {
     // hub-first rows, the first is the highest-degree neighbour): bottom-up's
     // first probe, read coalesced
     int *first = nullptr;      // n
-    int *second = nullptr;     // n
+    int *second = nullptr;     // n; not allocated for hub-first rows (probed at the first entry alone)
     bool hub_rows = false;     // rows are hub-first (csr_hub_first ran)
     // multi-source pull pieces (built on demand by ms_prepare): every row of
     // degree > 2 * MS_PIECE contributes {vertex, j} for its j-th MS_PIECE edges
