@@ -231,6 +231,23 @@ def cpu_bfs_sample(n: int, row: np.ndarray, col: np.ndarray, sources, threads: i
     return wall, edges, levels
 
 
+def host_cpu() -> str:
+    """The host CPU's model name and logical core count (reported beside every
+    CPU figure)."""
+    name = ""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                key = ln.split(":")[0].strip().lower()
+                if key in ("model name", "cpu model", "hardware") and not name:
+                    name = ln.split(":", 1)[1].strip()
+                if key == "cpu part" and not name:  # Arm cores list a part number only
+                    name = "Arm part " + ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return f"{name or 'unknown'}, {os.cpu_count()} logical cores"
+
+
 def cpu_parallel_queries(tasks, threads: int = 0) -> dict:
     """Embarrassingly parallel CPU throughput: the oracle's queue BFS (the
     reference's CPU algorithm), one query per host core at a time.  `tasks`
@@ -242,7 +259,7 @@ def cpu_parallel_queries(tasks, threads: int = 0) -> dict:
         levels = list(ex.map(lambda t: oracle.bfs_queue(t[0], int(t[1])), tasks))
     wall = time.perf_counter() - t0
     return {"queries_per_s": round(len(tasks) / wall, 1), "cores": threads, "queries": len(tasks),
-            "seconds": round(wall, 3)}, levels
+            "seconds": round(wall, 3), "host": host_cpu()}, levels
 
 
 def run_reference(args, rank: int, world: int) -> None:
@@ -277,6 +294,7 @@ def run_reference(args, rank: int, world: int) -> None:
         "vs_baseline": None, "dtype": "int32", "data": "synthetic",
         "config": config_block(args, n, int(g.m)),
         "cpu_baseline": {"value": round(gteps, 4), "unit": "GTEPS", "cores": per_step, "kind": "port",
+                         "host": host_cpu(),
                          "sample": f"{per_step} of the {len(sources)} sources per step, one per thread, "
                                    "oracle restatement of the reference's queue BFS"},
         "e2e": {"value": round(gteps, 4), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -694,6 +712,7 @@ def main():
         sel = sources[: min(threads, k)]
         wall, e, lv = cpu_bfs_sample(n, row, col, sel, len(sel))
         cpu = {"value": round(e / wall / 1e9, 4), "unit": "GTEPS", "cores": len(sel), "kind": "port",
+               "host": host_cpu(),
                "sample": f"{len(sel)} of the {k} sources, one per thread, oracle restatement of the "
                          f"reference's queue BFS ({wall:.2f} s)"}
 
