@@ -17,18 +17,25 @@ summed over the sources (Graph500 convention).
   roofline    algorithmic bytes per launch (4*E_c + 8*V_c + 4*n) / mean
               launch time, against the measured HBM copy bandwidth
   cpu_baseline the oracle's restatement of the reference's CPU BFS (queue BFS
-              of the migration path) on the host cores, one source per thread
+              of the migration path) on the host cores, one source per
+              thread; with a single-thread figure timed as the reference
+              times itself (clock() around the search) and its own TEPS
+              convention (discovered vertices / s)
 
-Extra objects on the same line (rank 0, skipped with --no-extra): grid
-(7000 x 7000, persistent vs one launch per level), batched (64-lane
-multi-source on RMAT-20; 512 small graphs in one launch), primitives (CSR
-build, exclusive scan) and serving (32 resident graphs, Poisson arrivals;
---no-serving skips it).  The batched and serving objects carry a
-cpu_parallel throughput: the same queries through the oracle's queue BFS,
-one query per host core at a time.
+Extra objects on the same line (rank 0, skipped with --no-extra): config1
+(the reference's CPU-runnable ER case on GPU and CPU, levels checked against
+the reference binaries' stored output), e2e_from_edge_list (host edge list
+-> CSR build -> 64 searches -> host levels), grid (7000 x 7000, persistent
+vs one launch per level), batched (64-lane multi-source on RMAT-20; 512
+small graphs in one launch), primitives (CSR build, exclusive scan) and
+serving (32 resident graphs, Poisson arrivals; --no-serving skips it).  The
+batched and serving objects carry a cpu_parallel throughput: the same
+queries through the oracle's queue BFS, one query per host core at a time.
 
---impl reference times that CPU path alone (the reference's own code cannot
-be compiled on the GPU host: its sources are not shipped there).
+--impl reference times that CPU path alone, on the same graph, sources and
+config, loading only the oracle library (whose copy of the seeded
+generators builds the graph).  The reference's own compiled CPU code is not
+used there: its sources are not available on the GPU host.
 Multi-GPU (--gpus N under torchrun): independent replicas, no collective on
 the data path; value sums all ranks' edges over the slowest rank's time.
 """
@@ -111,9 +118,13 @@ class Dist:
             self.td.destroy_process_group()
 
 
-def workload(scale: int):
-    import gpu_graphs_gb300 as gb
-    src, dst = gb.gen_rmat(scale, RMAT["edge_factor"], RMAT["a"], RMAT["b"], RMAT["c"], RMAT["seed"])
+def workload(scale: int, gen=None):
+    """The RMAT edge list.  gen: a module with gen_rmat (the engine package on
+    the GPU arm; the oracle, which links the same generator code, on the CPU
+    reference arm so that arm never loads the engine)."""
+    if gen is None:
+        import gpu_graphs_gb300 as gen
+    src, dst = gen.gen_rmat(scale, RMAT["edge_factor"], RMAT["a"], RMAT["b"], RMAT["c"], RMAT["seed"])
     return 1 << scale, src, dst
 
 
@@ -199,14 +210,36 @@ def log(msg: str) -> None:
     print(f"[bench] {msg}", file=sys.stderr, flush=True)
 
 
-def profiled_traffic() -> int | None:
-    """DRAM bytes per k_bfs launch from the committed ncu summary, if present."""
+KERNEL_SOURCES = ("bfs.cu", "bfs.cuh", "common.cuh", "blockq.cuh")
+
+
+def kernel_source_hash() -> str:
+    """sha256 (16 hex digits) of the single-source kernel's source files."""
+    import hashlib
+    h = hashlib.sha256()
+    for name in KERNEL_SOURCES:
+        h.update((ROOT / "gpu_graphs_gb300" / "csrc" / name).read_bytes())
+    return h.hexdigest()[:16]
+
+
+def profiled_traffic() -> tuple[int | None, str]:
+    """DRAM bytes per k_bfs launch from the committed ncu summary, only when
+    the summary was taken of the kernel source being built (its stamped
+    source hash equals kernel_source_hash()); else (None, why)."""
     p = ROOT / "profiles" / "k_bfs_rmat22.md"
-    if p.exists():
-        for ln in p.read_text().splitlines():
-            if ln.startswith("traffic_bytes_per_launch ="):
-                return int(ln.split("=")[1])
-    return None
+    if not p.exists():
+        return None, "no profile"
+    traffic, stamp = None, None
+    for ln in p.read_text().splitlines():
+        if ln.startswith("traffic_bytes_per_launch ="):
+            traffic = int(ln.split("=")[1])
+        if ln.startswith("kernel_source_sha256_16 ="):
+            stamp = ln.split("=")[1].strip()
+    if traffic is None:
+        return None, "profile has no traffic line"
+    if stamp != kernel_source_hash():
+        return None, f"profile taken of other kernel sources ({stamp} != {kernel_source_hash()})"
+    return traffic, f"ncu dram__bytes_read+write per launch, profiles/k_bfs_rmat22.md (sources {stamp})"
 
 
 def measured_peak() -> tuple[float, str]:
@@ -219,16 +252,38 @@ def measured_peak() -> tuple[float, str]:
     return 6800.0, "fallback"
 
 
-def cpu_bfs_sample(n: int, row: np.ndarray, col: np.ndarray, sources, threads: int):
-    """Oracle queue BFS (the reference's CPU algorithm), one source per thread."""
+def cpu_bfs_sample(g, sources, threads: int):
+    """Oracle queue BFS (the reference's CPU algorithm), one source per thread.
+    g: an oracle CSR.  Returns (wall s, undirected component edges, levels)."""
     import oracle
-    g = oracle.CSR(n, row.astype(np.int64), col)
     t0 = time.perf_counter()
     with cf.ThreadPoolExecutor(threads) as ex:
         levels = list(ex.map(lambda s: oracle.bfs_queue(g, int(s)), sources))
     wall = time.perf_counter() - t0
     edges = sum(oracle.component_edges(g, lv) for lv in levels) / 2
     return wall, edges, levels
+
+
+def cpu_single_thread(g, sources) -> dict:
+    """The reference's CPU BFS the way its driver runs it: one thread, one
+    source at a time, clock() around each search (migration cpuBFS.cpp:5-6,
+    51-53), plus wall time; GTEPS in the Graph500 convention and TEPS in the
+    reference's own (discovered vertices per second of exec_time,
+    2D Partition/src/gpuBFS.cu:514-515, counted as cpuBFS.cpp:59 does)."""
+    import oracle
+    wall = exec_ms = edges = disc = 0.0
+    for s0 in sources:
+        t0 = time.perf_counter()
+        lv, ms, d = oracle.bfs_queue_clock(g, int(s0))
+        wall += time.perf_counter() - t0
+        exec_ms += ms
+        disc += d
+        edges += oracle.component_edges(g, lv) / 2
+    return {"value": round(edges / wall / 1e9, 4), "unit": "GTEPS", "cores": 1, "sources": len(sources),
+            "wall_ms_per_source": round(1e3 * wall / len(sources), 2),
+            "exec_time_ms_per_source": round(exec_ms / len(sources), 2),
+            "reference_teps": round(disc / (exec_ms / 1e3), 1) if exec_ms > 0 else None,
+            "reference_teps_convention": "discovered vertices / exec_time (clock())"}
 
 
 def host_cpu() -> str:
@@ -263,21 +318,23 @@ def cpu_parallel_queries(tasks, threads: int = 0) -> dict:
 
 
 def run_reference(args, rank: int, world: int) -> None:
-    """--impl reference: the reference's CPU BFS (oracle port) on the host cores."""
+    """--impl reference: the reference's CPU BFS (the oracle's restatement of
+    its queue BFS) on the host cores, on the same graph, sources, metric and
+    config as the GPU arm.  Loads only the oracle library: the graph comes
+    from the oracle's copy of the seeded generators and its CSR build."""
     if rank != 0:
         return
     import oracle
-    n, src, dst = workload(args.scale)
+    n, src, dst = workload(args.scale, oracle)
     g = oracle.csr_build(n, src, dst, oracle.UNDIRECTED)
-    deg = g.degrees()
-    sources = pick_sources(deg, args.sources)
+    del src, dst
+    sources = pick_sources(g.degrees(), args.sources)
     threads = args.cpu_threads or (os.cpu_count() or 1)
     per_step = min(threads, len(sources))
-    row32 = g.row_offset.astype(np.int32)
 
     def step(i):
         sel = [sources[(i * per_step + j) % len(sources)] for j in range(per_step)]
-        return cpu_bfs_sample(n, row32, g.col_idx, sel, per_step)
+        return cpu_bfs_sample(g, sel, per_step)
 
     for i in range(args.warmup):
         step(i)
@@ -287,6 +344,7 @@ def run_reference(args, rank: int, world: int) -> None:
         wall += w
         edges += e
     gteps = edges / wall / 1e9
+    single = cpu_single_thread(g, sources[:2])
     line = {
         "impl": "reference", "metric": "single-source GTEPS", "value": round(gteps, 4), "unit": "GTEPS",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -296,19 +354,102 @@ def run_reference(args, rank: int, world: int) -> None:
         "cpu_baseline": {"value": round(gteps, 4), "unit": "GTEPS", "cores": per_step, "kind": "port",
                          "host": host_cpu(),
                          "sample": f"{per_step} of the {len(sources)} sources per step, one per thread, "
-                                   "oracle restatement of the reference's queue BFS"},
+                                   "oracle restatement of the reference's queue BFS",
+                         "single_thread": single},
         "e2e": {"value": round(gteps, 4), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
 def config_block(args, n: int, m: int) -> dict:
-    return {"workload": f"rmat-scale{args.scale}-ef16-64src", "graph": "RMAT a=.57 b=.19 c=.19 d=.05, ids permuted",
+    """The workload, identical on both arms (engine settings go elsewhere)."""
+    return {"workload": f"rmat-scale{args.scale}-ef16-{args.sources}src",
+            "graph": "RMAT a=.57 b=.19 c=.19 d=.05, ids permuted, symmetrised, deduplicated, no self-loops",
             "vertices": n, "directed_edges": m, "sources_per_step": args.sources,
             "l2": "inputs larger than L2 (CSR ~0.5 GB vs 129 MB L2)"}
 
 
 # ---- the other configurations (extra objects on the same line) --------------------
+
+def measure_config1(torch) -> dict:
+    """The reference's own CPU-runnable case: Erdos-Renyi n = 65,536 with
+    262,144 distinct undirected pairs (seed 1), symmetrised, source 0, plain
+    top-down BFS.  GPU: device time of one launch and the same through the
+    C ABI into a host buffer; CPU: the reference's queue BFS (oracle
+    restatement) on one thread, timed by clock() as the reference does.
+    Levels are checked against the reference binaries' own output for this
+    graph (tests/golden/syn_er16.npz) and against the oracle."""
+    import gpu_graphs_gb300 as gb
+    import oracle
+    n = 65536
+    src, dst = gb.gen_er(n, 262144, 1)
+    g = gb.Graph.from_edges(n, src, dst, gb.UNDIRECTED)
+    og = oracle.csr_build(n, src, dst, oracle.UNDIRECTED)
+    dev = torch.empty(n, dtype=torch.int32, device="cuda")
+    res = {"workload": "ER n=65536, 262144 undirected pairs (seed 1), symmetrised, source 0",
+           "vertices": n, "directed_edges": int(g.m)}
+    for name, direction in (("topdown", gb.DIR_TOPDOWN), ("direction_optimising", gb.DIR_OPTIMIZING)):
+        g.set_params(direction=direction)
+        for _ in range(5):
+            g.bfs(0, out=dev)
+        runs = [g.bfs(0, out=dev, stats=True)[1] for _ in range(50)]
+        ms = float(np.median([r.ms for r in runs]))
+        st = runs[-1]
+        host = np.empty(n, np.int32)
+        t0 = time.perf_counter()
+        for _ in range(50):
+            g.bfs(0, out=host)
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / 50
+        res[name] = {"gpu_ms": round(ms, 4), "gteps": round(st.edges_in_component / 2 / (ms / 1e3) / 1e9, 3),
+                     "reference_teps": round(st.edges_traversed / (ms / 1e3), 1),
+                     "e2e_ms_host_output": round(e2e_ms, 4), "levels": int(st.levels),
+                     "levels_identical_oracle": bool(np.array_equal(host, oracle.bfs_queue(og, 0)))}
+    g.set_params(direction=gb.DIR_OPTIMIZING)
+    lv, exec_ms, disc = oracle.bfs_queue_clock(og, 0)
+    walls = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        oracle.bfs_queue(og, 0)
+        walls.append(time.perf_counter() - t0)
+    wall_ms = 1e3 * float(np.median(walls))
+    ec = oracle.component_edges(og, lv) / 2
+    res["cpu"] = {"kind": "port", "cores": 1, "host": host_cpu(), "exec_time_ms": round(exec_ms, 3),
+                  "wall_ms": round(wall_ms, 3), "gteps": round(ec / (wall_ms / 1e3) / 1e9, 4),
+                  "reference_teps": round(disc / (exec_ms / 1e3), 1) if exec_ms > 0 else None,
+                  "timing": "clock() around the queue BFS (migration cpuBFS.cpp:5-6,51-53); wall = median of 5"}
+    golden = ROOT / "tests" / "golden" / "syn_er16.npz"
+    if golden.exists():
+        z = np.load(golden)
+        res["levels_identical_reference_binaries"] = bool(int(z["sources"][0]) == 0 and
+                                                          np.array_equal(z["levels"][0], host))
+    res["speedup_gpu_vs_cpu_wall"] = round(wall_ms / res["topdown"]["gpu_ms"], 1)
+    return res
+
+
+def measure_e2e_from_edge_list(scale: int, sources, torch) -> dict:
+    """The whole graphBFS path through the public API: host edge list in,
+    CSR built on the GPU (symmetrised, deduplicated, hub-first rows), the 64
+    searches, every level array copied back into pinned host memory."""
+    import gpu_graphs_gb300 as gb
+    n, src, dst = workload(scale)
+    host = torch.empty((len(sources), n), dtype=torch.int32, pin_memory=True).numpy()
+    times = []
+    for i in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g = gb.Graph.from_edges(n, src, dst, gb.UNDIRECTED | gb.HUB_FIRST)
+        t1 = time.perf_counter()
+        _, sts = g.bfs_many(sources, out=host)
+        t2 = time.perf_counter()
+        times.append((t2 - t0, t1 - t0, t2 - t1))
+        edges = sum(s.edges_in_component for s in sts) / 2
+        del g
+    tot, build, bfs = min(times)
+    return {"workload": f"RMAT scale {scale}: {len(src)} host edges in, {len(sources)} level arrays out",
+            "h2d_bytes": 8 * len(src), "d2h_bytes": 4 * n * len(sources),
+            "total_ms": round(tot * 1e3, 2), "csr_build_ms": round(build * 1e3, 2),
+            "searches_ms": round(bfs * 1e3, 2), "gteps_incl_build": round(edges / tot / 1e9, 2)}
+
 
 def measure_grid(side: int, torch) -> dict:
     """High-diameter grid: one persistent launch vs one launch per level (host
@@ -346,6 +487,22 @@ def measure_grid(side: int, torch) -> dict:
             "gteps_persistent": round(st.edges_in_component / 2 / (t_p / 1e3) / 1e9, 3),
             "us_per_level_persistent": round(1e3 * t_p / max(1, st.levels), 3),
             "levels_identical": same}
+
+
+def many_graphs_workload(gen, count: int = 512):
+    """The fused-launch configuration: `count` Erdos-Renyi graphs, n
+    log-uniform in [2^8, 2^16], 4n sampled pairs each (average degree 8 once
+    symmetrised), one source each drawn among its vertices of degree > 0.
+    gen: a module with gen_er.  Returns ([(n, src, dst)], sources)."""
+    rng = np.random.default_rng(1)
+    sizes = np.exp(rng.uniform(np.log(256), np.log(65536), count)).astype(np.int64)
+    graphs, srcs = [], []
+    for i, ni in enumerate(sizes):
+        s_, d_ = gen.gen_er(int(ni), int(4 * ni), 1000 + i)
+        deg = np.bincount(np.concatenate([s_, d_]), minlength=int(ni)) - 2 * np.bincount(s_[s_ == d_], minlength=int(ni))
+        graphs.append((int(ni), s_, d_))
+        srcs.append(int(rng.choice(np.flatnonzero(deg > 0))))
+    return graphs, srcs
 
 
 def measure_batched(torch) -> dict:
@@ -390,14 +547,8 @@ def measure_batched(torch) -> dict:
                                                            cpu["queries_per_s"], 1)
     del plain_out, multi_out, g, og, row, col, mo, lv
 
-    rng = np.random.default_rng(1)
-    sizes = np.exp(rng.uniform(np.log(256), np.log(65536), 512)).astype(np.int64)
-    graphs, srcs = [], []
-    for i, ni in enumerate(sizes):
-        s_, d_ = gb.gen_er(int(ni), int(4 * ni), 1000 + i)
-        deg = np.bincount(np.concatenate([s_, d_]), minlength=int(ni)) - 2 * np.bincount(s_[s_ == d_], minlength=int(ni))
-        graphs.append((int(ni), s_, d_))
-        srcs.append(int(rng.choice(np.flatnonzero(deg > 0))))
+    graphs, srcs = many_graphs_workload(gb)
+    sizes = np.array([g[0] for g in graphs], np.int64)
     gs = gb.GraphSet.from_edges(graphs)
     fused, st = gs.bfs(srcs, stats=True)
     t_fused = min(gs.bfs(srcs, stats=True)[1].ms for _ in range(3))
@@ -628,11 +779,17 @@ def main():
     out = torch.empty((k, n), dtype=torch.int32, device="cuda")
     stream = torch.cuda.ExternalStream(g.stream)
 
-    # parity spot check against the oracle (outside the timed region)
+    # parity check against the oracle (outside the timed region): the
+    # highest-degree vertex and the first 7 bench sources, bit for bit
     import oracle
     og = oracle.CSR(n, row.astype(np.int64), col)
-    g.bfs_many(sources[:2], out=out[:2])
-    parity = all(np.array_equal(out[i].cpu().numpy(), oracle.bfs_queue(og, int(s))) for i, s in enumerate(sources[:2]))
+    chk = [int(np.argmax(deg))] + [int(s) for s in sources[:7]]
+    got = g.bfs_many(chk)[0]
+    with cf.ThreadPoolExecutor(min(len(chk), os.cpu_count() or 1)) as ex:
+        want = list(ex.map(lambda s0: oracle.bfs_queue(og, s0), chk))
+    parity = {"sources": len(chk), "includes_max_degree_vertex": True,
+              "levels_identical": all(np.array_equal(a, b) for a, b in zip(got, want))}
+    del got, want
 
     launch_ms, launch_ec, edges_c, verts, lvls = [], [], 0, 0, []
     with ClockSampler(local) as clk:
@@ -666,11 +823,17 @@ def main():
     b_alg = 4 * edges_c + 8 * verts + 4 * n * launches
     peak, peak_kind = measured_peak()
     achieved = (b_alg / launches) / (np.mean(launch_ms) / 1e3) / 1e9
+    traffic, traffic_src = profiled_traffic() if args.scale == 22 else (None, "other workload")
+    mean_s = float(np.mean(launch_ms)) / 1e3
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                "bytes_per_launch": int(b_alg / launches), "mean_launch_us": round(1e3 * float(np.mean(launch_ms)), 2),
-                "traffic": profiled_traffic() if args.scale == 22 else None,
-                "traffic_source": "ncu dram__bytes_read+write per launch, profiles/k_bfs_rmat22.md"}
+                "achieved_is": "algorithmic bytes per launch (4*E_c + 8*V_c + 4*n) / mean launch time",
+                "bytes_per_launch": int(b_alg / launches), "mean_launch_us": round(1e3 * mean_s, 2),
+                "traffic": traffic, "traffic_source": traffic_src,
+                "dram_achieved": round(traffic / mean_s / 1e9, 1) if traffic else None,
+                "dram_frac": round(traffic / mean_s / 1e9 / peak, 4) if traffic else None,
+                "limiter": "latency and level synchronisation: bottom-up steps stop at the first parent, so "
+                           "measured DRAM traffic is a fraction of the algorithmic bytes"}
     gteps_each = [(e / 2) / (t / 1e3) / 1e9 for e, t in zip(launch_ec, launch_ms)]
 
     # e2e through the C ABI with pinned host output buffers
@@ -681,7 +844,7 @@ def main():
         g.bfs_many(sources, out=hv)
         torch.cuda.synchronize()
         dist.barrier()
-        steps_e2e = max(1, min(args.steps, 3))
+        steps_e2e = max(1, args.steps)
         t0 = time.perf_counter()
         for _ in range(steps_e2e):
             g.bfs_many(sources, out=hv)
@@ -690,13 +853,18 @@ def main():
         wall = dist.reduce(t1 - t0, "max")
         e2e = {"value": round(dist.reduce(und_edges / args.steps * steps_e2e, "sum") / wall / 1e9, 3),
                "unit": "GTEPS", "h2d_bytes_per_step": 4 * k, "d2h_bytes_per_step": 4 * k * n,
-               "steps": steps_e2e}
+               "steps": steps_e2e, "clock": "host perf_counter around the calls",
+               "graph": "resident in HBM (built before the timed region; see e2e_from_edge_list)"}
         del host, hv
 
     extra = {}
     # the other configurations and the CPU baseline: single-GPU runs only
     # (a scaling run holds all N GPUs; its line needs the headline alone)
     if rank == 0 and world == 1 and not args.no_extra:
+        extra["config1"] = measure_config1(torch)
+        log("config1 done")
+        extra["e2e_from_edge_list"] = measure_e2e_from_edge_list(args.scale, sources, torch)
+        log("e2e from edge list done")
         extra["grid"] = measure_grid(args.grid_side, torch)
         log("grid done")
         extra["batched"] = measure_batched(torch)
@@ -710,21 +878,22 @@ def main():
     if not args.no_cpu and rank == 0 and world == 1:
         threads = args.cpu_threads or (os.cpu_count() or 1)
         sel = sources[: min(threads, k)]
-        wall, e, lv = cpu_bfs_sample(n, row, col, sel, len(sel))
+        wall, e, lv = cpu_bfs_sample(og, sel, len(sel))
         cpu = {"value": round(e / wall / 1e9, 4), "unit": "GTEPS", "cores": len(sel), "kind": "port",
                "host": host_cpu(),
                "sample": f"{len(sel)} of the {k} sources, one per thread, oracle restatement of the "
-                         f"reference's queue BFS ({wall:.2f} s)"}
+                         f"reference's queue BFS ({wall:.2f} s)",
+               "single_thread": cpu_single_thread(og, sources[:2])}
 
     if rank == 0:
         line = {
             "metric": "single-source GTEPS", "value": round(value, 3), "unit": "GTEPS", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-            "data": "synthetic", "config": config_block(args, n, g.m) | {"parallelism": f"replicas{world}",
-                                                                            "layout": args.layout, "params": params},
+            "data": "synthetic", "config": config_block(args, n, g.m),
+            "engine": {"parallelism": f"replicas{world}", "layout": args.layout, "params": params},
             "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
-            "clocks": clk.summary(), "parity_spot_check": parity,
+            "clocks": clk.summary(), "parity_check": parity,
             "per_source_gteps": {"min": round(min(gteps_each), 2), "median": round(statistics.median(gteps_each), 2),
                                  "max": round(max(gteps_each), 2)},
             "levels_td_bu": sorted(set(lvls))[:8],

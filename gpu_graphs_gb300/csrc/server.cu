@@ -75,6 +75,10 @@ struct gbfs_server {
     gbfs_server_config cfg{};
     int device = 0;
     int max_ctas = 0;
+    // held by gbfs_server_add_graph from its budget check to its commit, so
+    // concurrent admissions see each other's bytes and never resize the slot
+    // workspaces against a stale capacity (workers never take it)
+    std::mutex admit_mu;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::map<int32_t, SrvGraph> graphs;
@@ -313,6 +317,7 @@ extern "C" void gbfs_server_destroy(gbfs_server *s)
 extern "C" int gbfs_server_add_graph(gbfs_server *s, gbfs_graph *g, int32_t *graph_id)
 {
     if (!s || !g || !graph_id) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
+    std::lock_guard<std::mutex> admit(s->admit_mu);
     std::unique_lock<std::mutex> lk(s->mu);
     // a directed graph that may step bottom-up gets its transpose (in-edge
     // rows plus their heavy-row list) built here, inside the budget
@@ -427,7 +432,7 @@ extern "C" int gbfs_server_wait(gbfs_server *s, int64_t ticket, int32_t timeout_
     std::unique_lock<std::mutex> lk(s->mu);
     auto it = s->queries.find(ticket);
     if (it == s->queries.end()) return fail(GBFS_ERR_NOT_FOUND, "unknown ticket");
-    auto q = it->second;
+    auto q = it->second;  // keeps the query alive across the wait
     auto pred = [&] { return q->done; };
     if (timeout_ms < 0) s->cv_done.wait(lk, pred);
     else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred))
@@ -438,7 +443,9 @@ extern "C" int gbfs_server_wait(gbfs_server *s, int64_t ticket, int32_t timeout_
         info->batch_lanes = q->lanes;
         info->status = q->status;
     }
-    s->queries.erase(it);
+    // erase by key: another thread waiting on the same ticket may have
+    // erased it while this one slept (the iterator would be stale)
+    s->queries.erase(ticket);
     return q->status == GBFS_OK ? GBFS_OK : fail(q->status, "query failed on the device");
 }
 

@@ -50,10 +50,12 @@ class Server:
         return t.value
 
     def wait(self, ticket: int, timeout_ms: int = -1):
+        """(levels, QueryInfo) of a ticket.  If several threads wait on one
+        ticket, all of them see its status; the levels array goes to one."""
         info = _lib.QueryInfo()
         rc = lib.gbfs_server_wait(self._h, int(ticket), int(timeout_ms), C.byref(info))
         check(rc, "gbfs_server_wait")
-        return self._outs.pop(ticket), info
+        return self._outs.pop(ticket, None), info
 
     def stats(self) -> dict:
         st = _lib.ServerStats()

@@ -23,6 +23,8 @@
  * cudaPointerGetAttributes; device pointers must be on the current device.
  * Thread safety: calls on one graph handle are serialised by a per-graph
  * lock; different handles may be used from different threads at once.
+ * The library keeps per-device launch settings for the life of the
+ * process: cudaDeviceReset while it is in use is not supported.
  */
 #ifndef GBFS_H
 #define GBFS_H
@@ -290,6 +292,8 @@ int gbfs_exclusive_scan_i32(const int32_t *d_in, int64_t *d_out, int64_t n,
  *   - n <= GBFS_SCAN_NOALLOC_MAX_N, else GBFS_ERR_TOO_LARGE;
  *   - the first call on a device looks the array's address up once (with
  *     that device current); make that first call before any stream capture;
+ *   - do not call cudaDeviceReset between calls: the library keeps that
+ *     address (and its other per-device launch settings) for the process;
  *   - all calls share the array: calls whose work overlaps on the GPU
  *     (different streams or threads) race; serialise them;
  *   - the call synchronises `stream` to report the scan's status.
@@ -393,7 +397,8 @@ void gbfs_server_destroy(gbfs_server *s);
  * A directed graph whose direction is not GBFS_DIR_TOPDOWN gets its
  * transpose (in-edge rows, for bottom-up and pull steps) built here and
  * counted in the budget.  GBFS_ERR_BUDGET if its CSR plus one slot's
- * workspace does not fit. */
+ * workspace does not fit.  Concurrent calls are serialised (each sees the
+ * bytes the others admitted). */
 int gbfs_server_add_graph(gbfs_server *s, gbfs_graph *g, int32_t *graph_id);
 int gbfs_server_remove_graph(gbfs_server *s, int32_t graph_id);
 /* Queue one query; levels_out (host, n int32) is written before completion
@@ -401,7 +406,9 @@ int gbfs_server_remove_graph(gbfs_server *s, int32_t graph_id);
 int gbfs_server_submit(gbfs_server *s, int32_t graph_id, int32_t source,
                        int32_t *levels_out, int64_t *ticket);
 /* Wait for a ticket (timeout_ms < 0: forever).  GBFS_ERR_TIMEOUT if it is
- * still pending; otherwise the query's own status.  info nullable. */
+ * still pending; otherwise the query's own status.  info nullable.  The
+ * ticket is released when a wait returns its result: threads already
+ * waiting on it all get the result, later waits get GBFS_ERR_NOT_FOUND. */
 int gbfs_server_wait(gbfs_server *s, int64_t ticket, int32_t timeout_ms,
                      gbfs_query_info *info);
 int gbfs_server_get_stats(gbfs_server *s, gbfs_server_stats *st);

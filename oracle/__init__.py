@@ -6,10 +6,14 @@ timed CPU baseline; the engine never calls it.
 
   * liboracle.so -- oracle.c, a plain-C restatement of the reference's CPU
     path (CSR build of 2D Partition/src/csc.cpp, level-synchronous BFS of
-    2D Partition/src/cpuBFS.cpp, queue BFS of the migration cpuBFS.cpp).
+    2D Partition/src/cpuBFS.cpp, queue BFS of the migration cpuBFS.cpp),
+    linked with the seeded workload generators (the engine's host-only
+    gen.cpp compiled a second time), so the CPU reference arm of bench.py
+    builds its graphs without loading the engine.
   * _ref/ref_c9, _ref/ref_c10 -- the reference's own CPU BFS compiled from
-    its unmodified sources by oracle/Makefile (only where the reference is
-    mounted); used to pin the restatement and to make tests/golden/.
+    its unmodified sources by oracle/Makefile, only when
+    GBFS_REFERENCE_ROOT names a checkout of the reference project; used to
+    pin the restatement and to make tests/golden/.
 """
 from __future__ import annotations
 
@@ -24,24 +28,31 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "liboracle.so"
 REF_DIR = HERE / "_ref"
-REFERENCE_ROOT = Path(os.environ.get("GBFS_REFERENCE_ROOT", "/root/reference"))
+# a checkout of the reference project, or None (then _ref/ is not built)
+REFERENCE_ROOT = Path(os.environ["GBFS_REFERENCE_ROOT"]) if os.environ.get("GBFS_REFERENCE_ROOT") else None
+GEN_SRC = HERE.parent / "gpu_graphs_gb300" / "csrc" / "gen.cpp"
 
 SYMMETRIZE, DEDUP, DROP_SELF_LOOPS = 1, 2, 4
 UNDIRECTED = 7
 
 
+def reference_present() -> bool:
+    return REFERENCE_ROOT is not None and REFERENCE_ROOT.exists()
+
+
 def build(ref: bool = False) -> None:
     """make liboracle.so (and the reference binaries when asked and possible)."""
-    targets = ["all"] + (["ref"] if ref and REFERENCE_ROOT.exists() else [])
-    subprocess.run(["make", "-s", "-C", str(HERE), *targets, f"REF={REFERENCE_ROOT}"], check=True,
-                   stdout=subprocess.DEVNULL)
+    targets = ["all"] + (["ref"] if ref and reference_present() else [])
+    extra = [f"REF={REFERENCE_ROOT}"] if reference_present() else []
+    subprocess.run(["make", "-s", "-C", str(HERE), *targets, *extra], check=True, stdout=subprocess.DEVNULL)
 
 
 def _stale() -> bool:
     if not LIB_PATH.exists():
         return True
     t = LIB_PATH.stat().st_mtime
-    return any(p.stat().st_mtime > t for p in (HERE / "oracle.c", HERE / "oracle.h"))
+    deps = (HERE / "oracle.c", HERE / "oracle.h", GEN_SRC, HERE.parent / "include" / "gbfs.h")
+    return any(p.stat().st_mtime > t for p in deps if p.exists())
 
 
 _lib = None
@@ -60,6 +71,17 @@ def lib() -> C.CDLL:
         L.oracle_bfs_levelsync.argtypes = [C.c_int32, P, P, C.c_int32, P, P]
         L.oracle_bfs_queue.restype = C.c_int
         L.oracle_bfs_queue.argtypes = [C.c_int32, P, P, C.c_int32, P]
+        L.oracle_bfs_queue_clock.restype = C.c_int
+        L.oracle_bfs_queue_clock.argtypes = [C.c_int32, P, P, C.c_int32, P, P, P]
+        L.gbfs_gen_er.restype = C.c_int64
+        L.gbfs_gen_er.argtypes = [C.c_int32, C.c_int64, C.c_uint64, P, P, C.c_int64]
+        L.gbfs_gen_rmat.restype = C.c_int64
+        L.gbfs_gen_rmat.argtypes = [C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_uint64, P, P,
+                                    C.c_int64]
+        L.gbfs_gen_grid.restype = C.c_int64
+        L.gbfs_gen_grid.argtypes = [C.c_int32, C.c_double, C.c_double, C.c_int32, C.c_uint64, P, P, C.c_int64]
+        L.gbfs_gen_grid_capacity.restype = C.c_int64
+        L.gbfs_gen_grid_capacity.argtypes = [C.c_int32, C.c_double]
         L.oracle_exclusive_scan_i32.restype = None
         L.oracle_exclusive_scan_i32.argtypes = [P, P, C.c_int64]
         L.oracle_component_edges.restype = C.c_int64
@@ -118,6 +140,48 @@ def bfs_queue(g: CSR, source: int) -> np.ndarray:
     if lib().oracle_bfs_queue(g.n, _p(g.row_offset), _p(g.col_idx), source, _p(level)) != 0:
         raise ValueError("bad source")
     return level
+
+
+def bfs_queue_clock(g: CSR, source: int) -> tuple[np.ndarray, float, int]:
+    """Queue BFS timed the reference's way (clock() around it, in ms); also
+    the reference's edge count (discovered vertices).  Single-threaded use
+    only: clock() counts the whole process's CPU time."""
+    level = np.empty(g.n, np.int32)
+    ms = C.c_double()
+    disc = C.c_int64()
+    if lib().oracle_bfs_queue_clock(g.n, _p(g.row_offset), _p(g.col_idx), source, _p(level), C.byref(ms),
+                                    C.byref(disc)) != 0:
+        raise ValueError("bad source")
+    return level, float(ms.value), int(disc.value)
+
+
+# ---- seeded workload generators (the same code as the engine's, host only) -------------
+
+def _gen_call(fn, cap: int, *args) -> tuple[np.ndarray, np.ndarray]:
+    src = np.empty(max(cap, 1), np.int32)
+    dst = np.empty(max(cap, 1), np.int32)
+    r = fn(*args, _p(src), _p(dst), cap)
+    if r < 0:
+        raise ValueError(f"{fn.__name__} failed ({r})")
+    return src[:r], dst[:r]
+
+
+def gen_er(n: int, pairs: int, seed: int) -> tuple[np.ndarray, np.ndarray]:
+    return _gen_call(lib().gbfs_gen_er, pairs, int(n), int(pairs), int(seed))
+
+
+def gen_rmat(scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+             seed: int = 1) -> tuple[np.ndarray, np.ndarray]:
+    return _gen_call(lib().gbfs_gen_rmat, (1 << scale) * edge_factor, int(scale), int(edge_factor), float(a),
+                     float(b), float(c), int(seed))
+
+
+def gen_grid(side: int, drop: float = 0.1, extra: float = 0.001, radius: int = 8,
+             seed: int = 1) -> tuple[np.ndarray, np.ndarray]:
+    cap = int(lib().gbfs_gen_grid_capacity(int(side), float(extra)))
+    if cap < 0:
+        raise ValueError("gbfs_gen_grid_capacity failed")
+    return _gen_call(lib().gbfs_gen_grid, cap, int(side), float(drop), float(extra), int(radius), int(seed))
 
 
 def exclusive_scan(x) -> np.ndarray:

@@ -8,6 +8,7 @@
 #include "oracle.h"
 
 #include <stdlib.h>
+#include <time.h>
 #include <string.h>
 
 static int cmp_i32(const void *a, const void *b)
@@ -141,6 +142,26 @@ int oracle_bfs_queue(int32_t n, const int64_t *row_offset,
     }
     free(queue);
     return 0;
+}
+
+/* Timing of migration cpuBFS.cpp:5-6,51-53 around the queue BFS above. */
+int oracle_bfs_queue_clock(int32_t n, const int64_t *row_offset,
+                           const int32_t *col_idx, int32_t source,
+                           int32_t *level, double *exec_ms,
+                           int64_t *discovered)
+{
+    clock_t start = clock();
+    int r = oracle_bfs_queue(n, row_offset, col_idx, source, level);
+    clock_t end = clock();
+    if (exec_ms) *exec_ms = ((double)(end - start)) / CLOCKS_PER_SEC * 1000.0;
+    if (discovered) {
+        int64_t d = 0;
+        int32_t v;
+        if (r == 0)
+            for (v = 0; v < n; v++) d += level[v] > 0;
+        *discovered = d;
+    }
+    return r;
 }
 
 /* Reference contract: 2D Partition/src/prefixSum.cu:136-224 (exclusive). */

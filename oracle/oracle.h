@@ -65,6 +65,21 @@ int oracle_bfs_queue(int32_t n, const int64_t *row_offset,
                      const int32_t *col_idx, int32_t source, int32_t *level);
 
 /*
+ * oracle_bfs_queue with the reference's own timing around it: clock() at
+ * entry and exit, exec_ms = (end - start) / CLOCKS_PER_SEC * 1000
+ * (migration cpuBFS.cpp:5-6,51-53; the same formula in
+ * 2D Partition/src/cpuBFS.cpp:5-6,71-72).  clock() counts the CPU time of
+ * the whole process, so exec_ms is meaningful only when no other thread
+ * runs meanwhile.  Also returns the reference's edge count convention, the
+ * number of discovered vertices (2D Partition/src/cpuBFS.cpp:59), in
+ * *discovered.  Returns 0, or -1 on a bad source.
+ */
+int oracle_bfs_queue_clock(int32_t n, const int64_t *row_offset,
+                           const int32_t *col_idx, int32_t source,
+                           int32_t *level, double *exec_ms,
+                           int64_t *discovered);
+
+/*
  * Exclusive prefix sum, the contract of PrefixSum::sum_scan_blelloch
  * (2D Partition/src/prefixSum.cu:136-224: out[0]=0, out[i]=sum in[0..i-1]).
  * 64-bit accumulation.

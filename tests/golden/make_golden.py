@@ -1,7 +1,7 @@
 """Generate tests/golden/*.npz from the reference's own CPU BFS.
 
-Run in a container where the reference project is mounted (default
-/root/reference, override with GBFS_REFERENCE_ROOT); it builds
+Run where a checkout of the reference project is available, named by
+GBFS_REFERENCE_ROOT (or --reference <dir>); it builds
 oracle/_ref/ref_c9 and ref_c10 from the reference's unmodified sources
 (oracle/Makefile), then records:
 
@@ -17,7 +17,8 @@ oracle/_ref/ref_c9 and ref_c10 from the reference's unmodified sources
     the oracle's CSR builder) injected into the reference BFS objects.
 
 The .npz files hold only inputs and outputs; nothing at test time reads the
-reference.  Usage:  python tests/golden/make_golden.py
+reference.  Usage:
+  GBFS_REFERENCE_ROOT=<reference checkout> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -35,7 +36,6 @@ sys.path.insert(0, str(ROOT))
 
 import oracle  # noqa: E402
 
-REF = Path(os.environ.get("GBFS_REFERENCE_ROOT", "/root/reference"))
 OUT = Path(__file__).resolve().parent
 
 TEXT_FIXTURES = {
@@ -104,8 +104,15 @@ def edge_hash(src: np.ndarray, dst: np.ndarray) -> str:
 
 
 def main() -> None:
+    global REF
+    if "--reference" in sys.argv:
+        os.environ["GBFS_REFERENCE_ROOT"] = sys.argv[sys.argv.index("--reference") + 1]
+    if not os.environ.get("GBFS_REFERENCE_ROOT"):
+        sys.exit("name the reference checkout: GBFS_REFERENCE_ROOT=<dir> or --reference <dir>")
+    REF = Path(os.environ["GBFS_REFERENCE_ROOT"])
     if not REF.exists():
         sys.exit(f"reference not found at {REF}")
+    oracle.REFERENCE_ROOT = REF
     oracle.build(ref=True)
     for name, rel in TEXT_FIXTURES.items():
         path = REF / rel
@@ -134,7 +141,7 @@ def main() -> None:
                         sources=np.array(sources, np.int32), levels=levels, origin=rel)
     print("ref_wiki_vote", n, len(src), levels.shape)
 
-    import gpu_graphs_gb300 as gb  # generators only (host code)
+    gb = oracle  # the seeded generators (host code, linked into the oracle library)
     for name, (kind, args, sources) in SYNTHETIC.items():
         if kind == "er":
             src, dst = gb.gen_er(args["n"], args["pairs"], args["seed"])

@@ -135,3 +135,26 @@ def test_oracle_parents_small_graph(orc):
     assert level.tolist() == [0, 1, 1, 2, -1]
     assert pred[3] == 2  # row 0 lists 2 first, so 2 discovers 3 first
     assert orc.min_parents(g, level).tolist() == [-1, 0, 0, 1, -1]
+
+
+@pytest.mark.parametrize("name", golden_names("syn_"))
+def test_oracle_generators_reproduce_golden_edges(orc, name):
+    """The oracle's copy of the seeded generators gives the bytes the golden
+    graphs were made from, and the same bytes as the engine's copy."""
+    import ast
+    import hashlib
+    d = load_golden(name)
+    kind = str(d["kind"])
+    args = ast.literal_eval(str(d["args"]))
+    if kind == "er":
+        src, dst = orc.gen_er(args["n"], args["pairs"], args["seed"])
+    elif kind == "rmat":
+        src, dst = orc.gen_rmat(args["scale"], args["edge_factor"], seed=args["seed"])
+    else:
+        src, dst = orc.gen_grid(args["side"], args["drop"], args["extra"], args["radius"], args["seed"])
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(src, np.int32).tobytes())
+    h.update(np.ascontiguousarray(dst, np.int32).tobytes())
+    assert h.hexdigest() == str(d["edge_sha256"])
+    _, s2, d2 = synthetic_edges(d)
+    assert np.array_equal(src, s2) and np.array_equal(dst, d2)

@@ -11,6 +11,8 @@ from __future__ import annotations
 
 import ctypes as C
 import re
+import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -51,7 +53,67 @@ def test_noalloc_scan_matches_pooled_scan(gb):
         assert lib.gbfs_exclusive_scan_i32_noalloc(C.c_void_p(x.data_ptr()), C.c_void_p(got.data_ptr()), n,
                                                    None) == 0
         assert torch.equal(got, want)
+        if n < max_n:  # and against an independent host computation
+            xh = x.cpu().numpy().astype(np.int64)
+            ref = np.concatenate([[0], np.cumsum(xh)[:-1]])
+            assert np.array_equal(got.cpu().numpy(), ref)
     # limits: empty input is a no-op, beyond the scratch is refused
     assert lib.gbfs_exclusive_scan_i32_noalloc(C.c_void_p(x.data_ptr()), C.c_void_p(got.data_ptr()), 0, None) == 0
     assert lib.gbfs_exclusive_scan_i32_noalloc(C.c_void_p(x.data_ptr()), C.c_void_p(got.data_ptr()), max_n + 1,
                                                None) == gb._lib.ERR_TOO_LARGE
+
+
+def test_noalloc_scan_on_a_side_stream(gb):
+    """Two calls in a row on a non-default stream, against numpy."""
+    torch = pytest.importorskip("torch")
+    lib = bind(gb)
+    side = torch.cuda.Stream()
+    rng = np.random.default_rng(11)
+    for n in (1_048_577, 4099):
+        xh = rng.integers(-1000, 1000, size=n, dtype=np.int32)
+        with torch.cuda.stream(side):
+            x = torch.from_numpy(xh).cuda(non_blocking=False)
+            got = torch.full((n,), -7, dtype=torch.int64, device="cuda")
+        side.synchronize()
+        assert lib.gbfs_exclusive_scan_i32_noalloc(C.c_void_p(x.data_ptr()), C.c_void_p(got.data_ptr()), n,
+                                                   C.c_void_p(side.cuda_stream)) == 0
+        side.synchronize()
+        ref = np.concatenate([[0], np.cumsum(xh.astype(np.int64))[:-1]])
+        assert np.array_equal(got.cpu().numpy(), ref)
+
+
+_FRESH = r"""
+import ctypes as C, sys
+import numpy as np, torch
+sys.path.insert(0, {root!r})
+import gpu_graphs_gb300 as gb
+lib = C.CDLL(gb.library_path())
+fn = lib.gbfs_exclusive_scan_i32_noalloc
+fn.restype = C.c_int
+fn.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+n = 5_000_000
+x = torch.from_numpy(np.arange(n, dtype=np.int32) % 97).cuda()
+out = torch.empty(n, dtype=torch.int64, device="cuda")
+torch.cuda.synchronize()
+assert fn(C.c_void_p(x.data_ptr()), C.c_void_p(out.data_ptr()), n, None) == 0  # first call in the process
+free0 = torch.cuda.mem_get_info()[0]
+for _ in range(3):
+    assert fn(C.c_void_p(x.data_ptr()), C.c_void_p(out.data_ptr()), n, None) == 0
+torch.cuda.synchronize()
+free1 = torch.cuda.mem_get_info()[0]
+ref = np.concatenate([[0], np.cumsum(np.arange(n, dtype=np.int64) % 97)[:-1]])
+assert np.array_equal(out.cpu().numpy(), ref)
+print("FREE", free0, free1)
+"""
+
+
+def test_noalloc_scan_allocates_nothing_in_a_fresh_process():
+    """First in its process, then three more calls: the device's free memory
+    does not move (a cudaMalloc would take at least one 2 MB page)."""
+    pytest.importorskip("torch")
+    r = subprocess.run([sys.executable, "-c", _FRESH.format(root=str(ROOT))], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    line = [ln for ln in r.stdout.splitlines() if ln.startswith("FREE")][-1]
+    _, f0, f1 = line.split()
+    assert int(f0) == int(f1)
