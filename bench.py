@@ -828,7 +828,7 @@ def main():
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                 "achieved_is": "algorithmic bytes per launch (4*E_c + 8*V_c + 4*n) / mean launch time",
-                "bytes_per_launch": int(b_alg / launches), "mean_launch_us": round(1e3 * mean_s, 2),
+                "bytes_per_launch": int(b_alg / launches), "mean_launch_us": round(1e6 * mean_s, 2),
                 "traffic": traffic, "traffic_source": traffic_src,
                 "dram_achieved": round(traffic / mean_s / 1e9, 1) if traffic else None,
                 "dram_frac": round(traffic / mean_s / 1e9 / peak, 4) if traffic else None,

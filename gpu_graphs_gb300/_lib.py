@@ -6,9 +6,11 @@ module without it raises ImportError: there is no Python or CPU fallback.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
-LIB_PATH = Path(__file__).resolve().parent / "libgbfs.so"
+# GBFS_LIBRARY names another build of the same library (e.g. to compare two builds)
+LIB_PATH = Path(os.environ.get("GBFS_LIBRARY") or Path(__file__).resolve().parent / "libgbfs.so")
 
 OK = 0
 ERR_INVALID_ARG = -1

@@ -77,6 +77,7 @@ struct BfsArgs {
     int resume;              // 1: continue the level loop saved in ctrl->rs
     int max_steps;           // > 0: leave after this many levels (state saved)
     int alpha, beta, big_degree, direction;
+    int has_big;             // some row has big_degree entries or more (else none is ever deferred)
     unsigned long long timeout_ns;
 };
 
@@ -320,6 +321,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
     extern __shared__ int smem[];
     __shared__ unsigned long long s_red[32];
     __shared__ unsigned long long s_base;
+    __shared__ unsigned long long s_cd;
+    __shared__ unsigned s_nb;
     __shared__ int s_warp[33];
     __shared__ int s_wq[33];
     constexpr int NW = BLOCK / 32;
@@ -357,11 +360,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
             a.visited[w] = z;
             a.fb[0][w] = 0;
             a.fb[1][w] = 0;
+            a.fb[2][w] = 0;
         }
         if (root >= 0 && gtid == 0) {
             a.q0[0] = root;
-            ctrl->cnt[0] = 1;
-            ctrl->deg[0] = (unsigned long long)(__ldg(a.row + root + 1) - __ldg(a.row + root));
+            ctrl->cd[0] = cd_pack(1, (unsigned long long)(__ldg(a.row + root + 1) - __ldg(a.row + root)));
         }
         if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
         if (root >= 0) {
@@ -372,10 +375,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                     const int r = a.roots[i];
                     if (atomicCAS(&a.level[r], -1, 0) == -1) {
                         atomicOr(&a.visited[r >> 5], 1u << (r & 31));
-                        unsigned long long pos = atomicAdd(&ctrl->cnt[0], 1ull);
+                        const unsigned long long d = (unsigned long long)(__ldg(a.row + r + 1) - __ldg(a.row + r));
+                        const unsigned long long pos = cd_count(atomicAdd(&ctrl->cd[0], cd_pack(1, d)));
                         a.q0[pos] = r;
-                        atomicAdd(&ctrl->deg[0],
-                                  (unsigned long long)(__ldg(a.row + r + 1) - __ldg(a.row + r)));
                     }
                 }
             }
@@ -393,6 +395,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
     bool td = true;
     bool fn_set = false;  // the last top-down step marked its finds in fn
     unsigned long long prev_mf = 0;  // the last level's frontier edges
+    // Frontier bitmaps that may hold set bits (bit i: fb[i]); a bitmap is
+    // cleared two levels before it is next written only if it is dirty, so
+    // levels that never touch the bitmaps (top-down steps without marking)
+    // write none of them.  All three are zero after initialisation.
+    unsigned dirty = 0;
     if (a.resume) {
         const BfsResume r = ctrl->rs;
         m_u = r.m_u;
@@ -404,6 +411,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
         td_levels = r.td_levels;
         bu_levels = r.bu_levels;
         td = r.td != 0;
+        dirty = (unsigned)r.dirty;
     }
     for (int steps = 0;; ++steps) {
         if (a.max_steps > 0 && steps == a.max_steps) {
@@ -420,14 +428,18 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                 r.bu_levels = bu_levels;
                 r.td = td ? 1 : 0;
                 r.done = 0;
-                r.pad = 0;
+                r.dirty = (int)dirty;
                 ctrl->rs = r;
             }
             grid_exit(&ctrl->bar, &ctrl->t_exit);
             return;
         }
-        const unsigned long long nf = ld_relaxed_u64(&ctrl->cnt[L % 3]);
-        const unsigned long long mf = ld_relaxed_u64(&ctrl->deg[L % 3]);
+        // the frontier's count and degree sum: one load per CTA, shared
+        if (threadIdx.x == 0) s_cd = ld_relaxed_u64(&ctrl->cd[L % 3]);
+        __syncthreads();
+        const unsigned long long cdv = s_cd;
+        const unsigned long long nf = cd_count(cdv);
+        const unsigned long long mf = cd_degree(cdv);
         if (nf == 0) break;
         if (L == 0) roots = nf;
         reached += nf;
@@ -445,14 +457,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
         unsigned *fc = a.fb[L % 3];
         unsigned *fn = a.fb[(L + 1) % 3];
         unsigned *fz = a.fb[(L + 2) % 3];   // zeroed now: the next level's fn
-        unsigned long long *cnt_next = &ctrl->cnt[(L + 1) % 3];
-        unsigned long long *deg_next = &ctrl->deg[(L + 1) % 3];
+        unsigned long long *cnt_next = &ctrl->cd[(L + 1) % 3];  // count | degree sum of frontier L+1
         const int nl = L + 1;
+        const unsigned bit_c = 1u << (L % 3), bit_n = 1u << ((L + 1) % 3), bit_z = 1u << ((L + 2) % 3);
 
         bool traced_big = false;
         if (gtid == 0) {
-            ctrl->cnt[(L + 2) % 3] = 0;
-            ctrl->deg[(L + 2) % 3] = 0;
+            ctrl->cd[(L + 2) % 3] = 0;
             ctrl->big[(L + 1) % 3] = 0;
         }
 
@@ -463,6 +474,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                 const int v = __ldcg(qc + i);
                 atomicOr(&fc[v >> 5], 1u << (v & 31));
             }
+            dirty |= bit_c;
             if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
         }
         // back to top-down with few frontier edges: expand the frontier
@@ -475,7 +487,10 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
         }
         td = !bu;
 
-        for (long long w = gtid; w < W; w += gthreads) fz[w] = 0;
+        if (dirty & bit_z) {
+            for (long long w = gtid; w < W; w += gthreads) fz[w] = 0;
+            dirty &= ~bit_z;
+        }
         if (td) {
             ++td_levels;
             if (gtid == 0) ctrl->fill = 0;
@@ -507,26 +522,29 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                     expand_lane_rows(v, b, d, a, nl, q, cnt_next, qn, my_deg, &ctrl->big[L % 3], lane, fnw);
                 }
             }
-            block_flush(q, cnt_next, qn, s_wq, &s_base);
-            {
-                const unsigned long long bd = block_reduce_sum(my_deg, s_red);
-                if (threadIdx.x == 0 && bd) atomicAdd(deg_next, bd);
-            }
+            block_flush_packed(q, cnt_next, qn, my_deg, s_wq, s_red, &s_base);
             if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
 
-            const int nb = nf > (unsigned long long)SEG || from_bitmap ? (int)__ldcg(&ctrl->big[L % 3]) : 0;
+            // rows deferred to the grid pass (only large frontiers defer, and
+            // only when some row is that long)
+            int nb = 0;
+            if (a.has_big && (nf > (unsigned long long)SEG || from_bitmap)) {
+                if (threadIdx.x == 0) s_nb = __ldcg(&ctrl->big[L % 3]);
+                __syncthreads();
+                nb = (int)s_nb;
+            }
             traced_big = nb > 0;
             if (nb > 0) {
                 my_deg = 0;
                 grid_expand_list<BLOCK>(a.bigl, nb, a, nl, q, cnt_next, qn, my_deg, s_pre, s_beg, s_warp, fnw, true);
-                block_flush(q, cnt_next, qn, s_wq, &s_base);
-                const unsigned long long bd = block_reduce_sum(my_deg, s_red);
-                if (threadIdx.x == 0 && bd) atomicAdd(deg_next, bd);
+                block_flush_packed(q, cnt_next, qn, my_deg, s_wq, s_red, &s_base);
                 if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
             }
             fn_set = fnw != nullptr;
+            if (fn_set) dirty |= bit_n;
         } else {
             fn_set = false;
+            dirty |= bit_n;
             ++bu_levels;
             unsigned long long my_cnt = 0, my_deg = 0;
             // A warp takes chunks of cw bitmap words and probes the chunk's
@@ -807,10 +825,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                     __syncwarp();
                 }
             }
-            const unsigned long long bc = block_reduce_sum(my_cnt, s_red);
-            if (threadIdx.x == 0 && bc) atomicAdd(cnt_next, bc);
-            const unsigned long long bd = block_reduce_sum(my_deg, s_red);
-            if (threadIdx.x == 0 && bd) atomicAdd(deg_next, bd);
+            // both sums below 2^32 per block, so they add packed
+            const unsigned long long bcd = block_reduce_sum(cd_pack(my_cnt, my_deg), s_red);
+            if (threadIdx.x == 0 && bcd) atomicAdd(cnt_next, bcd);
             if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
         }
         prev_mf = mf;
@@ -839,8 +856,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
         *a.out = o;
         ctrl->rs.done = 1;
         for (int i = 0; i < 3; i++) {
-            ctrl->cnt[i] = 0;
-            ctrl->deg[i] = 0;
+            ctrl->cd[i] = 0;
             ctrl->big[i] = 0;
         }
         ctrl->fill = 0;
@@ -1041,6 +1057,7 @@ BfsArgs make_args(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const in
     a.beta = std::max(1, p.beta);
     a.big_degree = std::max(32, p.big_degree);
     a.direction = p.direction;
+    a.has_big = g.max_degree >= a.big_degree ? 1 : 0;
     a.timeout_ns = (unsigned long long)std::max(1, p.timeout_ms) * 1000000ull;
     return a;
 }

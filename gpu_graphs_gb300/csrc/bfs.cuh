@@ -33,15 +33,25 @@ struct BfsOut {
 struct BfsResume {
     long long m_u;
     unsigned long long prev_nf, reached, edges_c, roots;
-    int L, td_levels, bu_levels, td, done, pad;
+    int L, td_levels, bu_levels, td, done, dirty;  // dirty: frontier bitmaps that may hold set bits
 };
+
+// A frontier's vertex count and out-degree sum share one 64-bit word (count
+// in the low half, degree sum in the high half: both below 2^31, so the
+// halves never carry into each other), so a CTA adds both, and gets its
+// queue slots, with one atomic.
+__host__ __device__ inline unsigned long long cd_pack(unsigned long long cnt, unsigned long long deg)
+{
+    return (deg << 32) | cnt;
+}
+__host__ __device__ inline unsigned long long cd_count(unsigned long long cd) { return cd & 0xffffffffull; }
+__host__ __device__ inline unsigned long long cd_degree(unsigned long long cd) { return cd >> 32; }
 
 struct BfsCtrl {
     GridBarrier bar;
     int status;
     int pad0;
-    unsigned long long cnt[3];   // frontier vertex counts, rotating by level
-    unsigned long long deg[3];   // frontier out-degree sums, rotating by level
+    unsigned long long cd[3];    // frontier count | out-degree sum (cd_pack), rotating by level
     unsigned big[3];             // top-down rows deferred to the grid pass
     unsigned pad1;
     unsigned long long fill;     // bitmap -> queue conversion slots

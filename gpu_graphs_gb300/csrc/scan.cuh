@@ -2,16 +2,18 @@
 //
 // Replaces the reference's three-launch recursive Blelloch scan
 // (2D Partition/src/prefixSum.cu:15-224, which cudaMallocs and frees its
-// block-sum arrays on every call) with one launch: each tile of
-// SCAN_THREADS * SCAN_ITEMS elements is staged through shared memory (loads
-// and stores coalesced), scans itself with warp shuffles, publishes its
-// aggregate, looks back over its predecessors' published aggregates /
-// inclusive prefixes 32 at a time (one warp), and publishes its inclusive
-// prefix.
-// Tiles take ids from an atomic counter in launch order, so a tile only
-// ever waits on tiles that are already running.  The scratch is
-// self-cleaning (epoch-tagged flags, counters reset by the last tile), so
-// repeated calls need no memset.
+// block-sum arrays on every call) with one launch, one CTA per tile of
+// SCAN_TILE elements: the tile is bulk-copied (TMA) into shared memory, each
+// warp reads its run of consecutive elements as 16-byte vectors interleaved
+// by lane, the tile publishes its aggregate, looks back over its
+// predecessors' published aggregates / inclusive prefixes (the whole CTA,
+// 256 predecessors per step, one round trip each: value and status share a
+// 16-byte word), publishes its inclusive prefix and writes its outputs from
+// registers as 16-byte coalesced stores.  Small shared memory and few
+// registers keep several tiles in flight per SM.
+// A tile waits only on tiles with smaller indices, which start first.  The
+// tile states carry a call number (epoch), so repeated calls need no
+// clearing of them.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -19,15 +21,21 @@
 
 namespace gbfs {
 
-constexpr int SCAN_THREADS = 1024;
-constexpr int SCAN_ITEMS = 16;
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 32;      // elements per thread (SCAN_TILE = 8192)
+constexpr int SCAN_MIN_BLOCKS = 6;  // CTAs per SM the register budget is sized for
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
+// A tile's published aggregate or inclusive prefix and its status,
+// (call number << 2) | {1 aggregate, 2 inclusive}, in one 16-byte word.
+struct alignas(16) ScanDesc {
+    long long value;
+    unsigned long long status;
+};
+
 struct ScanScratch {
-    unsigned *flags = nullptr;      // per tile: (epoch << 2) | {1 agg, 2 inclusive}
-    long long *agg = nullptr;       // per tile aggregate
-    long long *inc = nullptr;       // per tile inclusive prefix
-    unsigned *ctl = nullptr;        // [0] tile ticket, [1] tiles done, [2] status
+    ScanDesc *desc = nullptr;       // per tile
+    unsigned *ctl = nullptr;        // [2] status (a bounded wait ran out); [0], [1] unused
     int64_t max_tiles = 0;
     unsigned epoch = 0;             // host-side call counter
 };

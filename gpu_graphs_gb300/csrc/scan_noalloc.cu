@@ -15,9 +15,9 @@
 // that loads the library until the process exits, the input is limited to
 // GBFS_SCAN_NOALLOC_MAX_N elements, and all calls share the array, so
 // calls whose work overlaps on the GPU (other streams, other threads) race
-// and must be serialised by the caller.  What must start at zero (the tile
-// ticket, done and status counters) is cleared by every call; the per-tile
-// flags carry a call number, so the previous call's contents are ignored.
+// and must be serialised by the caller.  What must start at zero (the
+// status word) is cleared by every call; the per-tile states carry a call
+// number, so the previous call's contents are ignored.
 #include <mutex>
 
 #include "../../include/gbfs.h"
@@ -29,7 +29,7 @@ namespace {
 constexpr int64_t NOALLOC_TILES = (GBFS_SCAN_NOALLOC_MAX_N + gbfs::SCAN_TILE - 1) / gbfs::SCAN_TILE;
 constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 // Same carving as gbfs::scan_scratch_bytes(NOALLOC_TILES).
-constexpr size_t NOALLOC_BYTES = 256 + align256(NOALLOC_TILES * 4) + 2 * align256(NOALLOC_TILES * 8);
+constexpr size_t NOALLOC_BYTES = 256 + align256(NOALLOC_TILES * sizeof(gbfs::ScanDesc));
 
 static __device__ __align__(256) unsigned char g_scan_scratch[NOALLOC_BYTES];
 
