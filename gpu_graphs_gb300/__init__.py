@@ -198,11 +198,12 @@ class Graph:
     def last_trace(self) -> list[dict]:
         """Per-level trace of the last traversal: level, direction, frontier
         size and edges, and the step's end time in us after initialisation."""
-        rows = (_lib.LevelTrace * 1024)()
-        k = lib.gbfs_last_trace(self._h, C.cast(rows, C.c_void_p), 1024)
+        cap = 16384 + 3
+        rows = (_lib.LevelTrace * cap)()
+        k = lib.gbfs_last_trace(self._h, C.cast(rows, C.c_void_p), cap)
         if k < 0:
             raise GbfsError(k, "gbfs_last_trace")
-        dirs = {-3: "exit", -2: "end", -1: "init", 0: "td", 1: "bu", 2: "td+split"}
+        dirs = {-3: "exit", -2: "end", -1: "init", 0: "td", 1: "bu", 2: "td+split", 4: "td-cluster"}
         return [{"level": r.level, "dir": dirs.get(r.direction, str(r.direction)), "frontier": r.frontier_vertices,
                  "edges": r.frontier_edges, "t_us": round(r.t_us, 2)} for r in rows[:k]]
 

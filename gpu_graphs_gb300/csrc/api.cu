@@ -478,7 +478,7 @@ extern "C" int gbfs_bfs_many(gbfs_graph *g, const int32_t *sources, int32_t k, i
             r.levels = o.levels;
             r.td_levels = o.td_levels;
             r.bu_levels = o.bu_levels;
-            r.launches = 1;
+            r.launches = bfs_launches_per_search(g->csr, p);
             r.reached = (int64_t)o.reached;
             r.edges_c = (int64_t)o.edges_c;
             fill_stats(&stats[i], r, 1);

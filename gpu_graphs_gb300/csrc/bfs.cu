@@ -41,6 +41,7 @@
 #include <cstring>
 
 #include "bfs.cuh"
+#include "bfs_args.cuh"
 #include "blockq.cuh"
 
 namespace gbfs {
@@ -52,34 +53,21 @@ constexpr int ILP = 4;       // edges in flight per lane in top-down passes
 constexpr int PROBE = 8;     // neighbours probed per step in bottom-up
 constexpr int BU_DEF = 192;  // deferred bottom-up rows per warp: under 64 left plus a 128-vertex round (<= QCAP)
 constexpr unsigned long long BMTD_EDGES = 65536;  // top-down from the bitmap up to this many frontier edges
-
-struct BfsArgs {
-    int n;
-    int n_active;            // non-isolated vertices (for beta)
-    long long m;
-    const int *row;
-    const int *col;
-    const int *brow, *bcol;  // bottom-up adjacency: in-edges (row/col when symmetric)
-    const int *bfirst;       // first entry of each brow row (-1: empty row)
-    const int *bsecond;      // second entries (-1 past the end); null: probe the first alone
-    const unsigned *zmask;   // out-degree-0 bitmap, or NULL (directed graphs:
-                             // a sink still has in-edges, so it stays claimable)
-    int *level;
-    unsigned *visited;
-    unsigned *fb[3];         // frontier bitmaps, rotating by level
-    int *q0, *q1;            // frontier queues
-    int *bigl;
-    BfsCtrl *ctrl;
-    BfsOut *out;
-    const int *roots;
-    int nroots;
-    int single_root;         // >= 0: fast init for one root
-    int resume;              // 1: continue the level loop saved in ctrl->rs
-    int max_steps;           // > 0: leave after this many levels (state saved)
-    int alpha, beta, big_degree, direction;
-    int has_big;             // some row has big_degree entries or more (else none is ever deferred)
-    unsigned long long timeout_ns;
-};
+// Sparse phase (bfs_sparse.cu): used on graphs whose largest out-degree is
+// at most SPARSE_MAX_DEGREE (meshes, grids, road networks: long searches of
+// small frontiers), from level SPARSE_YIELD_LEVEL on, for frontiers of up
+// to SPARSE_ENTER_F vertices, until one exceeds SPARSE_LEAVE_F.  Measured
+// on the 7000 x 7000 grid, a level costs the grid kernel 9.3-9.5 us for
+// frontiers of 2 k to 14 k vertices and the 16-CTA cluster 5.5 us below
+// 1 k, 6.8 us at 2-4 k, 9.7 us at 6-8 k: the two cross near 6.5 k.
+// SPARSE_PHASES bounds the hand-overs: a search is queued as grid launch,
+// then (cluster launch, grid launch) SPARSE_PHASES times, and a launch
+// with nothing left to do returns at once.
+constexpr int SPARSE_MAX_DEGREE = 16;
+constexpr int SPARSE_YIELD_LEVEL = 16;
+constexpr int SPARSE_ENTER_F = 4000;
+constexpr int SPARSE_LEAVE_F = 6500;
+constexpr int SPARSE_PHASES = 2;
 
 // Top-down claim of ILP neighbours per lane, all loads and atomics issued
 // before any result is used.  w[j] < 0 means "no edge".  A vertex is won by
@@ -341,7 +329,15 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
     BfsCtrl *ctrl = a.ctrl;
     WarpQ q{s_q + (threadIdx.x >> 5) * QCAP, 0};
     unsigned epoch = 0;
-    if (gtid == 0) ctrl->t_entry = globaltimer_ns();
+    if (a.resume) {
+        // a continuation: nothing to do when the search has ended or failed,
+        // or when it was handed to the sparse-phase kernel and that kernel
+        // did not take it (it only declines after a device error)
+        const int done = ctrl->rs.done, mode = ctrl->rs.mode, status = ctrl->status;
+        if (done || mode == RESUME_SPARSE || status != DEV_OK) return;
+    } else if (gtid == 0) {
+        ctrl->t_entry = globaltimer_ns();
+    }
 
     // ---- init ----------------------------------------------------------
     if (!a.resume) {
@@ -412,26 +408,35 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
         bu_levels = r.bu_levels;
         td = r.td != 0;
         dirty = (unsigned)r.dirty;
+        prev_mf = r.prev_mf;
     }
+    // park the loop state at the top of level L for the launch that
+    // continues it (mode: ResumeMode)
+    auto park = [&](int mode) {
+        if (gtid == 0) {
+            BfsResume r;
+            r.m_u = m_u;
+            r.prev_nf = prev_nf;
+            r.reached = reached;
+            r.edges_c = edges_c;
+            r.roots = roots;
+            r.prev_mf = prev_mf;
+            r.L = L;
+            r.td_levels = td_levels;
+            r.bu_levels = bu_levels;
+            r.td = td ? 1 : 0;
+            r.done = 0;
+            r.dirty = (int)dirty;
+            r.mode = mode;
+            r.pad = 0;
+            ctrl->rs = r;
+        }
+        grid_exit(&ctrl->bar, &ctrl->t_exit);
+    };
     for (int steps = 0;; ++steps) {
         if (a.max_steps > 0 && steps == a.max_steps) {
             // per-level-launch mode: park the loop state for the next launch
-            if (gtid == 0) {
-                BfsResume r;
-                r.m_u = m_u;
-                r.prev_nf = prev_nf;
-                r.reached = reached;
-                r.edges_c = edges_c;
-                r.roots = roots;
-                r.L = L;
-                r.td_levels = td_levels;
-                r.bu_levels = bu_levels;
-                r.td = td ? 1 : 0;
-                r.done = 0;
-                r.dirty = (int)dirty;
-                ctrl->rs = r;
-            }
-            grid_exit(&ctrl->bar, &ctrl->t_exit);
+            park(RESUME_LEVEL);
             return;
         }
         // the frontier's count and degree sum: one load per CTA, shared
@@ -450,6 +455,17 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
         else if (a.direction == GBFS_DIR_BOTTOMUP) bu = true;
         else if (td) bu = (long long)mf * a.alpha > m_u;
         else bu = !((long long)nf * a.beta < a.n_active && nf < prev_nf);
+        // a long run of small top-down frontiers (a high-diameter graph):
+        // hand the loop to the sparse-phase cluster kernel queued after
+        // this launch, with frontier L still in its queue
+        if (a.may_yield && td && !bu && L >= a.yield_level && nf <= (unsigned long long)a.sparse_enter_f &&
+            (long long)((nf + a.sparse_ctas - 1) / a.sparse_ctas) * a.max_degree <= a.sparse_cap) {
+            reached -= nf;
+            edges_c -= mf;
+            m_u += (long long)mf;
+            park(RESUME_SPARSE);
+            return;
+        }
         prev_nf = nf;
 
         int *qc = (L & 1) ? a.q1 : a.q0;
@@ -855,6 +871,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
         o.edges_c = edges_c;
         *a.out = o;
         ctrl->rs.done = 1;
+        ctrl->rs.mode = RESUME_LEVEL;
         for (int i = 0; i < 3; i++) {
             ctrl->cd[i] = 0;
             ctrl->big[i] = 0;
@@ -1058,6 +1075,13 @@ BfsArgs make_args(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const in
     a.big_degree = std::max(32, p.big_degree);
     a.direction = p.direction;
     a.has_big = g.max_degree >= a.big_degree ? 1 : 0;
+    a.max_degree = std::max(1, (int)g.max_degree);
+    a.may_yield = 0;
+    a.yield_level = SPARSE_YIELD_LEVEL;
+    a.sparse_ctas = 1;
+    a.sparse_cap = 0;
+    a.sparse_enter_f = SPARSE_ENTER_F;
+    a.sparse_leave_f = SPARSE_LEAVE_F;
     a.timeout_ns = (unsigned long long)std::max(1, p.timeout_ms) * 1000000ull;
     return a;
 }
@@ -1145,12 +1169,48 @@ cudaError_t add_bfs_node(cudaGraph_t g, const cudaGraphNode_t *dep, size_t ndep,
 
 }  // namespace
 
+int bfs_sparse_ctas(const DeviceCsr &g, const gbfs_params &p)
+{
+    if (p.per_level_launch || p.direction == GBFS_DIR_BOTTOMUP || g.max_degree > SPARSE_MAX_DEGREE) return 0;
+    int ctas = 0, cap = 0;
+    if (bfs_sparse_shape(ctas, cap) != cudaSuccess) return 0;
+    return ctas;
+}
+
+int bfs_launches_per_search(const DeviceCsr &g, const gbfs_params &p)
+{
+    return bfs_sparse_ctas(g, p) > 0 ? 1 + 2 * SPARSE_PHASES : 1;
+}
+
 cudaError_t bfs_enqueue(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_roots, int k,
                         int single_root, int *d_level, BfsOut *slot, cudaStream_t st, bool symmetric, int resume,
                         int max_steps, int max_ctas)
 {
     BfsArgs a = make_args(g, p, w, d_roots, k, single_root, d_level, slot, symmetric, resume, max_steps);
-    return bfs_launch_any(a, p.threads_per_block, p.blocks_per_sm, st, max_ctas);
+    if (resume || max_steps || bfs_sparse_ctas(g, p) == 0)
+        return bfs_launch_any(a, p.threads_per_block, p.blocks_per_sm, st, max_ctas);
+    // a graph of small degree: the grid kernel may hand runs of small
+    // frontiers to the sparse-phase cluster kernel queued behind it, which
+    // hands larger ones back to the resuming grid launch behind it, and so
+    // on SPARSE_PHASES times (the last grid launch keeps the search); every
+    // later launch returns at once when the search is already complete
+    int ctas = 0, cap = 0;
+    cudaError_t e = bfs_sparse_shape(ctas, cap);
+    if (e != cudaSuccess) return e;
+    a.may_yield = 1;
+    a.sparse_ctas = ctas;
+    a.sparse_cap = cap;
+    e = bfs_launch_any(a, p.threads_per_block, p.blocks_per_sm, st, max_ctas);
+    for (int ph = 0; ph < SPARSE_PHASES && e == cudaSuccess; ph++) {
+        e = bfs_sparse_launch(a, st);
+        if (e == cudaSuccess) {
+            BfsArgs r = a;
+            r.resume = 1;
+            r.may_yield = ph + 1 < SPARSE_PHASES ? 1 : 0;
+            e = bfs_launch_any(r, p.threads_per_block, p.blocks_per_sm, st, max_ctas);
+        }
+    }
+    return e;
 }
 
 void bfs_graph_free(BfsWork &w)
@@ -1255,7 +1315,7 @@ int bfs_run(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_r
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // single_root lives on this stack frame
     }
     if (e == cudaSuccess) e = cudaEventRecord(w.ev0, st);
-    int launches = 1;
+    int launches = bfs_launches_per_search(g, p);
     if (p.per_level_launch == 2) {
         if (e == cudaSuccess) e = bfs_graph_launch(g, p, w, d_roots ? k : 1, d_level, st, symmetric);
         launches = -1;  // the graph's own launches: levels + 1, filled in below
@@ -1286,8 +1346,13 @@ int bfs_run(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_r
     }
     const BfsCtrl &h = *w.h_ctrl;
     if (h.status != DEV_OK) {
+        const int status = h.status;
         cudaMemsetAsync(w.ctrl, 0, sizeof(BfsCtrl), st);
         cudaStreamSynchronize(st);
+        if (status == DEV_OVERFLOW) {
+            err = "an on-chip frontier queue overflowed";
+            return GBFS_ERR_CUDA;
+        }
         err = "a device-side wait ran out (grid barrier)";
         return GBFS_ERR_TIMEOUT;
     }

@@ -16,12 +16,13 @@ namespace gbfs {
 // One row of the per-level trace (thread 0 writes it after the level's barrier).
 struct LevelTrace {
     int level;                   // frontier index L expanded by this step
-    int dir;                     // 0 top-down, 1 bottom-up, +2 if a grid-split pass ran
+    int dir;                     // 0 top-down, 1 bottom-up, +2 if a grid-split pass ran,
+                                 // 4 top-down in the sparse-phase cluster kernel
     unsigned long long frontier; // vertices in frontier L
     unsigned long long edges;    // their out-edges
     unsigned long long t_ns;     // %globaltimer when the step's last barrier completed
 };
-constexpr int TRACE_CAP = 1024;  // levels kept (the first TRACE_CAP - 1, then the last)
+constexpr int TRACE_CAP = 16384;  // levels kept (the first TRACE_CAP - 1, then the last)
 
 // Results of one traversal, written by the kernel's thread 0.
 struct BfsOut {
@@ -29,11 +30,20 @@ struct BfsOut {
     unsigned long long reached, edges_c;
 };
 
-// Level-loop state kept between launches in per-level-launch mode.
+// Who continues a parked level loop (BfsResume::mode).
+enum ResumeMode : int {
+    RESUME_LEVEL = 0,     // per-level-launch mode: the next grid launch
+    RESUME_SPARSE = 1,    // the sparse-phase cluster kernel
+    RESUME_HANDBACK = 2,  // the grid kernel again, after the sparse phase
+};
+
+// Level-loop state kept between launches (per-level-launch mode, and the
+// hand-over between the grid kernel and the sparse-phase cluster kernel).
 struct BfsResume {
     long long m_u;
-    unsigned long long prev_nf, reached, edges_c, roots;
+    unsigned long long prev_nf, reached, edges_c, roots, prev_mf;
     int L, td_levels, bu_levels, td, done, dirty;  // dirty: frontier bitmaps that may hold set bits
+    int mode, pad;                                 // mode: ResumeMode
 };
 
 // A frontier's vertex count and out-degree sum share one 64-bit word (count
@@ -129,6 +139,12 @@ cudaError_t bfs_enqueue(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, co
 // level count after each (the reference's loop shape).
 int bfs_run(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_roots, int k,
             int single_root, int *d_level, cudaStream_t st, BfsResult &res, std::string &err, bool symmetric);
+
+// Cluster CTAs of the sparse-phase kernel a search with these parameters
+// may use on graph g (0: single persistent launches only), and the kernel
+// launches one search enqueues (1, or 3 with the sparse phase).
+int bfs_sparse_ctas(const DeviceCsr &g, const gbfs_params &p);
+int bfs_launches_per_search(const DeviceCsr &g, const gbfs_params &p);
 
 // CTAs of one full-GPU single-source launch with these parameters (0 on error).
 int bfs_max_ctas(const gbfs_params &p);

@@ -202,6 +202,7 @@ enum DevStatus : int {
     DEV_OK = 0,
     DEV_TIMEOUT = 1,   // a bounded wait ran out
     DEV_BAD_ID = 2,    // an input id outside [0, n)
+    DEV_OVERFLOW = 3,  // a bounded on-chip queue would have overflowed
 };
 
 // ---- bounded grid barrier ---------------------------------------------------

@@ -204,13 +204,16 @@ int gbfs_bfs_many(gbfs_graph *g, const int32_t *sources, int32_t k,
 typedef struct gbfs_level_trace {
     int32_t level;              /* frontier expanded by this step            */
     int32_t direction;          /* 0 top-down, 1 bottom-up, 2 top-down with
-                                   a grid-split pass over long rows          */
+                                   a grid-split pass over long rows, 4
+                                   top-down on one thread-block cluster
+                                   (the sparse phase of small-degree graphs) */
     int64_t frontier_vertices;
     int64_t frontier_edges;     /* out-edges of the frontier                 */
     double  t_us;               /* end of the step, us after initialisation  */
 } gbfs_level_trace;
 
-/* Copies up to cap rows; returns the number of rows (>= 0) or a status.
+/* Copies up to cap rows (up to 16,384 levels are kept: the first 16,383
+ * and the last); returns the number of rows (>= 0) or a status.
  * Row 0 describes initialisation: level -1, t_us = minus its duration
  * (from the first CTA's entry to the first level).  Then one row per level,
  * then a row with level -2 marking the end of the level loop (termination

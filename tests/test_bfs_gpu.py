@@ -101,8 +101,11 @@ def test_grid_high_diameter(gb, orc):
     src, dst = gb.gen_grid(side, 0.1, 0.001, 8, seed=3)
     g, o = _check_against_oracle(gb, orc, side * side, src, dst, [0, side * side // 2 + 7])
     want, st = g.bfs(0, stats=True)
-    assert st.levels > side  # hundreds of levels in one persistent launch
-    assert st.launches == 1
+    assert st.levels > side  # hundreds of levels
+    # degree <= 16: the persistent grid launch hands the small frontiers to
+    # the sparse-phase cluster launch queued behind it (grid, cluster, grid,
+    # cluster, grid; launches with nothing left return at once)
+    assert st.launches == 5
     g.set_params(per_level_launch=1)  # the reference's shape: a launch per level
     got, st2 = g.bfs(0, stats=True)
     assert np.array_equal(got, want)
@@ -381,3 +384,60 @@ def test_back_to_back_launches(gb, orc, out_kind):
             if out is not None:
                 row = got[i].cpu().numpy() if out_kind == "device" else got[i]
                 assert np.array_equal(row, want), (out_kind, i)
+
+
+def _bounded_degree_graph(n_path: int, n_exp: int, seed: int):
+    """A path of n_path vertices (0 .. n_path-1) ending in a random graph of
+    degree <= 3 on n_exp vertices (three random perfect matchings): from
+    vertex 0 the frontier stays at one vertex for n_path levels, then roughly
+    doubles each level."""
+    rng = np.random.default_rng(seed)
+    src = list(range(n_path - 1))
+    dst = list(range(1, n_path))
+    src.append(n_path - 1)
+    dst.append(n_path)
+    for _ in range(3):
+        perm = rng.permutation(n_exp) + n_path
+        src.extend(perm[0::2][: n_exp // 2].tolist())
+        dst.extend(perm[1::2][: n_exp // 2].tolist())
+    return n_path + n_exp, np.array(src, np.int32), np.array(dst, np.int32)
+
+
+@pytest.mark.parametrize("direction", [0, 1])
+def test_sparse_phase_hands_back(gb, orc, direction):
+    """The sparse phase takes over on a long thin start (level 16 on), then
+    the frontier outgrows the cluster's queues and the grid kernel resumes
+    (and may step bottom-up); levels stay exact from several sources."""
+    n, src, dst = _bounded_degree_graph(40, 1 << 20, 7)
+    g = gb.Graph.from_edges(n, src, dst, gb.UNDIRECTED)
+    assert g.max_degree <= 16
+    g.set_params(direction=direction)
+    o = orc.csr_build(n, src, dst, orc.UNDIRECTED)
+    for s0 in (0, 5, 39, 40 + 12345, n - 1):
+        got, st = g.bfs(s0, stats=True)
+        assert np.array_equal(got, orc.bfs_queue(o, s0)), s0
+        assert st.launches == 5
+        assert st.vertices_reached == int((got >= 0).sum())
+    # back-to-back launches and a device output buffer
+    sources = [0, 40 + 7, 3]
+    outs, sts = g.bfs_many(sources)
+    for i, s0 in enumerate(sources):
+        assert np.array_equal(outs[i], orc.bfs_queue(o, s0))
+
+
+def test_sparse_phase_multiroot_and_directed(gb, orc):
+    side = 300
+    src, dst = gb.gen_grid(side, 0.1, 0.001, 8, seed=11)
+    n = side * side
+    g = gb.Graph.from_edges(n, src, dst, gb.UNDIRECTED)
+    o = orc.csr_build(n, src, dst, orc.UNDIRECTED)
+    roots = [0, n - 1, n // 2]
+    got = g.bfs_multiroot(roots)
+    want = np.min(np.stack([np.where(lv < 0, 1 << 30, lv) for lv in (orc.bfs_queue(o, r) for r in roots)]), axis=0)
+    want = np.where(want == 1 << 30, -1, want).astype(np.int32)
+    assert np.array_equal(got, want)
+    # the grid as stored (directed: in-edges from a transpose for bottom-up)
+    gd = gb.Graph.from_edges(n, src, dst, gb.DEDUP | gb.DROP_SELF_LOOPS)
+    od = orc.csr_build(n, src, dst, orc.DEDUP | orc.DROP_SELF_LOOPS)
+    for s0 in (0, n // 3):
+        assert np.array_equal(gd.bfs(s0), orc.bfs_queue(od, s0))
