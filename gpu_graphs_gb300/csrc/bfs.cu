@@ -57,16 +57,17 @@ constexpr unsigned long long BMTD_EDGES = 65536;  // top-down from the bitmap up
 // at most SPARSE_MAX_DEGREE (meshes, grids, road networks: long searches of
 // small frontiers), from level SPARSE_YIELD_LEVEL on, for frontiers of up
 // to SPARSE_ENTER_F vertices, until one exceeds SPARSE_LEAVE_F.  Measured
-// on the 7000 x 7000 grid, a level costs the grid kernel 9.3-9.5 us for
-// frontiers of 2 k to 14 k vertices and the 16-CTA cluster 5.5 us below
-// 1 k, 6.8 us at 2-4 k, 9.7 us at 6-8 k: the two cross near 6.5 k.
+// on the 7000 x 7000 grid, a level costs the grid kernel 9.3-9.7 us for
+// frontiers of 2 k to 14 k vertices and the 16-CTA cluster 5.2 us below
+// 1 k, 6.5 us at 2-4 k, 7.7 us at 4-6 k, 8.8 us at 6-8 k: the two cross
+// near 9 k.
 // SPARSE_PHASES bounds the hand-overs: a search is queued as grid launch,
 // then (cluster launch, grid launch) SPARSE_PHASES times, and a launch
 // with nothing left to do returns at once.
 constexpr int SPARSE_MAX_DEGREE = 16;
 constexpr int SPARSE_YIELD_LEVEL = 16;
-constexpr int SPARSE_ENTER_F = 4000;
-constexpr int SPARSE_LEAVE_F = 6500;
+constexpr int SPARSE_ENTER_F = 6000;
+constexpr int SPARSE_LEAVE_F = 8500;
 constexpr int SPARSE_PHASES = 2;
 
 // Top-down claim of ILP neighbours per lane, all loads and atomics issued

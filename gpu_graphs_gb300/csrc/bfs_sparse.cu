@@ -15,15 +15,15 @@
 //   * a level ends with the cluster's hardware barrier instead of a global
 //     one, and each CTA learns the level's size from the other CTAs'
 //     counters (also in distributed shared memory);
-//   * each CTA expands the rows of its own queue while the queues stay
-//     balanced (the largest at most 1.5 times the mean: on a mesh each
-//     CTA's part of the wavefront grows with the others'); otherwise the
-//     level's rows are split evenly over the CTAs (rank order of their
-//     queues) and read remotely;
-//   * the graph's degrees are small (at most 16), so a row is one thread's:
-//     its entries four at a time, a plain-load filter on the visited bitmap,
-//     then the atomicOr claim issued with the row-bound loads of the
-//     candidate; the winner writes the level and joins its CTA's queue.
+//   * each CTA expands the rows of its own queue when every queue is short
+//     or the queues are balanced (the longest within 15 % of the mean);
+//     otherwise the level's rows are split evenly over the CTAs (rank order
+//     of their queues) and read remotely;
+//   * small levels (latency-bound) take one row per lane; larger ones, as in
+//     the grid kernel's top-down step, 32 rows per warp as one concatenated
+//     edge range; a plain-load filter on the visited bitmap, then the
+//     atomicOr claim issued with the row-bound loads of the candidate; the
+//     winner writes the level and joins its CTA's queue.
 // The visited bitmap and the level array stay in global memory, so the
 // result is the same array the grid kernel would write.  When a frontier
 // grows past sparse_leave_f vertices (or what the CTAs' queues can hold),
@@ -44,7 +44,9 @@ namespace {
 
 constexpr int SP_BLOCK = 1024;
 constexpr int SP_NW = SP_BLOCK / 32;
-constexpr int SP_ILP = 4;        // row entries in flight per thread
+constexpr int SP_ILP = 4;        // edges in flight per lane
+constexpr unsigned SP_LOCAL_ROWS = 128;  // a CTA expands its own queue when no queue is longer
+constexpr unsigned SP_ROW_F = 2048;      // levels up to this size expand one row per lane
 constexpr int SP_MAX_CTAS = 16;  // largest cluster tried
 constexpr int SP_CAP = 9216;     // queue entries per CTA and level (two levels held: 24 B each)
 
@@ -263,79 +265,119 @@ __global__ void __launch_bounds__(SP_BLOCK, 1) k_bfs_sparse(BfsArgs a)
         if (t == 0) s_cnt[nb] = 0;  // others read it a level ago, before the last cluster barrier
         __syncthreads();
 
-        // this CTA's rows: its own queue while the queues are balanced and
-        // each CTA can hold what its rows may find, else rows
+        // this CTA's rows: its own queue while the queues are balanced (or
+        // all small) and each CTA can hold what its rows may find, else rows
         // [F r / C, F (r + 1) / C) of the concatenated queues
         const unsigned maxcnt = s_maxcnt;
         const unsigned long long even = (F + C - 1) / C;
-        const bool local = 2ull * maxcnt <= 3ull * even && (long long)maxcnt * a.max_degree <= cap;
+        const bool local = (maxcnt <= SP_LOCAL_ROWS || 20ull * maxcnt <= 23ull * even) &&
+                           (long long)maxcnt * a.max_degree <= cap;
         const unsigned long long rlo = local ? 0 : F * r / C;
         const unsigned long long rhi = local ? s_cnt[buf] : F * (r + 1) / C;
         const int2 *lq = qbe0 + buf * cap;
         unsigned long long my_deg = 0;
-        for (unsigned long long i0 = rlo + (unsigned long long)warp * 32; i0 < rhi;
-             i0 += (unsigned long long)SP_NW * 32) {
-            const unsigned long long i = i0 + lane;
-            int b = 0, e = 0;
-            if (i < rhi) {
-                int2 be;
-                if (local) {
-                    be = lq[i];
-                } else {
-                    int o = 0;  // the owner: the last CTA whose segment starts at or before i
+        auto row_bounds = [&](unsigned long long i) -> int2 {
+            if (local) return lq[i];
+            int o = 0;  // the owner: the last CTA whose segment starts at or before i
 #pragma unroll
-                    for (int s = SP_MAX_CTAS / 2; s > 0; s >>= 1)
-                        if (o + s < (int)C && s_off[o + s] <= i) o += s;
-                    const unsigned idx = (unsigned)(i - s_off[o]);
-                    be = ld_dsmem_int2(dsmem_map(&lq[idx], (unsigned)o));
+            for (int s = SP_MAX_CTAS / 2; s > 0; s >>= 1)
+                if (o + s < (int)C && s_off[o + s] <= i) o += s;
+            const unsigned idx = (unsigned)(i - s_off[o]);
+            return ld_dsmem_int2(dsmem_map(&lq[idx], (unsigned)o));
+        };
+        // SP_ILP candidate neighbours per lane (w < 0: none): a plain-load
+        // filter on the visited bitmap, then the claim and the candidate's
+        // row bounds issued together (the bounds of a candidate that loses
+        // the claim are not used); winners write their level and join this
+        // CTA's queue (warp-aggregated appends)
+        auto claim = [&](const int (&w)[SP_ILP]) {
+            unsigned word[SP_ILP], old[SP_ILP];
+#pragma unroll
+            for (int j = 0; j < SP_ILP; j++) word[j] = w[j] >= 0 ? a.visited[w[j] >> 5] : FULL;
+            int2 wb[SP_ILP];
+#pragma unroll
+            for (int j = 0; j < SP_ILP; j++) {
+                const unsigned bit = 1u << (w[j] & 31);
+                old[j] = FULL;
+                wb[j] = make_int2(0, 0);
+                if (!(word[j] & bit)) {
+                    old[j] = atomicOr(&a.visited[w[j] >> 5], bit);
+                    wb[j] = make_int2(__ldg(a.row + w[j]), __ldg(a.row + w[j] + 1));
                 }
-                b = be.x;
-                e = be.y;
             }
-            for (int k0 = b; __any_sync(FULL, k0 < e); k0 += SP_ILP) {
-                int w[SP_ILP];
+            bool won[SP_ILP];
 #pragma unroll
-                for (int j = 0; j < SP_ILP; j++) w[j] = k0 + j < e ? __ldg(a.col + k0 + j) : -1;
-                // a plain-load filter on the visited bitmap, then the claim
-                // and the candidate's row bounds issued together (the bounds
-                // of a candidate that loses the claim are not used)
-                unsigned word[SP_ILP], old[SP_ILP];
+            for (int j = 0; j < SP_ILP; j++) {
+                won[j] = w[j] >= 0 && !((old[j] >> (w[j] & 31)) & 1u);
+                if (won[j]) a.level[w[j]] = nl;
+            }
 #pragma unroll
-                for (int j = 0; j < SP_ILP; j++) word[j] = w[j] >= 0 ? a.visited[w[j] >> 5] : FULL;
-                int2 wb[SP_ILP];
-#pragma unroll
-                for (int j = 0; j < SP_ILP; j++) {
-                    const unsigned bit = 1u << (w[j] & 31);
-                    old[j] = FULL;
-                    wb[j] = make_int2(0, 0);
-                    if (!(word[j] & bit)) {
-                        old[j] = atomicOr(&a.visited[w[j] >> 5], bit);
-                        wb[j] = make_int2(__ldg(a.row + w[j]), __ldg(a.row + w[j] + 1));
+            for (int j = 0; j < SP_ILP; j++) {
+                const unsigned m = __ballot_sync(FULL, won[j]);
+                if (!m) continue;
+                const int leader = __ffs(m) - 1;
+                unsigned pos = 0;
+                if ((int)lane == leader) pos = atomicAdd(&s_cnt[nb], (unsigned)__popc(m));
+                pos = __shfl_sync(FULL, pos, leader) + __popc(m & lanemask_lt());
+                if (won[j]) {
+                    if (pos < (unsigned)cap) {
+                        qbe0[nb * cap + pos] = wb[j];
+                        qv0[nb * cap + pos] = w[j];
+                        my_deg += (unsigned long long)(wb[j].y - wb[j].x);
+                    } else {
+                        atomicCAS(&ctrl->status, DEV_OK, DEV_OVERFLOW);  // never: bounded by the fits rules
                     }
                 }
-                bool won[SP_ILP];
+            }
+        };
+        if (F <= SP_ROW_F) {
+            // a small level (latency-bound): one row per lane, its entries
+            // SP_ILP at a time
+            for (unsigned long long i0 = rlo + (unsigned long long)warp * 32; i0 < rhi;
+                 i0 += (unsigned long long)SP_NW * 32) {
+                const unsigned long long i = i0 + lane;
+                int2 be = make_int2(0, 0);
+                if (i < rhi) be = row_bounds(i);
+                for (int k0 = be.x; __any_sync(FULL, k0 < be.y); k0 += SP_ILP) {
+                    int w[SP_ILP];
 #pragma unroll
-                for (int j = 0; j < SP_ILP; j++) {
-                    won[j] = w[j] >= 0 && !((old[j] >> (w[j] & 31)) & 1u);
-                    if (won[j]) a.level[w[j]] = nl;
+                    for (int j = 0; j < SP_ILP; j++) w[j] = k0 + j < be.y ? __ldg(a.col + k0 + j) : -1;
+                    claim(w);
                 }
+            }
+        } else {
+            // a larger level: the warp's 32 rows as one concatenated edge
+            // range, SP_ILP edges per lane in flight
+            for (unsigned long long i0 = rlo + (unsigned long long)warp * 32; i0 < rhi;
+                 i0 += (unsigned long long)SP_NW * 32) {
+                const unsigned long long i = i0 + lane;
+                int b = 0, e = 0;
+                if (i < rhi) {
+                    const int2 be = row_bounds(i);
+                    b = be.x;
+                    e = be.y;
+                }
+                const int d = e - b;
+                const int incl = warp_incl_scan(d);
+                const int excl = incl - d;
+                const int T = __shfl_sync(FULL, incl, 31);
+                for (int e0 = 0; e0 < T; e0 += 32 * SP_ILP) {
+                    int w[SP_ILP];
 #pragma unroll
-                for (int j = 0; j < SP_ILP; j++) {
-                    const unsigned m = __ballot_sync(FULL, won[j]);
-                    if (!m) continue;
-                    const int leader = __ffs(m) - 1;
-                    unsigned pos = 0;
-                    if ((int)lane == leader) pos = atomicAdd(&s_cnt[nb], (unsigned)__popc(m));
-                    pos = __shfl_sync(FULL, pos, leader) + __popc(m & lanemask_lt());
-                    if (won[j]) {
-                        if (pos < (unsigned)cap) {
-                            qbe0[nb * cap + pos] = wb[j];
-                            qv0[nb * cap + pos] = w[j];
-                            my_deg += (unsigned long long)(wb[j].y - wb[j].x);
-                        } else {
-                            atomicCAS(&ctrl->status, DEV_OK, DEV_OVERFLOW);  // never: bounded by the fits rules
+                    for (int j = 0; j < SP_ILP; j++) {
+                        const int k = e0 + j * 32 + (int)lane;
+                        const int kk = min(k, T - 1);
+                        int lo = 0;
+#pragma unroll
+                        for (int s = 16; s > 0; s >>= 1) {
+                            const int c = lo + s;
+                            if (__shfl_sync(FULL, excl, c) <= kk) lo = c;
                         }
+                        const int ob = __shfl_sync(FULL, b, lo);
+                        const int oe = __shfl_sync(FULL, excl, lo);
+                        w[j] = k < T ? __ldg(a.col + ob + (kk - oe)) : -1;
                     }
+                    claim(w);
                 }
             }
         }
