@@ -51,61 +51,149 @@ namespace {
 constexpr int SEG = 2048;    // frontier rows expanded edge-balanced per pass
 constexpr int ILP = 4;       // edges in flight per lane in top-down passes
 constexpr int PROBE = 8;     // neighbours probed per step in bottom-up
-constexpr int BU_DEF = 192;  // deferred bottom-up rows per warp: under 64 left plus a 128-vertex round (<= QCAP)
+// Per warp, an int2 area of QCAP entries: in top-down steps the row bounds
+// of the warp queue's entries, in bottom-up steps the deferred rows' bounds
+// (under 64 left plus a 128-vertex round)
+constexpr int BU_DEF = QCAP;
 constexpr unsigned long long BMTD_EDGES = 65536;  // top-down from the bitmap up to this many frontier edges
 // Sparse phase (bfs_sparse.cu): used on graphs whose largest out-degree is
 // at most SPARSE_MAX_DEGREE (meshes, grids, road networks: long searches of
 // small frontiers), from level SPARSE_YIELD_LEVEL on, for frontiers of up
 // to SPARSE_ENTER_F vertices, until one exceeds SPARSE_LEAVE_F.  Measured
-// on the 7000 x 7000 grid, a level costs the grid kernel 9.3-9.7 us for
-// frontiers of 2 k to 14 k vertices and the 16-CTA cluster 5.2 us below
-// 1 k, 6.5 us at 2-4 k, 7.7 us at 4-6 k, 8.8 us at 6-8 k: the two cross
-// near 9 k.
+// on the 7000 x 7000 grid, a level costs the grid kernel (one CTA per SM,
+// below) 8.2 us for frontiers of 6 k to 14 k vertices and the 16-CTA
+// cluster 5.2 us below 1 k, 6.4 us at 2-4 k, 7.8 us at 4-6 k, 9.3 us at
+// 6-8 k: the two cross near 5 k.
 // SPARSE_PHASES bounds the hand-overs: a search is queued as grid launch,
 // then (cluster launch, grid launch) SPARSE_PHASES times, and a launch
 // with nothing left to do returns at once.
 constexpr int SPARSE_MAX_DEGREE = 16;
 constexpr int SPARSE_YIELD_LEVEL = 16;
-constexpr int SPARSE_ENTER_F = 6000;
-constexpr int SPARSE_LEAVE_F = 8500;
+constexpr int SPARSE_ENTER_F = 4500;
+constexpr int SPARSE_LEAVE_F = 6000;
+// In such a search the grid kernel runs only the larger, latency-bound
+// frontiers; one CTA per SM halves its barrier and counter traffic (7000^2
+// grid: 53.8 ms against 57.1 ms with two).
+constexpr int SPARSE_GRID_BPS = 1;
 constexpr int SPARSE_PHASES = 2;
 
+// A warp's staging queue whose entries carry their row bounds (row[v],
+// row[v + 1]), so the next level reads a frontier vertex's edge range with
+// the vertex instead of a dependent load of its row offsets.  The frontier
+// queues have a bounds array beside them (qb[0] beside q0, qb[1] beside q1).
+struct WarpQB {
+    int *buf;
+    int2 *bb;
+    int n;
+};
+
+// Append the warp's staged entries to out / outb with one global atomic on
+// the packed counter (its low 32 bits give the position).
+__device__ __forceinline__ void wqb_flush(WarpQB &q, unsigned long long *cnt, int *out, int2 *outb)
+{
+    __syncwarp();
+    if (q.n == 0) return;
+    unsigned long long base = 0;
+    if (lane_id() == 0) base = atomicAdd(cnt, (unsigned long long)q.n) & 0xffffffffull;
+    base = __shfl_sync(FULL, base, 0);
+    for (int i = lane_id(); i < q.n; i += 32) {
+        out[base + i] = q.buf[i];
+        outb[base + i] = q.bb[i];
+    }
+    __syncwarp();
+    q.n = 0;
+}
+
+// All 32 lanes call; lanes with `has` stage v and its row bounds.
+__device__ __forceinline__ void wqb_push(WarpQB &q, bool has, int v, int2 be, unsigned long long *cnt, int *out,
+                                         int2 *outb)
+{
+    const unsigned m = __ballot_sync(FULL, has);
+    if (!m) return;
+    const int c = __popc(m);
+    if (q.n + c > QCAP) wqb_flush(q, cnt, out, outb);
+    if (has) {
+        const int slot = q.n + __popc(m & lanemask_lt());
+        q.buf[slot] = v;
+        q.bb[slot] = be;
+    }
+    q.n += c;
+}
+
+// Flush every warp queue of the block with one global atomic on the packed
+// count | degree counter, adding the block's `hi` values (its vertices'
+// out-degrees) to the high half in the same atomic (all threads call).
+__device__ __forceinline__ void block_flush_bounds(WarpQB &q, unsigned long long *cnt, int *out, int2 *outb,
+                                                   unsigned long long hi, int *s_wq, unsigned long long *s_hi,
+                                                   unsigned long long *s_base)
+{
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const unsigned lane = lane_id();
+    const unsigned long long wh = warp_sum(hi);
+    __syncwarp();
+    if (lane == 0) {
+        s_wq[w] = q.n;
+        s_hi[w] = wh;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const int c = (int)lane < nw ? s_wq[lane] : 0;
+        const unsigned long long h = (int)lane < nw ? s_hi[lane] : 0ull;
+        const int incl = warp_incl_scan(c);
+        const int tot = __shfl_sync(FULL, incl, 31);
+        const unsigned long long htot = warp_sum(h);
+        if ((int)lane < nw) s_wq[lane] = incl - c;
+        if (lane == 0)
+            *s_base = (tot || htot) ? (atomicAdd(cnt, cd_pack((unsigned long long)tot, htot)) & 0xffffffffull) : 0ull;
+    }
+    __syncthreads();
+    const unsigned long long base = *s_base + (unsigned long long)s_wq[w];
+    for (int i = lane; i < q.n; i += 32) {
+        out[base + i] = q.buf[i];
+        outb[base + i] = q.bb[i];
+    }
+    q.n = 0;
+    __syncthreads();
+}
+
 // Top-down claim of ILP neighbours per lane, all loads and atomics issued
-// before any result is used.  w[j] < 0 means "no edge".  A vertex is won by
-// the atomicOr that sets its visited bit; the winner writes its level,
-// adds its out-degree to my_deg, appends it to the warp queue and, with fnw
-// given, marks it in the next frontier's bitmap too.
-__device__ __forceinline__ void claim_batch(const int (&w)[ILP], const BfsArgs &a, int nl, WarpQ &q,
-                                            unsigned long long *cnt, int *qn, unsigned long long &my_deg,
-                                            unsigned *fnw)
+// before any result is used.  w[j] < 0 means "no edge".  After a plain-load
+// filter on the visited bitmap, a candidate's atomicOr claim and the loads
+// of its row bounds are issued together (the bounds of a candidate that
+// loses are not used).  A vertex is won by the atomicOr that sets its
+// visited bit; the winner writes its level, adds its out-degree to my_deg,
+// appends itself and its bounds to the warp queue and, with fnw given,
+// marks itself in the next frontier's bitmap too.
+__device__ __forceinline__ void claim_batch(const int (&w)[ILP], const BfsArgs &a, int nl, WarpQB &q,
+                                            unsigned long long *cnt, int *qn, int2 *qbn,
+                                            unsigned long long &my_deg, unsigned *fnw)
 {
     unsigned word[ILP];
 #pragma unroll
     for (int j = 0; j < ILP; j++) word[j] = w[j] >= 0 ? a.visited[w[j] >> 5] : FULL;
     unsigned old[ILP];
+    int2 be[ILP];
 #pragma unroll
     for (int j = 0; j < ILP; j++) {
         const unsigned bit = 1u << (w[j] & 31);
         old[j] = FULL;
-        if (!(word[j] & bit)) old[j] = atomicOr(&a.visited[w[j] >> 5], bit);
+        be[j] = make_int2(0, 0);
+        if (!(word[j] & bit)) {
+            old[j] = atomicOr(&a.visited[w[j] >> 5], bit);
+            be[j] = make_int2(__ldg(a.row + w[j]), __ldg(a.row + w[j] + 1));
+        }
     }
     bool won[ILP];
-    int d0[ILP], d1[ILP];
 #pragma unroll
     for (int j = 0; j < ILP; j++) {
         won[j] = !((old[j] >> (w[j] & 31)) & 1u);
-        d0[j] = d1[j] = 0;
         if (won[j]) {
             a.level[w[j]] = nl;
-            d0[j] = __ldg(a.row + w[j]);
-            d1[j] = __ldg(a.row + w[j] + 1);
+            my_deg += (unsigned long long)(be[j].y - be[j].x);
         }
     }
 #pragma unroll
-    for (int j = 0; j < ILP; j++) {
-        my_deg += (unsigned long long)(d1[j] - d0[j]);
-        wq_push(q, won[j], w[j], cnt, qn);
-    }
+    for (int j = 0; j < ILP; j++) wqb_push(q, won[j], w[j], be[j], cnt, qn, qbn);
     if (fnw) {  // one branch, taken on whole levels or not at all
 #pragma unroll
         for (int j = 0; j < ILP; j++)
@@ -118,11 +206,13 @@ __device__ __forceinline__ void claim_batch(const int (&w)[ILP], const BfsArgs &
 // of W takes edges [E*g/W, E*(g+1)/W) of it -- all warps of the grid when
 // the list is one segment or `heavy` (every row long, so each segment holds
 // enough edges for the whole grid: segments are walked one after another),
-// the CTA's own warps on its own segments otherwise.
+// the CTA's own warps on its own segments otherwise.  lb: the rows' bounds
+// beside the list (a frontier queue), or null (then the row offsets are
+// loaded).
 template <int BLOCK>
-__device__ void grid_expand_list(const int *list, int cnt, const BfsArgs &a, int nl, WarpQ &q,
-                                 unsigned long long *cnt_next, int *qn, unsigned long long &my_deg, int *s_pre,
-                                 int *s_beg, int *s_warp, unsigned *fnw, bool heavy = false)
+__device__ void grid_expand_list(const int *list, const int2 *lb, int cnt, const BfsArgs &a, int nl, WarpQB &q,
+                                 unsigned long long *cnt_next, int *qn, int2 *qbn, unsigned long long &my_deg,
+                                 int *s_pre, int *s_beg, int *s_warp, unsigned *fnw, bool heavy = false)
 {
     constexpr int PER = SEG / BLOCK;
     const int lane = (int)lane_id();
@@ -143,10 +233,15 @@ __device__ void grid_expand_list(const int *list, int cnt, const BfsArgs &a, int
             const int j = threadIdx.x * PER + t;
             d[t] = 0;
             if (j < segn) {
-                const int v = __ldcg(list + seg + j);
-                const int b = __ldg(a.row + v);
-                s_beg[j] = b;
-                d[t] = __ldg(a.row + v + 1) - b;
+                int2 be;
+                if (lb) {
+                    be = __ldcg(lb + seg + j);
+                } else {
+                    const int v = __ldcg(list + seg + j);
+                    be = make_int2(__ldg(a.row + v), __ldg(a.row + v + 1));
+                }
+                s_beg[j] = be.x;
+                d[t] = be.y - be.x;
             }
             sum += d[t];
         }
@@ -176,7 +271,7 @@ __device__ void grid_expand_list(const int *list, int cnt, const BfsArgs &a, int
                     w[j] = __ldg(a.col + s_beg[l] + (int)(e - s_pre[l]));
                 }
             }
-            claim_batch(w, a, nl, q, cnt_next, qn, my_deg, fnw);
+            claim_batch(w, a, nl, q, cnt_next, qn, qbn, my_deg, fnw);
         }
         __syncthreads();
     }
@@ -186,8 +281,8 @@ __device__ void grid_expand_list(const int *list, int cnt, const BfsArgs &a, int
 // appends the vertices whose bit is set in (want ? bits : ~bits & valid)
 // to out, one global atomic per CTA tile.
 template <int BLOCK>
-__device__ void bitmap_to_list(const unsigned *bm, bool complement, int n, int W, int *out,
-                               unsigned long long *cnt, int *s_warp, unsigned long long *s_base)
+__device__ void bitmap_to_list(const unsigned *bm, bool complement, int n, int W, int *out, int2 *outb,
+                               const int *row, unsigned long long *cnt, int *s_warp, unsigned long long *s_base)
 {
     for (long long t0 = (long long)blockIdx.x * BLOCK; t0 < W; t0 += (long long)gridDim.x * BLOCK) {
         const long long w = t0 + threadIdx.x;
@@ -206,7 +301,10 @@ __device__ void bitmap_to_list(const unsigned *bm, bool complement, int n, int W
         unsigned long long pos = *s_base + (unsigned long long)off;
         while (bits) {
             const int b = __ffs(bits) - 1;
-            out[pos++] = (int)(w * 32 + b);
+            const int v = (int)(w * 32 + b);
+            out[pos] = v;
+            outb[pos] = make_int2(__ldg(row + v), __ldg(row + v + 1));
+            ++pos;
             bits &= bits - 1u;
         }
         __syncthreads();
@@ -216,9 +314,10 @@ __device__ void bitmap_to_list(const unsigned *bm, bool complement, int n, int W
 // Top-down expansion of one row per lane (d = 0: none) as one concatenated
 // edge range over the warp, ILP edges per lane in flight; rows of
 // big_degree or more go to bigl (counted in *bigcnt) for a grid-wide pass.
-__device__ __forceinline__ void expand_lane_rows(int v, int b, int d, const BfsArgs &a, int nl, WarpQ &q,
-                                                 unsigned long long *cnt, int *qn, unsigned long long &my_deg,
-                                                 unsigned *bigcnt, unsigned lane, unsigned *fnw)
+__device__ __forceinline__ void expand_lane_rows(int v, int b, int d, const BfsArgs &a, int nl, WarpQB &q,
+                                                 unsigned long long *cnt, int *qn, int2 *qbn,
+                                                 unsigned long long &my_deg, unsigned *bigcnt, unsigned lane,
+                                                 unsigned *fnw)
 {
     const bool isbig = d >= a.big_degree;
     const unsigned bm = __ballot_sync(FULL, isbig);
@@ -249,7 +348,7 @@ __device__ __forceinline__ void expand_lane_rows(int v, int b, int d, const BfsA
             const int oe = __shfl_sync(FULL, excl, lo);
             w[j] = k < T ? __ldg(a.col + ob + (kk - oe)) : -1;
         }
-        claim_batch(w, a, nl, q, cnt, qn, my_deg, fnw);
+        claim_batch(w, a, nl, q, cnt, qn, qbn, my_deg, fnw);
     }
 }
 
@@ -258,7 +357,7 @@ __device__ __forceinline__ void expand_lane_rows(int v, int b, int d, const BfsA
 // time, deals their frontier vertices one per lane, and expands those rows
 // with expand_lane_rows.  cw aims a chunk at about 32 frontier vertices.
 __device__ __forceinline__ void bitmap_expand(const unsigned *fb, int W, long long nf, const BfsArgs &a, int nl,
-                                              WarpQ &q, unsigned long long *cnt, int *qn,
+                                              WarpQB &q, unsigned long long *cnt, int *qn, int2 *qbn,
                                               unsigned long long &my_deg, unsigned *bigcnt, long long gwarp,
                                               long long nwarps, unsigned lane, unsigned *fnw)
 {
@@ -297,7 +396,7 @@ __device__ __forceinline__ void bitmap_expand(const unsigned *fb, int W, long lo
                 b = __ldg(a.row + v);
                 d = __ldg(a.row + v + 1) - b;
             }
-            expand_lane_rows(v, b, d, a, nl, q, cnt, qn, my_deg, bigcnt, lane, fnw);
+            expand_lane_rows(v, b, d, a, nl, q, cnt, qn, qbn, my_deg, bigcnt, lane, fnw);
         }
     }
 }
@@ -318,7 +417,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
     int *s_q = smem;                           // NW * QCAP warp queues
     int *s_pre = s_q + NW * QCAP;              // SEG degree prefix
     int *s_beg = s_pre + SEG;                  // SEG row begins
-    int2 *s_def = (int2 *)(s_beg + SEG);       // NW * BU_DEF deferred bottom-up rows
+    int2 *s_def = (int2 *)(s_beg + SEG);       // NW * BU_DEF: queue row bounds (top-down), deferred rows (bottom-up)
 
     const int n = a.n;
     const int W = (n + 31) >> 5;
@@ -328,7 +427,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
     const long long gwarp = gtid >> 5;
     const long long nwarps = gthreads >> 5;
     BfsCtrl *ctrl = a.ctrl;
-    WarpQ q{s_q + (threadIdx.x >> 5) * QCAP, 0};
+    WarpQB q{s_q + (threadIdx.x >> 5) * QCAP, s_def + (threadIdx.x >> 5) * BU_DEF, 0};
     unsigned epoch = 0;
     if (a.resume) {
         // a continuation: nothing to do when the search has ended or failed,
@@ -361,6 +460,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
         }
         if (root >= 0 && gtid == 0) {
             a.q0[0] = root;
+            a.qb[0][0] = make_int2(__ldg(a.row + root), __ldg(a.row + root + 1));
             ctrl->cd[0] = cd_pack(1, (unsigned long long)(__ldg(a.row + root + 1) - __ldg(a.row + root)));
         }
         if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
@@ -372,9 +472,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                     const int r = a.roots[i];
                     if (atomicCAS(&a.level[r], -1, 0) == -1) {
                         atomicOr(&a.visited[r >> 5], 1u << (r & 31));
-                        const unsigned long long d = (unsigned long long)(__ldg(a.row + r + 1) - __ldg(a.row + r));
-                        const unsigned long long pos = cd_count(atomicAdd(&ctrl->cd[0], cd_pack(1, d)));
+                        const int2 be = make_int2(__ldg(a.row + r), __ldg(a.row + r + 1));
+                        const unsigned long long pos =
+                            cd_count(atomicAdd(&ctrl->cd[0], cd_pack(1, (unsigned long long)(be.y - be.x))));
                         a.q0[pos] = r;
+                        a.qb[0][pos] = be;
                     }
                 }
             }
@@ -471,6 +573,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
 
         int *qc = (L & 1) ? a.q1 : a.q0;
         int *qn = (L & 1) ? a.q0 : a.q1;
+        const int2 *qbc = a.qb[L & 1];      // row bounds beside qc
+        int2 *qbn = a.qb[(L + 1) & 1];      // and beside qn
         unsigned *fc = a.fb[L % 3];
         unsigned *fn = a.fb[(L + 1) % 3];
         unsigned *fz = a.fb[(L + 2) % 3];   // zeroed now: the next level's fn
@@ -499,7 +603,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
         const bool from_bitmap = !bu && !td && mf <= BMTD_EDGES;
         if (!bu && !td && !from_bitmap) {
             // bitmap -> queue
-            bitmap_to_list<BLOCK>(fc, false, n, W, qc, &ctrl->fill, s_warp, &s_base);
+            bitmap_to_list<BLOCK>(fc, false, n, W, qc, a.qb[L & 1], a.row, &ctrl->fill, s_warp, &s_base);
             if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
         }
         td = !bu;
@@ -520,11 +624,12 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
             const bool likely_bu = (float)mf * growth * (float)a.alpha > (float)m_u;
             unsigned *fnw = a.direction == GBFS_DIR_OPTIMIZING && a.brow && likely_bu ? fn : nullptr;
             if (from_bitmap) {
-                bitmap_expand(fc, W, (long long)nf, a, nl, q, cnt_next, qn, my_deg, &ctrl->big[L % 3], gwarp, nwarps,
+                bitmap_expand(fc, W, (long long)nf, a, nl, q, cnt_next, qn, qbn, my_deg, &ctrl->big[L % 3], gwarp, nwarps,
                               lane, fnw);
             } else if (nf <= (unsigned long long)SEG) {
                 // small frontier: every edge of it balanced over the whole grid
-                grid_expand_list<BLOCK>(qc, (int)nf, a, nl, q, cnt_next, qn, my_deg, s_pre, s_beg, s_warp, fnw);
+                grid_expand_list<BLOCK>(qc, qbc, (int)nf, a, nl, q, cnt_next, qn, qbn, my_deg, s_pre, s_beg, s_warp,
+                                        fnw);
             } else {
                 // large frontier: 32 rows per warp as one concatenated edge
                 // range, rows of degree >= big_degree deferred to a grid pass
@@ -533,13 +638,14 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                     int v = 0, b = 0, d = 0;
                     if (i < (long long)nf) {
                         v = __ldcg(qc + i);
-                        b = __ldg(a.row + v);
-                        d = __ldg(a.row + v + 1) - b;
+                        const int2 be = __ldcg(qbc + i);
+                        b = be.x;
+                        d = be.y - be.x;
                     }
-                    expand_lane_rows(v, b, d, a, nl, q, cnt_next, qn, my_deg, &ctrl->big[L % 3], lane, fnw);
+                    expand_lane_rows(v, b, d, a, nl, q, cnt_next, qn, qbn, my_deg, &ctrl->big[L % 3], lane, fnw);
                 }
             }
-            block_flush_packed(q, cnt_next, qn, my_deg, s_wq, s_red, &s_base);
+            block_flush_bounds(q, cnt_next, qn, qbn, my_deg, s_wq, s_red, &s_base);
             if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
 
             // rows deferred to the grid pass (only large frontiers defer, and
@@ -553,8 +659,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
             traced_big = nb > 0;
             if (nb > 0) {
                 my_deg = 0;
-                grid_expand_list<BLOCK>(a.bigl, nb, a, nl, q, cnt_next, qn, my_deg, s_pre, s_beg, s_warp, fnw, true);
-                block_flush_packed(q, cnt_next, qn, my_deg, s_wq, s_red, &s_base);
+                grid_expand_list<BLOCK>(a.bigl, nullptr, nb, a, nl, q, cnt_next, qn, qbn, my_deg, s_pre, s_beg, s_warp,
+                                        fnw, true);
+                block_flush_bounds(q, cnt_next, qn, qbn, my_deg, s_wq, s_red, &s_base);
                 if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
             }
             fn_set = fnw != nullptr;
@@ -971,6 +1078,7 @@ int bfs_work_alloc(BfsWork &w, int32_t n, std::string &err)
     if (!al((void **)&w.level, bytes_int) || !al((void **)&w.visited, W * 4) ||
         !al((void **)&w.fb0, W * 4) || !al((void **)&w.fb1, W * 4) || !al((void **)&w.fb2, W * 4) ||
         !al((void **)&w.q0, bytes_int) || !al((void **)&w.q1, bytes_int) ||
+        !al((void **)&w.qb0, 2 * bytes_int) || !al((void **)&w.qb1, 2 * bytes_int) ||
         !al((void **)&w.big, bytes_int) || !al((void **)&w.roots, bytes_int) ||
         !al((void **)&w.ctrl, sizeof(BfsCtrl))) {
         bfs_work_free(w);
@@ -989,7 +1097,7 @@ int bfs_work_alloc(BfsWork &w, int32_t n, std::string &err)
 
 void bfs_work_free(BfsWork &w)
 {
-    void *ps[] = {w.level, w.visited, w.fb0, w.fb1, w.fb2, w.q0, w.q1, w.big, w.roots, w.ctrl, w.d_outs};
+    void *ps[] = {w.level, w.visited, w.fb0, w.fb1, w.fb2, w.q0, w.q1, w.qb0, w.qb1, w.big, w.roots, w.ctrl, w.d_outs};
     for (void *p : ps)
         if (p) cudaFree(p);
     if (w.h_outs) cudaFreeHost(w.h_outs);
@@ -1063,6 +1171,8 @@ BfsArgs make_args(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const in
     a.fb[2] = w.fb2;
     a.q0 = w.q0;
     a.q1 = w.q1;
+    a.qb[0] = w.qb0;
+    a.qb[1] = w.qb1;
     a.bigl = w.big;
     a.ctrl = w.ctrl;
     a.out = slot;
@@ -1201,14 +1311,15 @@ cudaError_t bfs_enqueue(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, co
     a.may_yield = 1;
     a.sparse_ctas = ctas;
     a.sparse_cap = cap;
-    e = bfs_launch_any(a, p.threads_per_block, p.blocks_per_sm, st, max_ctas);
+    const int bps = std::min(p.blocks_per_sm, SPARSE_GRID_BPS);
+    e = bfs_launch_any(a, p.threads_per_block, bps, st, max_ctas);
     for (int ph = 0; ph < SPARSE_PHASES && e == cudaSuccess; ph++) {
         e = bfs_sparse_launch(a, st);
         if (e == cudaSuccess) {
             BfsArgs r = a;
             r.resume = 1;
             r.may_yield = ph + 1 < SPARSE_PHASES ? 1 : 0;
-            e = bfs_launch_any(r, p.threads_per_block, p.blocks_per_sm, st, max_ctas);
+            e = bfs_launch_any(r, p.threads_per_block, bps, st, max_ctas);
         }
     }
     return e;

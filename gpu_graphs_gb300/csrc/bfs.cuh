@@ -86,6 +86,8 @@ struct BfsWork {
     unsigned *fb2 = nullptr;
     int *q0 = nullptr;           // n frontier queues
     int *q1 = nullptr;
+    int2 *qb0 = nullptr;         // n row bounds (row[v], row[v + 1]) beside q0 / q1
+    int2 *qb1 = nullptr;
     int *big = nullptr;          // n deferred rows
     int *roots = nullptr;        // root staging (n)
     BfsCtrl *ctrl = nullptr;

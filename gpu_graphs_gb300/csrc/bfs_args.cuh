@@ -22,6 +22,7 @@ struct BfsArgs {
     unsigned *visited;
     unsigned *fb[3];         // frontier bitmaps, rotating by level
     int *q0, *q1;            // frontier queues
+    int2 *qb[2];             // row bounds beside q0 and q1
     int *bigl;
     BfsCtrl *ctrl;
     BfsOut *out;

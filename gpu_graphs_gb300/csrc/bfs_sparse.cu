@@ -143,16 +143,16 @@ __global__ void __launch_bounds__(SP_BLOCK, 1) k_bfs_sparse(BfsArgs a)
     {
         const unsigned long long F0 = cd_count(ctrl->cd[L % 3]);
         const int *qg = (L & 1) ? a.q1 : a.q0;
+        const int2 *qbg = a.qb[L & 1];
         const unsigned long long lo = F0 * r / C, hi = F0 * (r + 1) / C;
         unsigned long long my_deg = 0;
         for (unsigned long long i = lo + t; i < hi; i += SP_BLOCK) {
             const int j = (int)(i - lo);
             if (j >= cap) break;  // never: the grid kernel checked the frontier fits
-            const int v = __ldcg(qg + i);
-            const int b = __ldg(a.row + v), e = __ldg(a.row + v + 1);
-            qbe0[j] = make_int2(b, e);
-            qv0[j] = v;
-            my_deg += (unsigned long long)(e - b);
+            const int2 be = __ldcg(qbg + i);
+            qbe0[j] = be;
+            qv0[j] = __ldcg(qg + i);
+            my_deg += (unsigned long long)(be.y - be.x);
         }
         const unsigned long long d = block_sum(my_deg);
         if (t == 0) {
@@ -229,8 +229,12 @@ __global__ void __launch_bounds__(SP_BLOCK, 1) k_bfs_sparse(BfsArgs a)
             // hand the loop back to the grid kernel: frontier L into its
             // global queue (CTA segments in rank order), state parked
             int *qg = (L & 1) ? a.q1 : a.q0;
+            int2 *qbg = a.qb[L & 1];
             const unsigned cnt = s_cnt[buf], off = s_off[r];
-            for (unsigned j = t; j < cnt; j += SP_BLOCK) qg[off + j] = qv0[buf * cap + j];
+            for (unsigned j = t; j < cnt; j += SP_BLOCK) {
+                qg[off + j] = qv0[buf * cap + j];
+                qbg[off + j] = qbe0[buf * cap + j];
+            }
             if (r == 0 && t == 0) {
                 ctrl->cd[L % 3] = cd_pack(F, mf);
                 ctrl->cd[(L + 1) % 3] = 0;

@@ -64,41 +64,6 @@ __device__ __forceinline__ void block_flush(WarpQ &q, unsigned long long *cnt, i
     __syncthreads();
 }
 
-// block_flush for a counter that packs the entry count (low 32 bits) with a
-// second sum (high 32 bits, e.g. the entries' out-degrees): every warp
-// queue of the block is appended and the block's `hi` values (one per
-// thread) are added with the same single global atomic.  Both block totals
-// must stay below 2^32 together with the counter's halves.
-__device__ __forceinline__ void block_flush_packed(WarpQ &q, unsigned long long *cnt, int *out,
-                                                   unsigned long long hi, int *s_wq,
-                                                   unsigned long long *s_hi, unsigned long long *s_base)
-{
-    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const unsigned lane = lane_id();
-    const unsigned long long wh = warp_sum(hi);
-    __syncwarp();
-    if (lane == 0) {
-        s_wq[w] = q.n;
-        s_hi[w] = wh;
-    }
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        const int c = (int)lane < nw ? s_wq[lane] : 0;
-        const unsigned long long h = (int)lane < nw ? s_hi[lane] : 0ull;
-        const int incl = warp_incl_scan(c);
-        const int tot = __shfl_sync(FULL, incl, 31);
-        const unsigned long long htot = warp_sum(h);
-        if ((int)lane < nw) s_wq[lane] = incl - c;
-        if (lane == 0)
-            *s_base = (tot || htot) ? (atomicAdd(cnt, (htot << 32) | (unsigned long long)tot) & 0xffffffffull) : 0ull;
-    }
-    __syncthreads();
-    const unsigned long long base = *s_base + (unsigned long long)s_wq[w];
-    for (int i = lane; i < q.n; i += 32) out[base + i] = q.buf[i];
-    q.n = 0;
-    __syncthreads();
-}
-
 template <typename T>
 __device__ __forceinline__ T block_reduce_sum(T x, T *s_red)
 {

@@ -61,8 +61,12 @@ struct SrvGraph {
     double est_us = 0;   // recent launch time (moving average), 0 before the first
 };
 
-// 64-lane workspace + single-source workspace (level, 3 bitmaps + visited, 4 int lists)
-int64_t slot_bytes(int64_t n) { return n > 0 ? ms_work_bytes(n) + 4 * n * 5 + n / 2 + (1 << 20) : 0; }
+// 64-lane workspace + single-source workspace (level, 3 bitmaps + visited,
+// 4 int lists, the row bounds beside the two queues, the control block)
+int64_t slot_bytes(int64_t n)
+{
+    return n > 0 ? ms_work_bytes(n) + 4 * n * 5 + 16 * n + n / 2 + (int64_t)sizeof(BfsCtrl) + (1 << 20) : 0;
+}
 
 double ms_between(Clock::time_point a, Clock::time_point b)
 {

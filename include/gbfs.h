@@ -119,7 +119,10 @@ int gbfs_graph_get_csr(const gbfs_graph *g, int32_t *row_offset,
 
 typedef struct gbfs_params {
     int32_t threads_per_block;  /* 256, 512 or 1024                         */
-    int32_t blocks_per_sm;      /* persistent CTAs per SM (capped by occupancy) */
+    int32_t blocks_per_sm;      /* persistent CTAs per SM (capped by occupancy;
+                                   on graphs of out-degree <= 16, whose
+                                   searches have a sparse phase on one
+                                   thread-block cluster, at most 1)        */
     int32_t alpha;              /* TD->BU when frontier edges > unexplored/alpha */
     int32_t beta;               /* BU->TD when frontier vertices < n/beta    */
     int32_t big_degree;         /* TD rows >= this are split across the grid */
