@@ -210,7 +210,7 @@ def log(msg: str) -> None:
     print(f"[bench] {msg}", file=sys.stderr, flush=True)
 
 
-KERNEL_SOURCES = ("bfs.cu", "bfs.cuh", "common.cuh", "blockq.cuh")
+KERNEL_SOURCES = ("bfs.cu", "bfs.cuh", "bfs_args.cuh", "common.cuh", "blockq.cuh")
 
 
 def kernel_source_hash() -> str:
@@ -459,12 +459,19 @@ def measure_grid(side: int, torch) -> dict:
     n = side * side
     g = gb.Graph.from_edges(n, src, dst, gb.UNDIRECTED)
     del src, dst
-    row, _ = g.csr()
+    row, col = g.csr()
     deg = np.diff(row)
     source = int(pick_sources(deg, 1)[0])
     out = torch.empty(n, dtype=torch.int32, device="cuda")
     g.bfs(source, out=out)
     ref = out.clone()
+    # the clone runs on torch's stream: finish it before the engine's stream
+    # writes `out` again
+    torch.cuda.synchronize()
+    import oracle
+    o = oracle.CSR(n, row.astype(np.int64), col)
+    same_oracle = bool(np.array_equal(ref.cpu().numpy(), oracle.bfs_queue(o, source)))
+    del o
     runs = [g.bfs(source, out=out, stats=True)[1] for _ in range(3)]
     st = runs[-1]
     t_p = float(np.mean([r.ms for r in runs]))
@@ -486,7 +493,7 @@ def measure_grid(side: int, torch) -> dict:
             "per_level_launches": int(runs_l[-1].launches), "speedup_vs_per_level": round(t_l / t_p, 2),
             "gteps_persistent": round(st.edges_in_component / 2 / (t_p / 1e3) / 1e9, 3),
             "us_per_level_persistent": round(1e3 * t_p / max(1, st.levels), 3),
-            "levels_identical": same}
+            "levels_identical": same, "levels_identical_oracle": same_oracle}
 
 
 def many_graphs_workload(gen, count: int = 512):
