@@ -57,6 +57,7 @@ struct MsArgs {
     const int *src;
     MsCtrl *ctrl;
     int pull_allowed, direction, pull_div;
+    int has_big;              // some push row has MS_BIG edges or more (else none is deferred)
     unsigned long long timeout_ns;
 };
 
@@ -203,18 +204,40 @@ __device__ __forceinline__ void push_rows(const MsArgs &a, const int *list, long
     }
 }
 
-// OR x over the block, then one atomicOr into *dst (all threads call).
-__device__ __forceinline__ void or_into(unsigned long long x, unsigned long long *dst, unsigned long long *s_red)
+// block_flush with an OR of lane masks in the same pass: every warp queue of the block is
+// appended with one global atomic on cnt, and the block's lanes (x, one mask
+// per thread) are ORed into *dst with one more, both issued by thread 0 after
+// the same two barriers (all threads call).
+__device__ __forceinline__ void block_flush_or(WarpQ &q, unsigned long long *cnt, int *out, unsigned long long x,
+                                               unsigned long long *dst, int *s_wq, unsigned long long *s_or,
+                                               unsigned long long *s_base)
 {
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const unsigned lane = lane_id();
     x = warp_or64(x);
-    __syncthreads();
-    if (lane_id() == 0) s_red[threadIdx.x >> 5] = x;
+    __syncwarp();
+    if (lane == 0) {
+        s_wq[w] = q.n;
+        s_or[w] = x;
+    }
     __syncthreads();
     if (threadIdx.x < 32) {
-        unsigned long long t = threadIdx.x < (blockDim.x >> 5) ? s_red[threadIdx.x] : 0ull;
-        t = warp_or64(t);
-        if (threadIdx.x == 0 && t) atomicOr(dst, t);
+        const int c = (int)lane < nw ? s_wq[lane] : 0;
+        const unsigned long long o = (int)lane < nw ? s_or[lane] : 0ull;
+        const int incl = warp_incl_scan(c);
+        const int tot = __shfl_sync(FULL, incl, 31);
+        const unsigned long long ot = warp_or64(o);
+        if ((int)lane < nw) s_wq[lane] = incl - c;
+        if (lane == 0) {
+            *s_base = tot ? atomicAdd(cnt, (unsigned long long)tot) : 0ull;
+            if (ot) atomicOr(dst, ot);
+        }
     }
+    __syncthreads();
+    const unsigned long long base = *s_base + (unsigned long long)s_wq[w];
+    for (int i = lane; i < q.n; i += 32) out[base + i] = q.buf[i];
+    q.n = 0;
+    __syncthreads();
 }
 
 __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
@@ -222,6 +245,7 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
     extern __shared__ int ms_smem[];
     __shared__ unsigned long long s_red[32];
     __shared__ unsigned long long s_base;
+    __shared__ unsigned long long s_ctl[3];  // this level's queue size, live lanes, last level's queue size
     __shared__ int s_warp[33];
     __shared__ int s_wq[33];
     constexpr int NW = MS_BLOCK / 32;
@@ -282,12 +306,19 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
 
     int L = 0, push_levels = 0, pull_levels = 0;
     for (;;) {
-        const unsigned long long nq = ld_relaxed_u64(&ctrl->qcnt[L % 4]);
+        // the level's control words: one load each per CTA, shared
+        if (threadIdx.x == 0) {
+            s_ctl[0] = ld_relaxed_u64(&ctrl->qcnt[L % 4]);
+            s_ctl[1] = ld_relaxed_u64(&ctrl->alive[L % 4]);
+            s_ctl[2] = L >= 1 ? ld_relaxed_u64(&ctrl->qcnt[(L + 3) % 4]) : 0ull;
+        }
+        __syncthreads();
+        const unsigned long long nq = s_ctl[0];
         if (nq == 0) break;
         // only lanes with a frontier at level L can reach anything at L+1
-        const unsigned long long live = ld_relaxed_u64(&ctrl->alive[L % 4]) & all;
+        const unsigned long long live = s_ctl[1] & all;
         unsigned long long my_or = 0;   // lanes this thread puts in the next frontier
-        const unsigned long long nz = L >= 1 ? ld_relaxed_u64(&ctrl->qcnt[(L + 3) % 4]) : 0ull;
+        const unsigned long long nz = s_ctl[2];
         bool pull;
         if (!a.pull_allowed || a.direction == GBFS_DIR_TOPDOWN) pull = false;
         else if (a.direction == GBFS_DIR_BOTTOMUP) pull = true;
@@ -460,8 +491,7 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
                     wq_push(q, lane == 0 && nw != 0, u, qcnt_next, Qn);
                 }
             }
-            block_flush(q, qcnt_next, Qn, s_wq, &s_base);
-            or_into(my_or, &ctrl->alive[(L + 1) % 4], s_red);
+            block_flush_or(q, qcnt_next, Qn, my_or, &ctrl->alive[(L + 1) % 4], s_wq, s_red, &s_base);
             if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
         } else {
             ++push_levels;
@@ -476,16 +506,21 @@ __global__ void __launch_bounds__(MS_BLOCK, 2) k_msbfs(MsArgs a)
             unsigned long long *bigcnt = &ctrl->big[L & 1];
             push_rows(a, Qc, (long long)nq, grid_wide, !grid_wide, nl, Fc, Fn, q, qcnt_next, Qn, my_or, s_pre,
                       s_beg, s_f, s_warp, bigcnt);
-            block_flush(q, qcnt_next, Qn, s_wq, &s_base);
-            or_into(my_or, &ctrl->alive[(L + 1) % 4], s_red);
+            block_flush_or(q, qcnt_next, Qn, my_or, &ctrl->alive[(L + 1) % 4], s_wq, s_red, &s_base);
             if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
-            const unsigned long long nb = grid_wide ? 0ull : ld_relaxed_u64(bigcnt);
+            // rows deferred to the grid pass (segmented queues only, and only
+            // when some row is that long): one load per CTA, shared
+            unsigned long long nb = 0;
+            if (!grid_wide && a.has_big) {
+                if (threadIdx.x == 0) s_ctl[0] = ld_relaxed_u64(bigcnt);
+                __syncthreads();
+                nb = s_ctl[0];
+            }
             if (nb) {
                 my_or = 0;
                 push_rows(a, a.bigl, (long long)nb, true, false, nl, Fc, Fn, q, qcnt_next, Qn, my_or, s_pre, s_beg,
                           s_f, s_warp, bigcnt);
-                block_flush(q, qcnt_next, Qn, s_wq, &s_base);
-                or_into(my_or, &ctrl->alive[(L + 1) % 4], s_red);
+                block_flush_or(q, qcnt_next, Qn, my_or, &ctrl->alive[(L + 1) % 4], s_wq, s_red, &s_base);
                 if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
             }
         }
@@ -765,6 +800,7 @@ cudaError_t msbfs_enqueue(const DeviceCsr &g, const gbfs_params &p, bool symmetr
     a.pull_allowed = pull_allowed ? 1 : 0;
     a.direction = p.direction;
     a.pull_div = 16;
+    a.has_big = g.max_degree >= MS_BIG ? 1 : 0;
     a.timeout_ns = (unsigned long long)std::max(1, p.timeout_ms) * 1000000ull;
     static LaunchSetup setup;
     const size_t smem = ms_smem_bytes();
