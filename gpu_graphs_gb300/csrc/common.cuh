@@ -127,23 +127,6 @@ __device__ __forceinline__ int ld_relaxed_i32(const int *p)
     return v;
 }
 
-// Read-only, streamed once: skip L1 allocation.
-__device__ __forceinline__ int4 ld_stream_v4(const int *p)
-{
-    int4 v;
-    asm volatile("ld.global.nc.L1::no_allocate.v4.s32 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-                 : "l"(p));
-    return v;
-}
-
-__device__ __forceinline__ int ld_stream(const int *p)
-{
-    int v;
-    asm volatile("ld.global.nc.L1::no_allocate.s32 %0, [%1];" : "=r"(v) : "l"(p));
-    return v;
-}
-
 // ---- mbarrier and bulk (TMA) copies, shared memory of this CTA ------------
 __device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 
