@@ -51,6 +51,7 @@ namespace {
 constexpr int SEG = 2048;    // frontier rows expanded edge-balanced per pass
 constexpr int ILP = 4;       // edges in flight per lane in top-down passes
 constexpr int PROBE = 8;     // neighbours probed per step in bottom-up
+constexpr int COOP_ROWS = 4; // bottom-up rows left in a warp below which the warp walks them together
 // Per warp, an int2 area of QCAP entries: in top-down steps the row bounds
 // of the warp queue's entries, in bottom-up steps the deferred rows' bounds
 // (under 64 left plus a 128-vertex round)
@@ -708,7 +709,42 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                     if (kb < dn) { vb = def_v[kb]; ib = def_b[kb].x; eb = def_b[kb].y; }
                     const int da = ea - ia + skip, db = eb - ib + skip;
                     bool fa = false, fb = false;
-                    while ((ia < ea && !fa) || (ib < eb && !fb)) {
+                    for (;;) {
+                        const bool aa = ia < ea && !fa, ab = ib < eb && !fb;
+                        const unsigned ma = __ballot_sync(FULL, aa), mb = __ballot_sync(FULL, ab);
+                        if (!(ma | mb)) break;
+                        if (__popc(ma) + __popc(mb) <= COOP_ROWS) {
+                            // a few long rows left: walk each with the whole
+                            // warp, 32 entries a step, instead of PROBE per lane
+                            int rem = max(aa ? ea - ia : 0, ab ? eb - ib : 0);
+#pragma unroll
+                            for (int o = 16; o > 0; o >>= 1) rem = max(rem, __shfl_xor_sync(FULL, rem, o));
+                            if (rem > 2 * PROBE) {
+                                unsigned ta = ma, tb = mb;
+                                while (ta | tb) {
+                                    const bool isb = ta == 0;
+                                    const int sl = __ffs(isb ? tb : ta) - 1;
+                                    if (isb) tb &= tb - 1; else ta &= ta - 1;
+                                    const int ri = __shfl_sync(FULL, isb ? ib : ia, sl);
+                                    const int re = __shfl_sync(FULL, isb ? eb : ea, sl);
+                                    bool found = false;
+                                    for (int i0 = ri; i0 < re && !found; i0 += 32) {
+                                        const int i = i0 + (int)lane;
+                                        unsigned hit = 0;
+                                        if (i < re) {
+                                            const int u = __ldg(a.bcol + i);
+                                            hit = (__ldcg(fc + (u >> 5)) >> (u & 31)) & 1u;
+                                        }
+                                        found = __any_sync(FULL, hit != 0);
+                                    }
+                                    if ((int)lane == sl) {
+                                        if (isb) { fb = found; ib = eb; }
+                                        else { fa = found; ia = ea; }
+                                    }
+                                }
+                                break;
+                            }
+                        }
                         int ua[PROBE], ub[PROBE];
 #pragma unroll
                         for (int t = 0; t < PROBE; t++) {
