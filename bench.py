@@ -670,7 +670,7 @@ def measure_serving(torch, seconds: float = 2.0, fractions=(0.25, 0.5, 0.75, 1.0
         g.set_params(direction=0)
     out = {"workload": "32 resident graphs: 16 RMAT scale U{12..22} ef 16, 16 grids side U[64, 4096]; "
                        "queries pick a graph uniformly and a source uniformly among degree>0 vertices; "
-                       "4 slots, batch window max(0.5 ms, 50% of the graph's recent launch time); "
+                       "4 slots, batch window max(0.5 ms, 10% of the graph's recent launch time); "
                        "results copied into pinned host buffers",
            "plain_one_query_per_launch": {"queries_per_s": round(len(plain_ms) / (sum(plain_ms) / 1e3), 1),
                                           "p50_ms": round(plain_ms[len(plain_ms) // 2], 3),
@@ -697,7 +697,7 @@ def measure_serving(torch, seconds: float = 2.0, fractions=(0.25, 0.5, 0.75, 1.0
     pinned = [[torch.empty(g.n, dtype=torch.int32, pin_memory=True) for _ in range(8)] for g in graphs]
     pools = [[t.numpy() for t in ts] for ts in pinned]
     counters = [0] * 32
-    cfg = dict(mem_budget_bytes=150 << 30, num_slots=4, max_lanes=64, batch_window_us=500, window_pct=50)
+    cfg = dict(mem_budget_bytes=150 << 30, num_slots=4, max_lanes=64, batch_window_us=500, window_pct=10)
 
     def submitter(srv, gids):
         def submit():

@@ -402,6 +402,66 @@ __device__ __forceinline__ void bitmap_expand(const unsigned *fb, int W, long lo
     }
 }
 
+// Bottom-up probing of up to two rows per lane (a: [ia, ea), b: [ib, eb)),
+// PROBE entries per lane and step, until each row finds a parent in the
+// frontier bitmap fc (fa / fb) or runs out.  When at most COOP_ROWS rows
+// with more than 2 * PROBE entries left remain in the warp, the warp walks
+// those together, 32 entries a step, instead of leaving most lanes idle.
+// All 32 lanes call it.
+__device__ __forceinline__ void probe_rows(int &ia, int ea, bool &fa, int &ib, int eb, bool &fb, const int *bcol,
+                                           const unsigned *fc, unsigned lane)
+{
+    for (;;) {
+        const bool aa = ia < ea && !fa, ab = ib < eb && !fb;
+        const unsigned ma = __ballot_sync(FULL, aa), mb = __ballot_sync(FULL, ab);
+        if (!(ma | mb)) return;
+        if (__popc(ma) + __popc(mb) <= COOP_ROWS) {
+            int rem = max(aa ? ea - ia : 0, ab ? eb - ib : 0);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) rem = max(rem, __shfl_xor_sync(FULL, rem, o));
+            if (rem > 2 * PROBE) {
+                unsigned ta = ma, tb = mb;
+                while (ta | tb) {
+                    const bool isb = ta == 0;
+                    const int sl = __ffs(isb ? tb : ta) - 1;
+                    if (isb) tb &= tb - 1; else ta &= ta - 1;
+                    const int ri = __shfl_sync(FULL, isb ? ib : ia, sl);
+                    const int re = __shfl_sync(FULL, isb ? eb : ea, sl);
+                    bool found = false;
+                    for (int i0 = ri; i0 < re && !found; i0 += 32) {
+                        const int i = i0 + (int)lane;
+                        unsigned hit = 0;
+                        if (i < re) {
+                            const int u = __ldg(bcol + i);
+                            hit = (__ldcg(fc + (u >> 5)) >> (u & 31)) & 1u;
+                        }
+                        found = __any_sync(FULL, hit != 0);
+                    }
+                    if ((int)lane == sl) {
+                        if (isb) { fb = found; ib = eb; }
+                        else { fa = found; ia = ea; }
+                    }
+                }
+                return;
+            }
+        }
+        int ua[PROBE], ub[PROBE];
+#pragma unroll
+        for (int t = 0; t < PROBE; t++) {
+            ua[t] = (aa && ia + t < ea) ? __ldg(bcol + ia + t) : -1;
+            ub[t] = (ab && ib + t < eb) ? __ldg(bcol + ib + t) : -1;
+        }
+        unsigned ga = 0, gb = 0;
+#pragma unroll
+        for (int t = 0; t < PROBE; t++) {
+            if (ua[t] >= 0) ga |= __ldcg(fc + (ua[t] >> 5)) >> (ua[t] & 31);
+            if (ub[t] >= 0) gb |= __ldcg(fc + (ub[t] >> 5)) >> (ub[t] & 31);
+        }
+        if (aa) { if (ga & 1u) fa = true; else ia += PROBE; }
+        if (ab) { if (gb & 1u) fb = true; else ib += PROBE; }
+    }
+}
+
 // MINB (CTAs per SM the register budget is sized for) only shapes register
 // allocation; the launch decides the actual grid.
 template <int BLOCK, int MINB>
@@ -709,57 +769,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                     if (kb < dn) { vb = def_v[kb]; ib = def_b[kb].x; eb = def_b[kb].y; }
                     const int da = ea - ia + skip, db = eb - ib + skip;
                     bool fa = false, fb = false;
-                    for (;;) {
-                        const bool aa = ia < ea && !fa, ab = ib < eb && !fb;
-                        const unsigned ma = __ballot_sync(FULL, aa), mb = __ballot_sync(FULL, ab);
-                        if (!(ma | mb)) break;
-                        if (__popc(ma) + __popc(mb) <= COOP_ROWS) {
-                            // a few long rows left: walk each with the whole
-                            // warp, 32 entries a step, instead of PROBE per lane
-                            int rem = max(aa ? ea - ia : 0, ab ? eb - ib : 0);
-#pragma unroll
-                            for (int o = 16; o > 0; o >>= 1) rem = max(rem, __shfl_xor_sync(FULL, rem, o));
-                            if (rem > 2 * PROBE) {
-                                unsigned ta = ma, tb = mb;
-                                while (ta | tb) {
-                                    const bool isb = ta == 0;
-                                    const int sl = __ffs(isb ? tb : ta) - 1;
-                                    if (isb) tb &= tb - 1; else ta &= ta - 1;
-                                    const int ri = __shfl_sync(FULL, isb ? ib : ia, sl);
-                                    const int re = __shfl_sync(FULL, isb ? eb : ea, sl);
-                                    bool found = false;
-                                    for (int i0 = ri; i0 < re && !found; i0 += 32) {
-                                        const int i = i0 + (int)lane;
-                                        unsigned hit = 0;
-                                        if (i < re) {
-                                            const int u = __ldg(a.bcol + i);
-                                            hit = (__ldcg(fc + (u >> 5)) >> (u & 31)) & 1u;
-                                        }
-                                        found = __any_sync(FULL, hit != 0);
-                                    }
-                                    if ((int)lane == sl) {
-                                        if (isb) { fb = found; ib = eb; }
-                                        else { fa = found; ia = ea; }
-                                    }
-                                }
-                                break;
-                            }
-                        }
-                        int ua[PROBE], ub[PROBE];
-#pragma unroll
-                        for (int t = 0; t < PROBE; t++) {
-                            ua[t] = (!fa && ia + t < ea) ? __ldg(a.bcol + ia + t) : -1;
-                            ub[t] = (!fb && ib + t < eb) ? __ldg(a.bcol + ib + t) : -1;
-                        }
-                        unsigned ga = 0, gb = 0;
-#pragma unroll
-                        for (int t = 0; t < PROBE; t++) {
-                            if (ua[t] >= 0) ga |= __ldcg(fc + (ua[t] >> 5)) >> (ua[t] & 31);
-                            if (ub[t] >= 0) gb |= __ldcg(fc + (ub[t] >> 5)) >> (ub[t] & 31);
-                        }
-                        if (!fa && ia < ea) { if (ga & 1u) fa = true; else ia += PROBE; }
-                        if (!fb && ib < eb) { if (gb & 1u) fb = true; else ib += PROBE; }
-                    }
+                    probe_rows(ia, ea, fa, ib, eb, fb, a.bcol, fc, lane);
                     if (fa) {
                         a.level[va] = nl;
                         atomicOr(fn + (va >> 5), 1u << (va & 31));
@@ -943,23 +953,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                         bool fa = ha & 1u, fb = hb & 1u;
                         ia += two ? 2 : 1;
                         ib += two ? 2 : 1;
-                        const int width = PROBE;
-                        while ((ia < ea && !fa) || (ib < eb && !fb)) {
-                            int ua[PROBE], ub[PROBE];
-#pragma unroll
-                            for (int t = 0; t < PROBE; t++) {
-                                ua[t] = (t < width && !fa && ia + t < ea) ? __ldg(a.bcol + ia + t) : -1;
-                                ub[t] = (t < width && !fb && ib + t < eb) ? __ldg(a.bcol + ib + t) : -1;
-                            }
-                            unsigned ga = 0, gb = 0;
-#pragma unroll
-                            for (int t = 0; t < PROBE; t++) {
-                                if (ua[t] >= 0) ga |= __ldcg(fc + (ua[t] >> 5)) >> (ua[t] & 31);
-                                if (ub[t] >= 0) gb |= __ldcg(fc + (ub[t] >> 5)) >> (ub[t] & 31);
-                            }
-                            if (!fa && ia < ea) { if (ga & 1u) fa = true; else ia += width; }
-                            if (!fb && ib < eb) { if (gb & 1u) fb = true; else ib += width; }
-                        }
+                        probe_rows(ia, ea, fa, ib, eb, fb, a.bcol, fc, lane);
                         // the next frontier's out-edges (for the direction rule): the
                         // probed in-degree when in-edges are the out-edges
                         if (fa) {
