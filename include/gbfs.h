@@ -159,7 +159,12 @@ typedef struct gbfs_stats {
     int32_t levels;             /* number of BFS levels (max level + 1)     */
     int32_t td_levels;          /* levels expanded top-down                 */
     int32_t bu_levels;          /* levels expanded bottom-up                */
-    int32_t launches;           /* kernel launches this call made           */
+    int32_t launches;           /* kernel launches this call queued per
+                                   search: 1; 5 on graphs of out-degree
+                                   <= 16 (grid and cluster launches of the
+                                   sparse phase, each returning at once
+                                   when the search is already done); one
+                                   per level (+1) with per_level_launch    */
     int64_t vertices_reached;   /* vertices with level >= 0 (all sources)   */
     int64_t edges_in_component; /* out-edges of reached vertices (E_c)      */
     int64_t edges_traversed;    /* reference convention: discovered vertices
