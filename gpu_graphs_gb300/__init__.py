@@ -203,7 +203,7 @@ class Graph:
         k = lib.gbfs_last_trace(self._h, C.cast(rows, C.c_void_p), cap)
         if k < 0:
             raise GbfsError(k, "gbfs_last_trace")
-        dirs = {-3: "exit", -2: "end", -1: "init", 0: "td", 1: "bu", 2: "td+split", 4: "td-cluster"}
+        dirs = {-3: "exit", -2: "end", -1: "init", 0: "td", 1: "bu", 2: "td+split", 4: "relaxed"}
         return [{"level": r.level, "dir": dirs.get(r.direction, str(r.direction)), "frontier": r.frontier_vertices,
                  "edges": r.frontier_edges, "t_us": round(r.t_us, 2)} for r in rows[:k]]
 

@@ -57,26 +57,17 @@ constexpr int COOP_ROWS = 4; // bottom-up rows left in a warp below which the wa
 // (under 64 left plus a 128-vertex round)
 constexpr int BU_DEF = QCAP;
 constexpr unsigned long long BMTD_EDGES = 65536;  // top-down from the bitmap up to this many frontier edges
-// Sparse phase (bfs_sparse.cu): used on graphs whose largest out-degree is
-// at most SPARSE_MAX_DEGREE (meshes, grids, road networks: long searches of
-// small frontiers), from level SPARSE_YIELD_LEVEL on, for frontiers of up
-// to SPARSE_ENTER_F vertices, until one exceeds SPARSE_LEAVE_F.  Measured
-// on the 7000 x 7000 grid, a level costs the grid kernel (one CTA per SM,
-// below) 8.2 us for frontiers of 6 k to 14 k vertices and the 16-CTA
-// cluster 5.2 us below 1 k, 6.4 us at 2-4 k, 7.8 us at 4-6 k, 9.3 us at
-// 6-8 k: the two cross near 5 k.
-// SPARSE_PHASES bounds the hand-overs: a search is queued as grid launch,
-// then (cluster launch, grid launch) SPARSE_PHASES times, and a launch
-// with nothing left to do returns at once.
-constexpr int SPARSE_MAX_DEGREE = 16;
-constexpr int SPARSE_YIELD_LEVEL = 16;
-constexpr int SPARSE_ENTER_F = 4500;
-constexpr int SPARSE_LEAVE_F = 6000;
-// In such a search the grid kernel runs only the larger, latency-bound
-// frontiers; one CTA per SM halves its barrier and counter traffic (7000^2
-// grid: 53.8 ms against 57.1 ms with two).
-constexpr int SPARSE_GRID_BPS = 1;
-constexpr int SPARSE_PHASES = 2;
+// Long searches on graphs whose largest out-degree is at most
+// RELAX_MAX_DEGREE (meshes, grids, road networks: thousands of levels of
+// small frontiers): from level RELAX_YIELD_LEVEL on, at a top-down frontier
+// of at most RELAX_ENTER_F vertices, the grid kernel parks its loop and the
+// label-correcting kernel (bfs_relax.cu) queued behind it finishes the
+// search, advancing pieces of the frontier many levels per grid-wide
+// barrier.  Measured on the 7000 x 7000 grid (7,194 levels): 18.9 ms,
+// against 78 ms level by level in the grid kernel.
+constexpr int RELAX_MAX_DEGREE = 16;
+constexpr int RELAX_YIELD_LEVEL = 4;
+constexpr int RELAX_ENTER_F = 4500;
 
 // A warp's staging queue whose entries carry their row bounds (row[v],
 // row[v + 1]), so the next level reads a frontier vertex's edge range with
@@ -492,10 +483,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
     unsigned epoch = 0;
     if (a.resume) {
         // a continuation: nothing to do when the search has ended or failed,
-        // or when it was handed to the sparse-phase kernel and that kernel
-        // did not take it (it only declines after a device error)
+        // or when it was handed to the label-correcting kernel
         const int done = ctrl->rs.done, mode = ctrl->rs.mode, status = ctrl->status;
-        if (done || mode == RESUME_SPARSE || status != DEV_OK) return;
+        if (done || mode == RESUME_RELAX || status != DEV_OK) return;
     } else if (gtid == 0) {
         ctrl->t_entry = globaltimer_ns();
     }
@@ -619,15 +609,14 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
         else if (a.direction == GBFS_DIR_BOTTOMUP) bu = true;
         else if (td) bu = (long long)mf * a.alpha > m_u;
         else bu = !((long long)nf * a.beta < a.n_active && nf < prev_nf);
-        // a long run of small top-down frontiers (a high-diameter graph):
-        // hand the loop to the sparse-phase cluster kernel queued after
+        // a long search of small top-down frontiers (a high-diameter
+        // graph): hand the loop to the label-correcting kernel queued after
         // this launch, with frontier L still in its queue
-        if (a.may_yield && td && !bu && L >= a.yield_level && nf <= (unsigned long long)a.sparse_enter_f &&
-            (long long)((nf + a.sparse_ctas - 1) / a.sparse_ctas) * a.max_degree <= a.sparse_cap) {
+        if (a.may_yield && td && !bu && L >= a.yield_level && nf <= (unsigned long long)a.yield_max_f) {
             reached -= nf;
             edges_c -= mf;
             m_u += (long long)mf;
-            park(RESUME_SPARSE);
+            park(RESUME_RELAX);
             return;
         }
         prev_nf = nf;
@@ -1218,11 +1207,8 @@ BfsArgs make_args(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const in
     a.has_big = g.max_degree >= a.big_degree ? 1 : 0;
     a.max_degree = std::max(1, (int)g.max_degree);
     a.may_yield = 0;
-    a.yield_level = SPARSE_YIELD_LEVEL;
-    a.sparse_ctas = 1;
-    a.sparse_cap = 0;
-    a.sparse_enter_f = SPARSE_ENTER_F;
-    a.sparse_leave_f = SPARSE_LEAVE_F;
+    a.yield_level = RELAX_YIELD_LEVEL;
+    a.yield_max_f = RELAX_ENTER_F;
     a.timeout_ns = (unsigned long long)std::max(1, p.timeout_ms) * 1000000ull;
     return a;
 }
@@ -1310,48 +1296,27 @@ cudaError_t add_bfs_node(cudaGraph_t g, const cudaGraphNode_t *dep, size_t ndep,
 
 }  // namespace
 
-int bfs_sparse_ctas(const DeviceCsr &g, const gbfs_params &p)
+bool bfs_relax_tail(const DeviceCsr &g, const gbfs_params &p)
 {
-    if (p.per_level_launch || p.direction == GBFS_DIR_BOTTOMUP || g.max_degree > SPARSE_MAX_DEGREE) return 0;
-    int ctas = 0, cap = 0;
-    if (bfs_sparse_shape(ctas, cap) != cudaSuccess) return 0;
-    return ctas;
+    return !p.per_level_launch && p.direction != GBFS_DIR_BOTTOMUP && g.max_degree <= RELAX_MAX_DEGREE;
 }
 
-int bfs_launches_per_search(const DeviceCsr &g, const gbfs_params &p)
-{
-    return bfs_sparse_ctas(g, p) > 0 ? 1 + 2 * SPARSE_PHASES : 1;
-}
+int bfs_launches_per_search(const DeviceCsr &g, const gbfs_params &p) { return bfs_relax_tail(g, p) ? 2 : 1; }
 
 cudaError_t bfs_enqueue(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_roots, int k,
                         int single_root, int *d_level, BfsOut *slot, cudaStream_t st, bool symmetric, int resume,
                         int max_steps, int max_ctas)
 {
     BfsArgs a = make_args(g, p, w, d_roots, k, single_root, d_level, slot, symmetric, resume, max_steps);
-    if (resume || max_steps || bfs_sparse_ctas(g, p) == 0)
+    if (resume || max_steps || !bfs_relax_tail(g, p))
         return bfs_launch_any(a, p.threads_per_block, p.blocks_per_sm, st, max_ctas);
-    // a graph of small degree: the grid kernel may hand runs of small
-    // frontiers to the sparse-phase cluster kernel queued behind it, which
-    // hands larger ones back to the resuming grid launch behind it, and so
-    // on SPARSE_PHASES times (the last grid launch keeps the search); every
-    // later launch returns at once when the search is already complete
-    int ctas = 0, cap = 0;
-    cudaError_t e = bfs_sparse_shape(ctas, cap);
-    if (e != cudaSuccess) return e;
+    // a graph of small degree: a search still running at level
+    // RELAX_YIELD_LEVEL with a small frontier is finished by the
+    // label-correcting kernel queued behind the grid launch (which returns
+    // at once when the search ended in the grid launch)
     a.may_yield = 1;
-    a.sparse_ctas = ctas;
-    a.sparse_cap = cap;
-    const int bps = std::min(p.blocks_per_sm, SPARSE_GRID_BPS);
-    e = bfs_launch_any(a, p.threads_per_block, bps, st, max_ctas);
-    for (int ph = 0; ph < SPARSE_PHASES && e == cudaSuccess; ph++) {
-        e = bfs_sparse_launch(a, st);
-        if (e == cudaSuccess) {
-            BfsArgs r = a;
-            r.resume = 1;
-            r.may_yield = ph + 1 < SPARSE_PHASES ? 1 : 0;
-            e = bfs_launch_any(r, p.threads_per_block, bps, st, max_ctas);
-        }
-    }
+    cudaError_t e = bfs_launch_any(a, p.threads_per_block, p.blocks_per_sm, st, max_ctas);
+    if (e == cudaSuccess) e = bfs_relax_launch(a, st, max_ctas);
     return e;
 }
 

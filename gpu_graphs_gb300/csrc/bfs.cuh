@@ -17,7 +17,9 @@ namespace gbfs {
 struct LevelTrace {
     int level;                   // frontier index L expanded by this step
     int dir;                     // 0 top-down, 1 bottom-up, +2 if a grid-split pass ran,
-                                 // 4 top-down in the sparse-phase cluster kernel
+                                 // 4 one round of the label-correcting kernel (up to
+                                 // RX_HOPS levels; `level` counts rounds on from the
+                                 // level it took over at)
     unsigned long long frontier; // vertices in frontier L
     unsigned long long edges;    // their out-edges
     unsigned long long t_ns;     // %globaltimer when the step's last barrier completed
@@ -33,12 +35,11 @@ struct BfsOut {
 // Who continues a parked level loop (BfsResume::mode).
 enum ResumeMode : int {
     RESUME_LEVEL = 0,     // per-level-launch mode: the next grid launch
-    RESUME_SPARSE = 1,    // the sparse-phase cluster kernel
-    RESUME_HANDBACK = 2,  // the grid kernel again, after the sparse phase
+    RESUME_RELAX = 1,     // the label-correcting kernel (bfs_relax.cu), to the end
 };
 
 // Level-loop state kept between launches (per-level-launch mode, and the
-// hand-over between the grid kernel and the sparse-phase cluster kernel).
+// hand-over from the grid kernel to the label-correcting kernel).
 struct BfsResume {
     long long m_u;
     unsigned long long prev_nf, reached, edges_c, roots, prev_mf;
@@ -67,6 +68,9 @@ struct BfsCtrl {
     unsigned long long fill;     // bitmap -> queue conversion slots
     BfsOut out;                  // results of the last traversal (default slot)
     BfsResume rs;                // per-level-launch mode: state between launches
+    unsigned long long rx_reached, rx_edges;  // label-correcting phase: first relaxations
+    int rx_max;                  // and the largest level
+    int pad4;
     unsigned long long t_entry;  // %globaltimer when CTA 0 started
     unsigned long long t_start;  // %globaltimer after initialisation
     unsigned long long t_end;    // %globaltimer when CTA 0 left the level loop
@@ -142,10 +146,10 @@ cudaError_t bfs_enqueue(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, co
 int bfs_run(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_roots, int k,
             int single_root, int *d_level, cudaStream_t st, BfsResult &res, std::string &err, bool symmetric);
 
-// Cluster CTAs of the sparse-phase kernel a search with these parameters
-// may use on graph g (0: single persistent launches only), and the kernel
-// launches one search enqueues (1, or 3 with the sparse phase).
-int bfs_sparse_ctas(const DeviceCsr &g, const gbfs_params &p);
+// Whether a search with these parameters on graph g ends in the
+// label-correcting kernel, and the kernel launches one search enqueues
+// (2 then, else 1).
+bool bfs_relax_tail(const DeviceCsr &g, const gbfs_params &p);
 int bfs_launches_per_search(const DeviceCsr &g, const gbfs_params &p);
 
 // CTAs of one full-GPU single-source launch with these parameters (0 on error).

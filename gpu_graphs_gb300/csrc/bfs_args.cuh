@@ -1,6 +1,6 @@
 // bfs_args.cuh -- launch arguments shared by the single-source kernels:
-// the persistent grid kernel (bfs.cu) and the sparse-phase cluster kernel
-// (bfs_sparse.cu), which continue one another's level loop.
+// the persistent grid kernel (bfs.cu) and the label-correcting kernel
+// (bfs_relax.cu) that finishes long searches on graphs of small degree.
 #pragma once
 
 #include "bfs.cuh"
@@ -34,25 +34,17 @@ struct BfsArgs {
     int alpha, beta, big_degree, direction;
     int has_big;             // some row has big_degree entries or more (else none is ever deferred)
     int max_degree;          // largest out-degree
-    // sparse phase: the grid kernel may hand a run of small top-down
-    // frontiers (at most sparse_enter_f vertices) to the cluster kernel
-    // launched right after it, from level yield_level on, when each of the
-    // cluster's sparse_ctas CTAs can hold the next frontier
-    // (ceil(frontier / sparse_ctas) * max_degree entries <= sparse_cap); the
-    // cluster kernel hands back frontiers of more than sparse_leave_f
+    // the grid kernel may park its level loop for the label-correcting
+    // kernel launched right after it: from level yield_level on, at a
+    // top-down frontier of at most yield_max_f vertices
     int may_yield;
     int yield_level;
-    int sparse_ctas;
-    int sparse_cap;
-    int sparse_enter_f;
-    int sparse_leave_f;
+    int yield_max_f;
     unsigned long long timeout_ns;
 };
 
-// The sparse-phase cluster kernel (bfs_sparse.cu): its cluster size (0 when
-// no such cluster fits this device) and per-CTA queue capacity, and its
-// launch (one cluster, after a grid launch with may_yield set).
-cudaError_t bfs_sparse_shape(int &ctas, int &cap);
-cudaError_t bfs_sparse_launch(const BfsArgs &args, cudaStream_t st);
+// The label-correcting kernel (bfs_relax.cu), queued after a grid launch
+// with may_yield set: it finishes a search the grid launch parked.
+cudaError_t bfs_relax_launch(const BfsArgs &args, cudaStream_t st, int max_ctas);
 
 }  // namespace gbfs

@@ -119,10 +119,7 @@ int gbfs_graph_get_csr(const gbfs_graph *g, int32_t *row_offset,
 
 typedef struct gbfs_params {
     int32_t threads_per_block;  /* 256, 512 or 1024                         */
-    int32_t blocks_per_sm;      /* persistent CTAs per SM (capped by occupancy;
-                                   on graphs of out-degree <= 16, whose
-                                   searches have a sparse phase on one
-                                   thread-block cluster, at most 1)        */
+    int32_t blocks_per_sm;      /* persistent CTAs per SM (capped by occupancy) */
     int32_t alpha;              /* TD->BU when frontier edges > unexplored/alpha */
     int32_t beta;               /* BU->TD when frontier vertices < n/beta    */
     int32_t big_degree;         /* TD rows >= this are split across the grid */
@@ -160,11 +157,12 @@ typedef struct gbfs_stats {
     int32_t td_levels;          /* levels expanded top-down                 */
     int32_t bu_levels;          /* levels expanded bottom-up                */
     int32_t launches;           /* kernel launches this call queued per
-                                   search: 1; 5 on graphs of out-degree
-                                   <= 16 (grid and cluster launches of the
-                                   sparse phase, each returning at once
-                                   when the search is already done); one
-                                   per level (+1) with per_level_launch    */
+                                   search: 1; 2 on graphs of out-degree
+                                   <= 16 (the grid launch and the
+                                   label-correcting launch that finishes a
+                                   long search, returning at once when the
+                                   search is already done); one per level
+                                   (+1) with per_level_launch              */
     int64_t vertices_reached;   /* vertices with level >= 0 (all sources)   */
     int64_t edges_in_component; /* out-edges of reached vertices (E_c)      */
     int64_t edges_traversed;    /* reference convention: discovered vertices
@@ -212,9 +210,11 @@ int gbfs_bfs_many(gbfs_graph *g, const int32_t *sources, int32_t k,
 typedef struct gbfs_level_trace {
     int32_t level;              /* frontier expanded by this step            */
     int32_t direction;          /* 0 top-down, 1 bottom-up, 2 top-down with
-                                   a grid-split pass over long rows, 4
-                                   top-down on one thread-block cluster
-                                   (the sparse phase of small-degree graphs) */
+                                   a grid-split pass over long rows, 4 one
+                                   round of the label-correcting phase of
+                                   long searches on small-degree graphs (up
+                                   to 64 levels; from the level it took
+                                   over at, `level` counts rounds)         */
     int64_t frontier_vertices;
     int64_t frontier_edges;     /* out-edges of the frontier                 */
     double  t_us;               /* end of the step, us after initialisation  */

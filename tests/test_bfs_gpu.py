@@ -102,10 +102,10 @@ def test_grid_high_diameter(gb, orc):
     g, o = _check_against_oracle(gb, orc, side * side, src, dst, [0, side * side // 2 + 7])
     want, st = g.bfs(0, stats=True)
     assert st.levels > side  # hundreds of levels
-    # degree <= 16: the persistent grid launch hands the small frontiers to
-    # the sparse-phase cluster launch queued behind it (grid, cluster, grid,
-    # cluster, grid; launches with nothing left return at once)
-    assert st.launches == 5
+    # degree <= 16: the persistent grid launch hands the search to the
+    # label-correcting launch queued behind it at level 4
+    assert st.launches == 2
+    assert any(r["dir"] == "relaxed" for r in g.last_trace())
     g.set_params(per_level_launch=1)  # the reference's shape: a launch per level
     got, st2 = g.bfs(0, stats=True)
     assert np.array_equal(got, want)
@@ -404,10 +404,12 @@ def _bounded_degree_graph(n_path: int, n_exp: int, seed: int):
 
 
 @pytest.mark.parametrize("direction", [0, 1])
-def test_sparse_phase_hands_back(gb, orc, direction):
-    """The sparse phase takes over on a long thin start (level 16 on), then
-    the frontier outgrows the cluster's queues and the grid kernel resumes
-    (and may step bottom-up); levels stay exact from several sources."""
+def test_relaxed_phase_thin_start(gb, orc, direction):
+    """The label-correcting phase takes over on a long thin start (level 4
+    on) and keeps the search when the frontier explodes into the bounded-
+    degree random part (pieces too large to hop: one level per round);
+    levels and counts stay exact from several sources, including ones in
+    the random part, where the grid kernel steps bottom-up first."""
     n, src, dst = _bounded_degree_graph(40, 1 << 20, 7)
     g = gb.Graph.from_edges(n, src, dst, gb.UNDIRECTED)
     assert g.max_degree <= 16
@@ -416,8 +418,10 @@ def test_sparse_phase_hands_back(gb, orc, direction):
     for s0 in (0, 5, 39, 40 + 12345, n - 1):
         got, st = g.bfs(s0, stats=True)
         assert np.array_equal(got, orc.bfs_queue(o, s0)), s0
-        assert st.launches == 5
+        assert st.launches == 2
         assert st.vertices_reached == int((got >= 0).sum())
+        assert st.edges_in_component == orc.component_edges(o, got)
+        assert st.levels == int(got.max()) + 1
     # back-to-back launches and a device output buffer
     sources = [0, 40 + 7, 3]
     outs, sts = g.bfs_many(sources)
@@ -425,7 +429,7 @@ def test_sparse_phase_hands_back(gb, orc, direction):
         assert np.array_equal(outs[i], orc.bfs_queue(o, s0))
 
 
-def test_sparse_phase_multiroot_and_directed(gb, orc):
+def test_relaxed_phase_multiroot_and_directed(gb, orc):
     side = 300
     src, dst = gb.gen_grid(side, 0.1, 0.001, 8, seed=11)
     n = side * side
@@ -441,3 +445,52 @@ def test_sparse_phase_multiroot_and_directed(gb, orc):
     od = orc.csr_build(n, src, dst, orc.DEDUP | orc.DROP_SELF_LOOPS)
     for s0 in (0, n // 3):
         assert np.array_equal(gd.bfs(s0), orc.bfs_queue(od, s0))
+
+
+def _ring_with_chords(n: int, chords: int, reach: int, seed: int):
+    rng = np.random.default_rng(seed)
+    a = np.arange(n, dtype=np.int64)
+    c = rng.integers(0, n, chords)
+    src = np.concatenate([a, c]).astype(np.int32)
+    dst = np.concatenate([(a + 1) % n, (c + rng.integers(2, reach + 1, chords)) % n]).astype(np.int32)
+    return src, dst
+
+
+def test_relaxed_phase_shapes(gb, orc):
+    """Label-correcting rounds on shapes that stress them: a ring whose two
+    arms meet at the far end (pieces of different CTAs race towards the same
+    vertices) with short chords (a CTA can reach a vertex before the piece
+    holding its shortest path), a long path (one-vertex frontiers, hundreds
+    of rounds), a directed comb whose teeth are sinks (reached vertices of
+    out-degree 0) and several components; levels, reached counts, component
+    edges and level counts against the oracle."""
+    cases = []
+    n = 200_000
+    s_, d_ = _ring_with_chords(n, 400, 8, 3)
+    cases.append(("ring", n, s_, d_, gb.UNDIRECTED, orc.UNDIRECTED, [0, 12345, n - 1]))
+    n = 60_000
+    s_ = np.arange(n - 1, dtype=np.int32)
+    cases.append(("path", n, s_, s_ + 1, gb.UNDIRECTED, orc.UNDIRECTED, [0, n // 2 + 3]))
+    k = 30_000  # comb: 0 -> 1 -> ... -> k-1, tooth i -> k + i (a sink)
+    spine = np.arange(k - 1, dtype=np.int32)
+    teeth = np.arange(k, dtype=np.int32)
+    cases.append(("comb", 2 * k, np.concatenate([spine, teeth]), np.concatenate([spine + 1, teeth + k]),
+                  gb.DEDUP | gb.DROP_SELF_LOOPS, orc.DEDUP | orc.DROP_SELF_LOOPS, [0, 7, k + 3]))
+    side = 500  # two grids and an isolated path
+    gs, gd = gb.gen_grid(side, 0.1, 0.001, 8, seed=5)
+    m = side * side
+    extra = np.arange(2 * m, 2 * m + 999, dtype=np.int32)
+    cases.append(("components", 2 * m + 1000, np.concatenate([gs, gs + m, extra]),
+                  np.concatenate([gd, gd + m, extra + 1]), gb.UNDIRECTED, orc.UNDIRECTED, [0, m + 17, 2 * m + 5]))
+    for name, n, s_, d_, flags, oflags, sources in cases:
+        g = gb.Graph.from_edges(n, s_, d_, flags)
+        assert g.max_degree <= 16, name
+        o = orc.csr_build(n, s_, d_, oflags)
+        for s0 in sources:
+            got, st = g.bfs(s0, stats=True)
+            want = orc.bfs_queue(o, s0)
+            assert np.array_equal(got, want), (name, s0)
+            assert st.vertices_reached == int((want >= 0).sum()), (name, s0)
+            assert st.edges_in_component == orc.component_edges(o, want), (name, s0)
+            assert st.levels == int(want.max()) + 1, (name, s0)
+            assert st.launches == 2

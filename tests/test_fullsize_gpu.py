@@ -70,7 +70,7 @@ def test_grid_7000_full_size(gb, orc):
     deg = np.diff(row)
     s = int(np.random.default_rng(2).choice(np.flatnonzero(deg > 0)))
     got, st = g.bfs(s, stats=True)
-    assert st.levels > 1000 and st.launches == 5  # grid and sparse-phase cluster launches
+    assert st.levels > 1000 and st.launches == 2  # grid and label-correcting launches
     check_bfs_properties(row, col, got, s)
     o = orc.CSR(n, row.astype(np.int64), col)
     assert np.array_equal(got, orc.bfs_queue(o, s))
