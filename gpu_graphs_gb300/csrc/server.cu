@@ -4,15 +4,25 @@
 // Here a server keeps graphs resident, admits them against an HBM budget and
 // answers queries as they arrive:
 //   * every query joins its graph's FIFO;
-//   * `num_slots` worker threads, each owning a CUDA stream and a 64-lane
-//     multi-source workspace sized for the largest admitted graph, take the
-//     ready graph whose oldest query has waited longest and pack up to
-//     `max_lanes` of its queries into one multi-source launch.  A graph is
-//     ready with a full batch or once its oldest query has waited
-//     `batch_window_us`, or `window_pct` percent of the graph's recent launch
-//     time if longer: a launch costs about the same for one source as for
-//     64, so slow graphs gather bigger batches, while other graphs' queries
-//     keep the slots busy meanwhile;
+//   * `num_slots` worker threads, each owning CUDA streams, a 64-lane
+//     multi-source workspace and SRV_SUB single-source workspaces sized for
+//     the largest admitted graph, take the ready graph whose oldest query
+//     has waited longest:
+//       - on most graphs they pack up to `max_lanes` of its queries into one
+//         multi-source launch.  Such a graph is ready with a full batch or
+//         once its oldest query has waited `batch_window_us`, or
+//         `window_pct` percent of the graph's recent launch time if longer:
+//         a launch costs about the same for one source as for 64, so slow
+//         graphs gather bigger batches, while other graphs' queries keep the
+//         slots busy meanwhile;
+//       - on a graph of small degree (meshes, grids, road networks) a
+//         search is a long chain of latency-bound levels that the
+//         label-correcting kernel runs at about the same speed on a quarter
+//         of the GPU, while a multi-source launch is bound by its lanes'
+//         combined frontiers; such a graph is ready as soon as it has a
+//         query, and a slot runs up to SRV_SUB of its queries as that many
+//         single-source searches at once, on its own streams, each capped
+//         to its share of the slot's CTAs;
 //   * slots run concurrently on their streams, each launch capped to
 //     1/num_slots of the GPU's CTAs so all of them fit on the GPU together
 //     (every launch waits on all of its own CTAs);
@@ -59,13 +69,26 @@ struct SrvGraph {
     std::deque<std::shared_ptr<SrvQuery>> pending;
     int inflight = 0;
     double est_us = 0;   // recent launch time (moving average), 0 before the first
+    bool singles = false;  // small degree: served as concurrent single-source searches
 };
 
-// 64-lane workspace + single-source workspace (level, 3 bitmaps + visited,
-// 4 int lists, the row bounds beside the two queues, the control block)
+// Single-source searches a slot runs at once on a graph of small degree.
+// Four slots on a 4000 x 4000 grid, 64 queries at once: 224 ms with four
+// searches per slot, 283 ms with two slots of four; batching a graph's
+// queries into multi-source launches from 16 pending on instead cut the
+// serving mix's capacity from 1,377 to 1,249 queries/s.
+#ifndef SRV_SUB_DEF
+#define SRV_SUB_DEF 4
+#endif
+constexpr int SRV_SUB = SRV_SUB_DEF;
+
+// 64-lane workspace + SRV_SUB single-source workspaces (level, 3 bitmaps +
+// visited, 4 int lists, the row bounds beside the two queues, the control
+// block)
 int64_t slot_bytes(int64_t n)
 {
-    return n > 0 ? ms_work_bytes(n) + 4 * n * 5 + 16 * n + n / 2 + (int64_t)sizeof(BfsCtrl) + (1 << 20) : 0;
+    return n > 0 ? ms_work_bytes(n) + SRV_SUB * (4 * n * 5 + 16 * n + n / 2 + (int64_t)sizeof(BfsCtrl)) + (1 << 20)
+                 : 0;
 }
 
 double ms_between(Clock::time_point a, Clock::time_point b)
@@ -106,9 +129,9 @@ struct gbfs_server {
     double lanes_sum = 0;
     // slots
     struct Slot {
-        cudaStream_t st = nullptr;
-        MsWork w;       // 64-lane workspace (batches of two or more)
-        BfsWork bw;     // single-source workspace (batches of one)
+        cudaStream_t st[SRV_SUB] = {};  // st[0]: multi-source batches and the first search of a group
+        MsWork w;                       // 64-lane workspace (multi-source batches)
+        BfsWork bw[SRV_SUB];            // single-source workspaces (one per concurrent search)
         int64_t cap = 0;
     };
     int bfs_ctas = 0;   // CTA cap of a single-source launch in a slot
@@ -145,7 +168,7 @@ void gbfs_server::worker(int idx)
                         const double window_us =
                             std::min(1e6, std::max<double>(cfg.batch_window_us, 0.01 * cfg.window_pct * c.est_us));
                         const auto ready_at = t0 + std::chrono::microseconds((int64_t)window_us);
-                        if ((int)c.pending.size() >= cfg.max_lanes || now >= ready_at || stop) {
+                        if (c.singles || (int)c.pending.size() >= cfg.max_lanes || now >= ready_at || stop) {
                             if (t0 < oldest) {
                                 oldest = t0;
                                 sg = &c;
@@ -161,7 +184,7 @@ void gbfs_server::worker(int idx)
                 if (next_ready != Clock::time_point::max()) cv_work.wait_until(lk, next_ready);
                 else cv_work.wait(lk);
             }
-            const int k = std::min<int>((int)sg->pending.size(), cfg.max_lanes);
+            const int k = std::min<int>((int)sg->pending.size(), sg->singles ? SRV_SUB : cfg.max_lanes);
             batch.clear();
             srcs.clear();
             const auto now = Clock::now();
@@ -183,53 +206,71 @@ void gbfs_server::worker(int idx)
         const auto t_launch = Clock::now();
         const DeviceCsr &csr = sg->csr;
         const size_t n = (size_t)csr.n;
-        int status = GBFS_OK;
         gbfs_params p = graph_params(g);
         p.timeout_ms = cfg.timeout_ms;
         if (!g->symmetric && !csr.trow) p.direction = GBFS_DIR_TOPDOWN;  // bottom-up needs in-edges
-        cudaError_t e = cudaSuccess;
-        int dev_status = DEV_OK;
-        if (k == 1) {
-            // one query: the single-source direction-optimising kernel
-            e = bfs_enqueue(csr, p, slot.bw, nullptr, 1, srcs[0], slot.bw.level, &slot.bw.ctrl->out, slot.st,
-                            g->symmetric, 0, 0, bfs_ctas);
-            if (e == cudaSuccess)
-                e = cudaMemcpyAsync(&slot.bw.h_ctrl->status, &slot.bw.ctrl->status, sizeof(int),
-                                    cudaMemcpyDeviceToHost, slot.st);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(slot.st);
-            if (e == cudaSuccess) dev_status = slot.bw.h_ctrl->status;
-            if (e == cudaSuccess && dev_status == DEV_OK)
-                e = cudaMemcpyAsync(batch[0]->out, slot.bw.level, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
-                                    slot.st);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(slot.st);
-            if (e == cudaSuccess && dev_status != DEV_OK) {
-                cudaMemsetAsync(slot.bw.ctrl, 0, sizeof(BfsCtrl), slot.st);
-                cudaStreamSynchronize(slot.st);
+        // per query: 0, or a status
+        int qstatus[MS_LANES];
+        for (int i = 0; i < k; i++) qstatus[i] = GBFS_OK;
+        if (k == 1 || (k <= SRV_SUB && bfs_relax_tail(csr, p))) {
+            // one query, or up to SRV_SUB on a graph of small degree: that
+            // many single-source searches at once, each on its own stream
+            // and workspace, sharing the slot's CTAs
+            const int cap = k == 1 ? bfs_ctas : std::max(1, bfs_ctas / k);
+            cudaError_t es[SRV_SUB];
+            for (int j = 0; j < k; j++) {
+                BfsWork &bw = slot.bw[j];
+                es[j] = bfs_enqueue(csr, p, bw, nullptr, 1, srcs[j], bw.level, &bw.ctrl->out, slot.st[j],
+                                    g->symmetric, 0, 0, cap);
+                if (es[j] == cudaSuccess)
+                    es[j] = cudaMemcpyAsync(&bw.h_ctrl->status, &bw.ctrl->status, sizeof(int), cudaMemcpyDeviceToHost,
+                                            slot.st[j]);
+            }
+            for (int j = 0; j < k; j++) {
+                BfsWork &bw = slot.bw[j];
+                if (es[j] == cudaSuccess) es[j] = cudaStreamSynchronize(slot.st[j]);
+                const int dev_status = es[j] == cudaSuccess ? bw.h_ctrl->status : DEV_OK;
+                if (es[j] == cudaSuccess && dev_status == DEV_OK)
+                    es[j] = cudaMemcpyAsync(batch[j]->out, bw.level, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
+                                            slot.st[j]);
+                if (es[j] == cudaSuccess && dev_status != DEV_OK) {
+                    cudaMemsetAsync(bw.ctrl, 0, sizeof(BfsCtrl), slot.st[j]);
+                    qstatus[j] = GBFS_ERR_TIMEOUT;
+                }
+            }
+            for (int j = 0; j < k; j++) {
+                if (es[j] == cudaSuccess) es[j] = cudaStreamSynchronize(slot.st[j]);
+                if (es[j] != cudaSuccess) qstatus[j] = GBFS_ERR_CUDA;
             }
         } else {
-            e = cudaMemcpyAsync(slot.w.src, srcs.data(), sizeof(int32_t) * k, cudaMemcpyHostToDevice, slot.st);
+            cudaError_t e = cudaMemcpyAsync(slot.w.src, srcs.data(), sizeof(int32_t) * k, cudaMemcpyHostToDevice,
+                                            slot.st[0]);
+            int dev_status = DEV_OK;
             if (e == cudaSuccess)
-                e = msbfs_enqueue(csr, p, g->symmetric, slot.w, slot.w.src, k, slot.w.out, slot.st, max_ctas);
+                e = msbfs_enqueue(csr, p, g->symmetric, slot.w, slot.w.src, k, slot.w.out, slot.st[0], max_ctas);
             if (e == cudaSuccess)
-                e = cudaMemcpyAsync(slot.w.h_ctrl, slot.w.ctrl, offsetof(MsCtrl, t_entry), cudaMemcpyDeviceToHost, slot.st);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(slot.st);
+                e = cudaMemcpyAsync(slot.w.h_ctrl, slot.w.ctrl, offsetof(MsCtrl, t_entry), cudaMemcpyDeviceToHost,
+                                    slot.st[0]);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(slot.st[0]);
             if (e == cudaSuccess) dev_status = slot.w.h_ctrl->status;
             if (e == cudaSuccess && dev_status != DEV_OK) {
-                cudaMemsetAsync(slot.w.ctrl, 0, sizeof(MsCtrl), slot.st);
-                cudaStreamSynchronize(slot.st);
+                cudaMemsetAsync(slot.w.ctrl, 0, sizeof(MsCtrl), slot.st[0]);
+                cudaStreamSynchronize(slot.st[0]);
             } else if (e == cudaSuccess) {
                 for (int i = 0; i < k && e == cudaSuccess; i++)
                     e = cudaMemcpyAsync(batch[i]->out, slot.w.out + n * i, sizeof(int32_t) * n,
-                                        cudaMemcpyDeviceToHost, slot.st);
-                if (e == cudaSuccess) e = cudaStreamSynchronize(slot.st);
+                                        cudaMemcpyDeviceToHost, slot.st[0]);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(slot.st[0]);
             }
+            const int status = e != cudaSuccess ? GBFS_ERR_CUDA : dev_status != DEV_OK ? GBFS_ERR_TIMEOUT : GBFS_OK;
+            for (int i = 0; i < k; i++) qstatus[i] = status;
         }
-        if (e != cudaSuccess) status = GBFS_ERR_CUDA;
-        else if (dev_status != DEV_OK) status = GBFS_ERR_TIMEOUT;
         {
             std::lock_guard<std::mutex> lk(mu);
             const auto now = Clock::now();
-            for (auto &q : batch) {
+            for (int i = 0; i < k; i++) {
+                auto &q = batch[i];
+                const int status = qstatus[i];
                 q->status = status;
                 q->done = true;
                 q->latency_ms = ms_between(q->t_submit, now);
@@ -290,10 +331,11 @@ extern "C" int gbfs_server_create(const gbfs_server_config *cfg, gbfs_server **o
     }
     s->slots.resize(cfg->num_slots);
     for (auto &sl : s->slots)
-        if (cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking) != cudaSuccess) {
-            gbfs_server_destroy(s);
-            return fail(GBFS_ERR_CUDA, "cudaStreamCreate");
-        }
+        for (auto &st : sl.st)
+            if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+                gbfs_server_destroy(s);
+                return fail(GBFS_ERR_CUDA, "cudaStreamCreate");
+            }
     for (int i = 0; i < cfg->num_slots; i++) s->workers.emplace_back(&gbfs_server::worker, s, i);
     *out = s;
     return GBFS_OK;
@@ -310,10 +352,12 @@ extern "C" void gbfs_server_destroy(gbfs_server *s)
     for (auto &t : s->workers)
         if (t.joinable()) t.join();
     for (auto &sl : s->slots) {
-        if (sl.st) cudaStreamSynchronize(sl.st);
+        for (auto st : sl.st)
+            if (st) cudaStreamSynchronize(st);
         ms_work_free(sl.w);
-        bfs_work_free(sl.bw);
-        if (sl.st) cudaStreamDestroy(sl.st);
+        for (auto &bw : sl.bw) bfs_work_free(bw);
+        for (auto st : sl.st)
+            if (st) cudaStreamDestroy(st);
     }
     delete s;
 }
@@ -344,28 +388,32 @@ extern "C" int gbfs_server_add_graph(gbfs_server *s, gbfs_graph *g, int32_t *gra
         s->cv_done.wait(lk, [&] { return s->busy_slots == 0; });
         std::string err;
         int rc = GBFS_OK;
-        for (auto &sl : s->slots) {
+        auto slot_free = [](gbfs_server::Slot &sl) {
             ms_work_free(sl.w);
-            bfs_work_free(sl.bw);
-            rc = ms_work_alloc(sl.w, (int32_t)new_cap, err);
-            if (!rc) rc = bfs_work_alloc(sl.bw, (int32_t)new_cap, err);
+            for (auto &bw : sl.bw) bfs_work_free(bw);
+            sl.cap = 0;
+        };
+        auto slot_alloc = [](gbfs_server::Slot &sl, int64_t cap, std::string &e) {
+            int r = ms_work_alloc(sl.w, (int32_t)cap, e);
+            for (auto &bw : sl.bw)
+                if (!r) r = bfs_work_alloc(bw, (int32_t)cap, e);
+            if (!r) sl.cap = cap;
+            return r;
+        };
+        for (auto &sl : s->slots) {
+            slot_free(sl);
+            rc = slot_alloc(sl, new_cap, err);
             if (rc) break;
-            sl.cap = new_cap;
         }
         s->resizing = false;
         if (rc) {
-            for (auto &sl : s->slots) {
-                ms_work_free(sl.w);
-                bfs_work_free(sl.bw);
-                sl.cap = 0;
-            }
+            for (auto &sl : s->slots) slot_free(sl);
             const int64_t old = s->n_cap;
             s->n_cap = 0;
             // restore the previous capacity if possible
+            std::string err2;
             for (auto &sl : s->slots)
-                if (old > 0 && ms_work_alloc(sl.w, (int32_t)old, err) == GBFS_OK &&
-                    bfs_work_alloc(sl.bw, (int32_t)old, err) == GBFS_OK)
-                    sl.cap = old;
+                if (old > 0 && slot_alloc(sl, old, err2) != GBFS_OK) slot_free(sl);
             s->n_cap = old;
             s->cv_work.notify_all();
             return fail(rc, "slot workspace: " + err);
@@ -385,6 +433,7 @@ extern "C" int gbfs_server_add_graph(gbfs_server *s, gbfs_graph *g, int32_t *gra
     sg.g = g;
     sg.csr = csr_snapshot;
     sg.bytes = gbytes;
+    sg.singles = bfs_relax_tail(csr_snapshot, graph_params(g));
     s->graphs.emplace(gid, std::move(sg));
     s->resident += gbytes;
     s->peak = std::max(s->peak, s->resident + s->slots_total(s->n_cap));

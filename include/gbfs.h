@@ -366,7 +366,11 @@ int64_t gbfs_gen_grid_capacity(int32_t side, double extra);
  * A server keeps graphs resident, admits them against an HBM budget and
  * answers BFS queries with continuous batching: same-graph queries that
  * arrive while others run are packed into 64-lane multi-source launches as
- * slots (streams with their own workspace) free up. */
+ * slots (streams with their own workspace) free up.  On a graph of
+ * out-degree <= 16 (meshes, grids, road networks: long searches of small
+ * frontiers) a slot instead runs up to 4 of its queries at once as
+ * single-source searches on its own streams, each with a share of the
+ * slot's CTAs (batch_lanes then counts the searches run together). */
 typedef struct gbfs_server gbfs_server;
 
 typedef struct gbfs_server_config {
