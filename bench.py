@@ -79,6 +79,8 @@ def parse_args():
     ap.add_argument("--no-extra", action="store_true", help="skip the grid and batched measurements")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep (32 resident graphs)")
     ap.add_argument("--grid-side", type=int, default=7000)
+    ap.add_argument("--grid-only", action="store_true",
+                    help="only --steps persistent searches on the --grid-side grid (a profiling workload)")
     return ap.parse_args()
 
 
@@ -496,6 +498,26 @@ def measure_grid(side: int, torch) -> dict:
             "levels_identical": same, "levels_identical_oracle": same_oracle}
 
 
+def grid_only(side: int, reps: int) -> dict:
+    """`reps` persistent searches from the grid measurement's source (the
+    grid kernel's first levels, then the label-correcting kernel)."""
+    import gpu_graphs_gb300 as gb
+    import torch
+    src, dst = gb.gen_grid(side, 0.1, 0.001, 8, seed=1)
+    n = side * side
+    g = gb.Graph.from_edges(n, src, dst, gb.UNDIRECTED)
+    del src, dst
+    row, _ = g.csr()
+    source = int(pick_sources(np.diff(row), 1)[0])
+    out = torch.empty(n, dtype=torch.int32, device="cuda")
+    runs = [g.bfs(source, out=out, stats=True)[1] for _ in range(max(1, reps))]
+    st = runs[-1]
+    ms = float(np.mean([r.ms for r in runs]))
+    return {"workload": f"grid {side}x{side}, 10% edges dropped, 0.1% extra edges within radius 8",
+            "vertices": n, "source": source, "levels": int(st.levels), "launches_per_search": int(st.launches),
+            "searches": len(runs), "ms": round(ms, 3), "us_per_level": round(1e3 * ms / max(1, st.levels), 3)}
+
+
 def many_graphs_workload(gen, count: int = 512):
     """The fused-launch configuration: `count` Erdos-Renyi graphs, n
     log-uniform in [2^8, 2^16], 4n sampled pairs each (average degree 8 once
@@ -768,6 +790,9 @@ def main():
         return
     import torch
     torch.cuda.set_device(local)
+    if args.grid_only:
+        print(json.dumps(grid_only(args.grid_side, args.steps)), flush=True)
+        return
     dist = Dist(world, "nccl")
     import gpu_graphs_gb300 as gb
 
