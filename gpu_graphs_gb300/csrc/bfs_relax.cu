@@ -38,6 +38,7 @@
 // (1D Partition/src/gpuBFS.cu:66-100) and its one-launch-per-level
 // linear_bfs expansion (1D Partition/src/gpuBFS_kernels.cu:16-40).
 #include <algorithm>
+#include <type_traits>
 
 #include "bfs.cuh"
 #include "bfs_args.cuh"
@@ -51,7 +52,13 @@ constexpr int RX_BLOCK = 512;
 constexpr int RX_NW = RX_BLOCK / 32;
 constexpr int RX_CAP = 1024;                 // entries of a CTA's local frontier (two held)
 constexpr int RX_PER_T = RX_CAP / RX_BLOCK;  // entries per thread in the degree scan
-constexpr int RX_ILP = 2;                    // edges per thread in flight
+// Edges per thread in flight: local frontiers of up to 64 entries (a few
+// hundred edges per CTA), and larger ones (searches capped to a few CTAs,
+// e.g. the server's concurrent searches: 64 queries on a 4000 x 4000 grid,
+// 16 at once with 19 CTAs each, 248 -> 209 ms with 4 instead of 2; 6 is
+// slower everywhere)
+constexpr int RX_ILP = 2;
+constexpr int RX_ILP_BIG = 4;
 // Levels a CTA advances its piece per round.  7000 x 7000 grid, 7,194
 // levels: 8 hops 21.9 ms, 16 hops 20.1, 32 hops 18.7, 64 hops 18.9 (and
 // 1.3-3.5 % faster than 32 on smaller grids and a 200 k-vertex path).
@@ -138,14 +145,15 @@ __global__ void __launch_bounds__(RX_BLOCK, 2) k_bfs_relax(BfsArgs a)
         // relax the edges (u, w[q]) (w[q] < 0: none) with level[u] + 1;
         // improvements join local frontier `nb` (its counter cnt_nb), or the
         // global queue if `last` or that frontier is full
-        auto relax = [&](const int (&w)[RX_ILP], const int (&u)[RX_ILP], bool last, int nb, unsigned *cnt_nb) {
-            unsigned nd[RX_ILP];
+        auto relax = [&](auto ilp, const int *w, const int *u, bool last, int nb, unsigned *cnt_nb) {
+            constexpr int Q = decltype(ilp)::value;
+            unsigned nd[Q];
 #pragma unroll
-            for (int q = 0; q < RX_ILP; q++) nd[q] = w[q] >= 0 ? __ldcg(lvl + u[q]) + 1u : 0u;  // 0: skip
-            unsigned old[RX_ILP];
-            int2 wb[RX_ILP];
+            for (int q = 0; q < Q; q++) nd[q] = w[q] >= 0 ? __ldcg(lvl + u[q]) + 1u : 0u;  // 0: skip
+            unsigned old[Q];
+            int2 wb[Q];
 #pragma unroll
-            for (int q = 0; q < RX_ILP; q++) {
+            for (int q = 0; q < Q; q++) {
                 old[q] = 0;
                 wb[q] = make_int2(0, 0);
                 if (nd[q] != 0) {
@@ -154,7 +162,7 @@ __global__ void __launch_bounds__(RX_BLOCK, 2) k_bfs_relax(BfsArgs a)
                 }
             }
 #pragma unroll
-            for (int q = 0; q < RX_ILP; q++) {
+            for (int q = 0; q < Q; q++) {
                 const bool imp = nd[q] != 0 && nd[q] < old[q];
                 if (imp) {
                     // the next hop (or round) reads this row: start its fetch into L2
@@ -201,6 +209,7 @@ __global__ void __launch_bounds__(RX_BLOCK, 2) k_bfs_relax(BfsArgs a)
                 const int ex0 = incl - d0 - d1, ex1 = ex0 + d0;
                 const int E = __shfl_sync(FULL, incl, 31);
                 for (int e0 = 0; e0 < E; e0 += RX_BLOCK * RX_ILP) {
+                    if (e0 + (int)(warp * 32) >= E) break;  // no edge left for this warp
                     int w[RX_ILP], u[RX_ILP];
 #pragma unroll
                     for (int q = 0; q < RX_ILP; q++) {
@@ -222,7 +231,7 @@ __global__ void __launch_bounds__(RX_BLOCK, 2) k_bfs_relax(BfsArgs a)
                             u[q] = s_v[cur][i];
                         }
                     }
-                    relax(w, u, last, nb, cnt_nb);
+                    relax(std::integral_constant<int, RX_ILP>{}, w, u, last, nb, cnt_nb);
                 }
                 return;
             }
@@ -258,10 +267,11 @@ __global__ void __launch_bounds__(RX_BLOCK, 2) k_bfs_relax(BfsArgs a)
             }
             __syncthreads();
             const int E = s_tot;
-            for (int e0 = 0; e0 < E; e0 += RX_BLOCK * RX_ILP) {
-                int w[RX_ILP], u[RX_ILP];
+            for (int e0 = 0; e0 < E; e0 += RX_BLOCK * RX_ILP_BIG) {
+                if (e0 + (int)(warp * 32) >= E) break;  // no edge left for this warp
+                int w[RX_ILP_BIG], u[RX_ILP_BIG];
 #pragma unroll
-                for (int q = 0; q < RX_ILP; q++) {
+                for (int q = 0; q < RX_ILP_BIG; q++) {
                     const int e = e0 + q * RX_BLOCK + (int)t;
                     w[q] = -1;
                     u[q] = 0;
@@ -275,7 +285,7 @@ __global__ void __launch_bounds__(RX_BLOCK, 2) k_bfs_relax(BfsArgs a)
                         u[q] = s_v[cur][i];
                     }
                 }
-                relax(w, u, last, nb, cnt_nb);
+                relax(std::integral_constant<int, RX_ILP_BIG>{}, w, u, last, nb, cnt_nb);
             }
         };
 
