@@ -22,12 +22,12 @@ import numpy as np
 
 from . import _lib
 from ._lib import (DEDUP, DIR_BOTTOMUP, DIR_OPTIMIZING, DIR_TOPDOWN, DROP_SELF_LOOPS, HUB_FIRST, SYMMETRIZE,
-                   UNDIRECTED, GbfsError, Params, Stats, check, lib)
+                   UNDIRECTED, WIDE_ROWS, GbfsError, Params, Stats, check, lib)
 
 __all__ = [
     "Graph", "GraphSet", "Server", "GbfsError", "Params", "Stats", "csr", "gpuBFS",
     "read_edge_list", "gen_er", "gen_rmat", "gen_grid", "exclusive_scan", "default_params",
-    "SYMMETRIZE", "DEDUP", "DROP_SELF_LOOPS", "UNDIRECTED", "HUB_FIRST", "DIR_OPTIMIZING", "DIR_TOPDOWN",
+    "SYMMETRIZE", "DEDUP", "DROP_SELF_LOOPS", "UNDIRECTED", "HUB_FIRST", "WIDE_ROWS", "DIR_OPTIMIZING", "DIR_TOPDOWN",
     "DIR_BOTTOMUP", "library_path",
 ]
 
@@ -68,6 +68,7 @@ class Graph:
         self.m = info.m
         self.max_degree = info.max_degree
         self.nonisolated = info.nonisolated
+        self.wide = bool(info.wide)  # 64-bit row offsets
 
     # ---- construction ----
     @classmethod
@@ -127,10 +128,11 @@ class Graph:
         return {k: getattr(info, k) for k, _ in info._fields_}
 
     def csr(self) -> tuple[np.ndarray, np.ndarray]:
-        row = np.empty(self.n + 1, np.int32)
+        """(row offsets, column ids); the offsets are int64 on a wide graph."""
+        row = np.empty(self.n + 1, np.int64 if self.wide else np.int32)
         col = np.empty(max(self.m, 1), np.int32)
-        check(lib.gbfs_graph_get_csr(self._h, C.c_void_p(row.ctypes.data), C.c_void_p(col.ctypes.data)),
-              "gbfs_graph_get_csr")
+        fn = lib.gbfs_graph_get_csr64 if self.wide else lib.gbfs_graph_get_csr
+        check(fn(self._h, C.c_void_p(row.ctypes.data), C.c_void_p(col.ctypes.data)), "gbfs_graph_get_csr")
         return row, col[: self.m]
 
     # ---- parameters ----

@@ -28,6 +28,7 @@ DEDUP = 2
 DROP_SELF_LOOPS = 4
 UNDIRECTED = SYMMETRIZE | DEDUP | DROP_SELF_LOOPS
 HUB_FIRST = 8
+WIDE_ROWS = 16
 
 DIR_OPTIMIZING = 0
 DIR_TOPDOWN = 1
@@ -73,6 +74,8 @@ class GraphInfo(C.Structure):
         ("m", C.c_int64),
         ("nonisolated", C.c_int64),
         ("device_bytes", C.c_int64),
+        ("wide", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 
@@ -140,6 +143,7 @@ SIGNATURES = {
     "gbfs_graph_destroy": (None, [P]),
     "gbfs_graph_get_info": (C.c_int, [P, C.POINTER(GraphInfo)]),
     "gbfs_graph_get_csr": (C.c_int, [P, P, P]),
+    "gbfs_graph_get_csr64": (C.c_int, [P, P, P]),
     "gbfs_default_params": (C.c_int, [C.POINTER(Params)]),
     "gbfs_get_params": (C.c_int, [P, C.POINTER(Params)]),
     "gbfs_set_params": (C.c_int, [P, C.POINTER(Params)]),

@@ -201,8 +201,7 @@ extern "C" int gbfs_graph_from_edges(int32_t n, int64_t m, const int32_t *src, c
     *out = nullptr;
     if (n < 1 || n > INT32_MAX - 1) return fail(GBFS_ERR_INVALID_ARG, "n must be in [1, 2^31-2]");
     if (m < 0 || (m > 0 && (!src || !dst))) return fail(GBFS_ERR_INVALID_ARG, "bad edge arrays");
-    if (flags & ~15u) return fail(GBFS_ERR_INVALID_ARG, "unknown flag bits");
-    if (m > (int64_t)INT32_MAX * 2) return fail(GBFS_ERR_TOO_LARGE, "too many edges");
+    if (flags & ~31u) return fail(GBFS_ERR_INVALID_ARG, "unknown flag bits");
     cudaStream_t st = nullptr;
     int rc = make_stream(&st);
     if (rc) return rc;
@@ -213,7 +212,7 @@ extern "C" int gbfs_graph_from_edges(int32_t n, int64_t m, const int32_t *src, c
     rc = to_device(src, m, st, &d_src, &own_s);
     if (!rc) rc = to_device(dst, m, st, &d_dst, &own_d);
     if (!rc) {
-        rc = csr_build_from_edges(n, m, d_src, d_dst, flags & 7u, st, csr, err);
+        rc = csr_build_from_edges(n, m, d_src, d_dst, flags & (7u | GBFS_WIDE_ROWS), st, csr, err);
         if (!rc && (flags & GBFS_HUB_FIRST)) rc = csr_hub_first(csr, st, err);
         if (rc) set_error(err);
     }
@@ -282,17 +281,51 @@ extern "C" int gbfs_graph_get_info(const gbfs_graph *g, gbfs_graph_info *info)
     info->max_degree = g->csr.max_degree;
     info->nonisolated = g->csr.nonisolated;
     info->device_bytes = csr_device_bytes(g->csr) + g->work.bytes + g->ms.bytes;
+    info->wide = g->csr.wide ? 1 : 0;
+    info->reserved = 0;
     return GBFS_OK;
 }
 
 extern "C" int gbfs_graph_get_csr(const gbfs_graph *g, int32_t *row_offset, int32_t *col_idx)
 {
     if (!g || !row_offset || (g->csr.m > 0 && !col_idx)) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
+    if (g->csr.wide) return fail(GBFS_ERR_TOO_LARGE, "64-bit row offsets: use gbfs_graph_get_csr64");
     gbfs_graph *gg = const_cast<gbfs_graph *>(g);
     std::lock_guard<std::mutex> lk(gg->mu);
     const cudaMemcpyKind kr = is_device_ptr(row_offset) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     const cudaMemcpyKind kc = is_device_ptr(col_idx) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     cudaError_t e = cudaMemcpyAsync(row_offset, g->csr.row, sizeof(int) * ((size_t)g->csr.n + 1), kr, g->stream);
+    if (e == cudaSuccess && g->csr.m > 0)
+        e = cudaMemcpyAsync(col_idx, g->csr.col, sizeof(int) * (size_t)g->csr.m, kc, g->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "CSR download");
+    return GBFS_OK;
+}
+
+extern "C" int gbfs_graph_get_csr64(const gbfs_graph *g, int64_t *row_offset, int32_t *col_idx)
+{
+    if (!g || !row_offset || (g->csr.m > 0 && !col_idx)) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
+    gbfs_graph *gg = const_cast<gbfs_graph *>(g);
+    std::lock_guard<std::mutex> lk(gg->mu);
+    const size_t nr = (size_t)g->csr.n + 1;
+    const bool dev_row = is_device_ptr(row_offset);
+    const cudaMemcpyKind kc = is_device_ptr(col_idx) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    cudaError_t e = cudaSuccess;
+    if (g->csr.wide) {
+        e = cudaMemcpyAsync(row_offset, g->csr.row64, sizeof(int64_t) * nr,
+                            dev_row ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, g->stream);
+    } else {
+        // 32-bit offsets widened on the host
+        std::vector<int32_t> r32(nr);
+        std::vector<int64_t> r64(nr);
+        e = cudaMemcpyAsync(r32.data(), g->csr.row, sizeof(int32_t) * nr, cudaMemcpyDeviceToHost, g->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+        if (e == cudaSuccess) {
+            std::copy(r32.begin(), r32.end(), r64.begin());
+            e = cudaMemcpy(row_offset, r64.data(), sizeof(int64_t) * nr,
+                           dev_row ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost);
+        }
+    }
     if (e == cudaSuccess && g->csr.m > 0)
         e = cudaMemcpyAsync(col_idx, g->csr.col, sizeof(int) * (size_t)g->csr.m, kc, g->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
@@ -336,7 +369,7 @@ static int run_bfs_locked(gbfs_graph *g, const int *d_roots, int k, int single_r
                           BfsResult &res)
 {
     std::string err;
-    int rc = bfs_work_alloc(g->work, g->csr.n, err);
+    int rc = bfs_work_alloc(g->work, g->csr.n, err, g->csr.wide);
     if (rc) return fail(rc, err);
     const bool dev_out = is_device_ptr(levels_out);
     int *d_level = dev_out ? levels_out : g->work.level;
@@ -372,7 +405,7 @@ extern "C" int gbfs_bfs_parents(gbfs_graph *g, int32_t source, int32_t *levels_o
     if (source < 0 || source >= g->csr.n) return fail(GBFS_ERR_INVALID_ARG, "source outside [0, n)");
     std::lock_guard<std::mutex> lk(g->mu);
     std::string err;
-    int rc = bfs_work_alloc(g->work, g->csr.n, err);
+    int rc = bfs_work_alloc(g->work, g->csr.n, err, g->csr.wide);
     if (rc) return fail(rc, err);
     BfsWork &w = g->work;
     const size_t n = (size_t)g->csr.n;
@@ -412,7 +445,7 @@ extern "C" int gbfs_bfs_many(gbfs_graph *g, const int32_t *sources, int32_t k, i
         if (hsrc[i] < 0 || hsrc[i] >= g->csr.n) return fail(GBFS_ERR_INVALID_ARG, "source outside [0, n)");
     std::lock_guard<std::mutex> lk(g->mu);
     std::string err;
-    int rc = bfs_work_alloc(g->work, g->csr.n, err);
+    int rc = bfs_work_alloc(g->work, g->csr.n, err, g->csr.wide);
     if (!rc) rc = bfs_work_reserve_many(g->work, k, err);
     if (rc) return fail(rc, err);
     BfsWork &w = g->work;
@@ -560,7 +593,7 @@ extern "C" int gbfs_bfs_multiroot(gbfs_graph *g, const int32_t *sources, int32_t
             if (sources[i] < 0 || sources[i] >= g->csr.n) return fail(GBFS_ERR_INVALID_ARG, "root outside [0, n)");
     std::lock_guard<std::mutex> lk(g->mu);
     std::string err;
-    int rc = bfs_work_alloc(g->work, g->csr.n, err);
+    int rc = bfs_work_alloc(g->work, g->csr.n, err, g->csr.wide);
     if (rc) return fail(rc, err);
     cudaError_t e = cudaMemcpyAsync(g->work.roots, sources, sizeof(int) * (size_t)k,
                                     dev_src ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, g->stream);
@@ -587,6 +620,7 @@ extern "C" int gbfs_bfs_multi(gbfs_graph *g, const int32_t *sources, int32_t k, 
     }
     for (int32_t i = 0; i < k; i++)
         if (hsrc[i] < 0 || hsrc[i] >= g->csr.n) return fail(GBFS_ERR_INVALID_ARG, "source outside [0, n)");
+    if (g->csr.wide) return fail(GBFS_ERR_TOO_LARGE, "multi-source search needs 32-bit row offsets");
     std::lock_guard<std::mutex> lk(g->mu);
     std::string err;
     int rc = ms_work_alloc(g->ms, g->csr.n, err);
@@ -740,18 +774,24 @@ extern "C" int gbfs_read_edge_list(const char *path, int32_t one_based, int32_t 
     return GBFS_OK;
 }
 
+// File layout: int32 n, int64 m, row offsets (n + 1), int32 col (m).  The
+// offsets are int32; a wide graph stores -n and int64 offsets (a reader
+// that only knows the int32 layout rejects the negative count).
 extern "C" int gbfs_graph_save(const gbfs_graph *g, const char *path)
 {
     if (!g || !path) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
-    std::vector<int32_t> row((size_t)g->csr.n + 1), col((size_t)std::max<int64_t>(g->csr.m, 1));
-    int rc = gbfs_graph_get_csr(g, row.data(), col.data());
+    const bool wide = g->csr.wide;
+    std::vector<int32_t> row32(wide ? 0 : (size_t)g->csr.n + 1), col((size_t)std::max<int64_t>(g->csr.m, 1));
+    std::vector<int64_t> row64(wide ? (size_t)g->csr.n + 1 : 0);
+    int rc = wide ? gbfs_graph_get_csr64(g, row64.data(), col.data()) : gbfs_graph_get_csr(g, row32.data(), col.data());
     if (rc) return rc;
     FILE *f = fopen(path, "wb");
     if (!f) return fail(GBFS_ERR_IO, std::string("cannot write ") + path);
-    int32_t n = g->csr.n;
+    int32_t n = wide ? -g->csr.n : g->csr.n;
     int64_t m = g->csr.m;
     bool ok = fwrite(&n, 4, 1, f) == 1 && fwrite(&m, 8, 1, f) == 1 &&
-              fwrite(row.data(), 4, row.size(), f) == row.size() &&
+              (wide ? fwrite(row64.data(), 8, row64.size(), f) == row64.size()
+                    : fwrite(row32.data(), 4, row32.size(), f) == row32.size()) &&
               (m == 0 || fwrite(col.data(), 4, (size_t)m, f) == (size_t)m);
     ok = (fclose(f) == 0) && ok;
     return ok ? GBFS_OK : fail(GBFS_ERR_IO, "short write");
@@ -765,14 +805,50 @@ extern "C" int gbfs_graph_load(const char *path, gbfs_graph **out)
     if (!f) return fail(GBFS_ERR_IO, std::string("cannot open ") + path);
     int32_t n = 0;
     int64_t m = 0;
-    if (fread(&n, 4, 1, f) != 1 || fread(&m, 8, 1, f) != 1 || n < 1 || m < 0 || m > INT32_MAX) {
+    if (fread(&n, 4, 1, f) != 1 || fread(&m, 8, 1, f) != 1) {
         fclose(f);
         return fail(GBFS_ERR_IO, "bad CSR header");
     }
-    std::vector<int32_t> row((size_t)n + 1), col((size_t)std::max<int64_t>(m, 1));
-    bool ok = fread(row.data(), 4, row.size(), f) == row.size() &&
+    const bool wide = n < 0;
+    if (wide) n = n == INT32_MIN ? 0 : -n;
+    if (n < 1 || n > INT32_MAX - 1 || m < 0 || (!wide && m > INT32_MAX)) {
+        fclose(f);
+        return fail(GBFS_ERR_IO, "bad CSR header");
+    }
+    std::vector<int32_t> row32(wide ? 0 : (size_t)n + 1), col((size_t)std::max<int64_t>(m, 1));
+    std::vector<int64_t> row64(wide ? (size_t)n + 1 : 0);
+    bool ok = (wide ? fread(row64.data(), 8, row64.size(), f) == row64.size()
+                    : fread(row32.data(), 4, row32.size(), f) == row32.size()) &&
               (m == 0 || fread(col.data(), 4, (size_t)m, f) == (size_t)m);
     fclose(f);
     if (!ok) return fail(GBFS_ERR_IO, "truncated CSR file");
-    return gbfs_graph_from_csr(n, m, row.data(), col.data(), out);
+    if (!wide) return gbfs_graph_from_csr(n, m, row32.data(), col.data(), out);
+    // a wide CSR: upload and adopt with 64-bit offsets
+    cudaStream_t st = nullptr;
+    int rc = make_stream(&st);
+    if (rc) return rc;
+    long long *d_row = nullptr;
+    int *d_col = nullptr;
+    cudaError_t e = cudaMalloc(&d_row, sizeof(long long) * ((size_t)n + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&d_col, sizeof(int) * (size_t)std::max<int64_t>(m, 1));
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_row, row64.data(), sizeof(long long) * ((size_t)n + 1), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && m > 0)
+        e = cudaMemcpyAsync(d_col, col.data(), sizeof(int) * (size_t)m, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        if (d_row) cudaFree(d_row);
+        if (d_col) cudaFree(d_col);
+        cudaStreamDestroy(st);
+        return cuda_fail(e, "CSR upload");
+    }
+    DeviceCsr csr;
+    std::string err;
+    rc = csr_adopt64(n, m, d_row, d_col, st, csr, err);
+    if (rc) {
+        set_error(err);
+        cudaStreamDestroy(st);
+        return rc;
+    }
+    return graph_wrap(csr, false, false, st, out);
 }

@@ -94,6 +94,7 @@ extern "C" int gbfs_graphset_from_graphs(int32_t count, gbfs_graph *const *graph
     bool sym = true;
     for (int32_t i = 0; i < count; i++) {
         if (!graphs[i]) return fail(GBFS_ERR_INVALID_ARG, "NULL member graph");
+        if (graphs[i]->csr.wide) return fail(GBFS_ERR_TOO_LARGE, "member graph with 64-bit row offsets");
         voff[i + 1] = voff[i] + graphs[i]->csr.n;
         eoff[i + 1] = eoff[i] + graphs[i]->csr.m;
         sym = sym && graphs[i]->symmetric;
@@ -174,7 +175,7 @@ extern "C" int gbfs_bfs_batch(gbfs_graphset *s, const int32_t *sources, int32_t 
     {
         std::string err;
         std::lock_guard<std::mutex> lk(g->mu);
-        int rc = bfs_work_alloc(g->work, g->csr.n, err);
+        int rc = bfs_work_alloc(g->work, g->csr.n, err, g->csr.wide);
         if (rc) return fail(rc, err);
     }
     int rc = gbfs_bfs_multiroot(g, roots.data(), count, g->work.level, &st);

@@ -73,15 +73,17 @@ constexpr int RELAX_ENTER_F = 4500;
 // row[v + 1]), so the next level reads a frontier vertex's edge range with
 // the vertex instead of a dependent load of its row offsets.  The frontier
 // queues have a bounds array beside them (qb[0] beside q0, qb[1] beside q1).
+template <typename RT>
 struct WarpQB {
     int *buf;
-    int2 *bb;
+    BndT<RT> *bb;
     int n;
 };
 
 // Append the warp's staged entries to out / outb with one global atomic on
 // the packed counter (its low 32 bits give the position).
-__device__ __forceinline__ void wqb_flush(WarpQB &q, unsigned long long *cnt, int *out, int2 *outb)
+template <typename RT>
+__device__ __forceinline__ void wqb_flush(WarpQB<RT> &q, unsigned long long *cnt, int *out, BndT<RT> *outb)
 {
     __syncwarp();
     if (q.n == 0) return;
@@ -97,8 +99,9 @@ __device__ __forceinline__ void wqb_flush(WarpQB &q, unsigned long long *cnt, in
 }
 
 // All 32 lanes call; lanes with `has` stage v and its row bounds.
-__device__ __forceinline__ void wqb_push(WarpQB &q, bool has, int v, int2 be, unsigned long long *cnt, int *out,
-                                         int2 *outb)
+template <typename RT>
+__device__ __forceinline__ void wqb_push(WarpQB<RT> &q, bool has, int v, BndT<RT> be, unsigned long long *cnt, int *out,
+                                         BndT<RT> *outb)
 {
     const unsigned m = __ballot_sync(FULL, has);
     if (!m) return;
@@ -115,7 +118,8 @@ __device__ __forceinline__ void wqb_push(WarpQB &q, bool has, int v, int2 be, un
 // Flush every warp queue of the block with one global atomic on the packed
 // count | degree counter, adding the block's `hi` values (its vertices'
 // out-degrees) to the high half in the same atomic (all threads call).
-__device__ __forceinline__ void block_flush_bounds(WarpQB &q, unsigned long long *cnt, int *out, int2 *outb,
+template <typename RT>
+__device__ __forceinline__ void block_flush_bounds(WarpQB<RT> &q, unsigned long long *cnt, int *out, BndT<RT> *outb,
                                                    unsigned long long hi, int *s_wq, unsigned long long *s_hi,
                                                    unsigned long long *s_base)
 {
@@ -156,23 +160,26 @@ __device__ __forceinline__ void block_flush_bounds(WarpQB &q, unsigned long long
 // visited bit; the winner writes its level, adds its out-degree to my_deg,
 // appends itself and its bounds to the warp queue and, with fnw given,
 // marks itself in the next frontier's bitmap too.
-__device__ __forceinline__ void claim_batch(const int (&w)[ILP], const BfsArgs &a, int nl, WarpQB &q,
-                                            unsigned long long *cnt, int *qn, int2 *qbn,
+template <typename RT>
+__device__ __forceinline__ void claim_batch(const int (&w)[ILP], const BfsArgs &a, int nl, WarpQB<RT> &q,
+                                            unsigned long long *cnt, int *qn, BndT<RT> *qbn,
                                             unsigned long long &my_deg, unsigned *fnw)
 {
+    using Sel = RowSel<RT>;
+    const RT *row = Sel::row(a);
     unsigned word[ILP];
 #pragma unroll
     for (int j = 0; j < ILP; j++) word[j] = w[j] >= 0 ? a.visited[w[j] >> 5] : FULL;
     unsigned old[ILP];
-    int2 be[ILP];
+    BndT<RT> be[ILP];
 #pragma unroll
     for (int j = 0; j < ILP; j++) {
         const unsigned bit = 1u << (w[j] & 31);
         old[j] = FULL;
-        be[j] = make_int2(0, 0);
+        be[j] = Sel::mk(0, 0);
         if (!(word[j] & bit)) {
             old[j] = atomicOr(&a.visited[w[j] >> 5], bit);
-            be[j] = make_int2(__ldg(a.row + w[j]), __ldg(a.row + w[j] + 1));
+            be[j] = Sel::mk(__ldg(row + w[j]), __ldg(row + w[j] + 1));
         }
     }
     bool won[ILP];
@@ -201,11 +208,14 @@ __device__ __forceinline__ void claim_batch(const int (&w)[ILP], const BfsArgs &
 // the CTA's own warps on its own segments otherwise.  lb: the rows' bounds
 // beside the list (a frontier queue), or null (then the row offsets are
 // loaded).
-template <int BLOCK>
-__device__ void grid_expand_list(const int *list, const int2 *lb, int cnt, const BfsArgs &a, int nl, WarpQB &q,
-                                 unsigned long long *cnt_next, int *qn, int2 *qbn, unsigned long long &my_deg,
-                                 int *s_pre, int *s_beg, int *s_warp, unsigned *fnw, bool heavy = false)
+template <int BLOCK, typename RT>
+__device__ void grid_expand_list(const int *list, const BndT<RT> *lb, int cnt, const BfsArgs &a, int nl,
+                                 WarpQB<RT> &q, unsigned long long *cnt_next, int *qn, BndT<RT> *qbn,
+                                 unsigned long long &my_deg, int *s_pre, RT *s_beg, int *s_warp, unsigned *fnw,
+                                 bool heavy = false)
 {
+    using Sel = RowSel<RT>;
+    const RT *row = Sel::row(a);
     constexpr int PER = SEG / BLOCK;
     const int lane = (int)lane_id();
     // One segment (or long rows): the grid's warps split each segment's
@@ -225,15 +235,15 @@ __device__ void grid_expand_list(const int *list, const int2 *lb, int cnt, const
             const int j = threadIdx.x * PER + t;
             d[t] = 0;
             if (j < segn) {
-                int2 be;
+                BndT<RT> be;
                 if (lb) {
                     be = __ldcg(lb + seg + j);
                 } else {
                     const int v = __ldcg(list + seg + j);
-                    be = make_int2(__ldg(a.row + v), __ldg(a.row + v + 1));
+                    be = Sel::mk(__ldg(row + v), __ldg(row + v + 1));
                 }
                 s_beg[j] = be.x;
-                d[t] = be.y - be.x;
+                d[t] = (int)(be.y - be.x);
             }
             sum += d[t];
         }
@@ -272,9 +282,9 @@ __device__ void grid_expand_list(const int *list, const int2 *lb, int cnt, const
 // Bits of a bitmap word set through a tile of BLOCK words per CTA pass:
 // appends the vertices whose bit is set in (want ? bits : ~bits & valid)
 // to out, one global atomic per CTA tile.
-template <int BLOCK>
-__device__ void bitmap_to_list(const unsigned *bm, bool complement, int n, int W, int *out, int2 *outb,
-                               const int *row, unsigned long long *cnt, int *s_warp, unsigned long long *s_base)
+template <int BLOCK, typename RT>
+__device__ void bitmap_to_list(const unsigned *bm, bool complement, int n, int W, int *out, BndT<RT> *outb,
+                               const RT *row, unsigned long long *cnt, int *s_warp, unsigned long long *s_base)
 {
     for (long long t0 = (long long)blockIdx.x * BLOCK; t0 < W; t0 += (long long)gridDim.x * BLOCK) {
         const long long w = t0 + threadIdx.x;
@@ -295,7 +305,7 @@ __device__ void bitmap_to_list(const unsigned *bm, bool complement, int n, int W
             const int b = __ffs(bits) - 1;
             const int v = (int)(w * 32 + b);
             out[pos] = v;
-            outb[pos] = make_int2(__ldg(row + v), __ldg(row + v + 1));
+            outb[pos] = RowSel<RT>::mk(__ldg(row + v), __ldg(row + v + 1));
             ++pos;
             bits &= bits - 1u;
         }
@@ -306,8 +316,9 @@ __device__ void bitmap_to_list(const unsigned *bm, bool complement, int n, int W
 // Top-down expansion of one row per lane (d = 0: none) as one concatenated
 // edge range over the warp, ILP edges per lane in flight; rows of
 // big_degree or more go to bigl (counted in *bigcnt) for a grid-wide pass.
-__device__ __forceinline__ void expand_lane_rows(int v, int b, int d, const BfsArgs &a, int nl, WarpQB &q,
-                                                 unsigned long long *cnt, int *qn, int2 *qbn,
+template <typename RT>
+__device__ __forceinline__ void expand_lane_rows(int v, RT b, int d, const BfsArgs &a, int nl, WarpQB<RT> &q,
+                                                 unsigned long long *cnt, int *qn, BndT<RT> *qbn,
                                                  unsigned long long &my_deg, unsigned *bigcnt, unsigned lane,
                                                  unsigned *fnw)
 {
@@ -336,7 +347,7 @@ __device__ __forceinline__ void expand_lane_rows(int v, int b, int d, const BfsA
                 const int c = lo + s;
                 if (__shfl_sync(FULL, excl, c) <= kk) lo = c;
             }
-            const int ob = __shfl_sync(FULL, b, lo);
+            const RT ob = __shfl_sync(FULL, b, lo);
             const int oe = __shfl_sync(FULL, excl, lo);
             w[j] = k < T ? __ldg(a.col + ob + (kk - oe)) : -1;
         }
@@ -348,8 +359,9 @@ __device__ __forceinline__ void expand_lane_rows(int v, int b, int d, const BfsA
 // bottom-up steps), with no bitmap -> queue pass: a warp takes cw words at a
 // time, deals their frontier vertices one per lane, and expands those rows
 // with expand_lane_rows.  cw aims a chunk at about 32 frontier vertices.
+template <typename RT>
 __device__ __forceinline__ void bitmap_expand(const unsigned *fb, int W, long long nf, const BfsArgs &a, int nl,
-                                              WarpQB &q, unsigned long long *cnt, int *qn, int2 *qbn,
+                                              WarpQB<RT> &q, unsigned long long *cnt, int *qn, BndT<RT> *qbn,
                                               unsigned long long &my_deg, unsigned *bigcnt, long long gwarp,
                                               long long nwarps, unsigned lane, unsigned *fnw)
 {
@@ -382,11 +394,13 @@ __device__ __forceinline__ void bitmap_expand(const unsigned *fb, int W, long lo
                     pos += s;
                 }
             }
-            int v = 0, b = 0, d = 0;
+            int v = 0, d = 0;
+            RT b = 0;
             if (slot < U) {
+                const RT *row = RowSel<RT>::row(a);
                 v = (int)((w0 + owner) * 32 + pos);
-                b = __ldg(a.row + v);
-                d = __ldg(a.row + v + 1) - b;
+                b = __ldg(row + v);
+                d = (int)(__ldg(row + v + 1) - b);
             }
             expand_lane_rows(v, b, d, a, nl, q, cnt, qn, qbn, my_deg, bigcnt, lane, fnw);
         }
@@ -399,7 +413,8 @@ __device__ __forceinline__ void bitmap_expand(const unsigned *fb, int W, long lo
 // with more than 2 * PROBE entries left remain in the warp, the warp walks
 // those together, 32 entries a step, instead of leaving most lanes idle.
 // All 32 lanes call it.
-__device__ __forceinline__ void probe_rows(int &ia, int ea, bool &fa, int &ib, int eb, bool &fb, const int *bcol,
+template <typename RT>
+__device__ __forceinline__ void probe_rows(RT &ia, RT ea, bool &fa, RT &ib, RT eb, bool &fb, const int *bcol,
                                            const unsigned *fc, unsigned lane)
 {
     for (;;) {
@@ -407,7 +422,7 @@ __device__ __forceinline__ void probe_rows(int &ia, int ea, bool &fa, int &ib, i
         const unsigned ma = __ballot_sync(FULL, aa), mb = __ballot_sync(FULL, ab);
         if (!(ma | mb)) return;
         if (__popc(ma) + __popc(mb) <= COOP_ROWS) {
-            int rem = max(aa ? ea - ia : 0, ab ? eb - ib : 0);
+            int rem = (int)max(aa ? ea - ia : (RT)0, ab ? eb - ib : (RT)0);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) rem = max(rem, __shfl_xor_sync(FULL, rem, o));
             if (rem > 2 * PROBE) {
@@ -416,11 +431,11 @@ __device__ __forceinline__ void probe_rows(int &ia, int ea, bool &fa, int &ib, i
                     const bool isb = ta == 0;
                     const int sl = __ffs(isb ? tb : ta) - 1;
                     if (isb) tb &= tb - 1; else ta &= ta - 1;
-                    const int ri = __shfl_sync(FULL, isb ? ib : ia, sl);
-                    const int re = __shfl_sync(FULL, isb ? eb : ea, sl);
+                    const RT ri = __shfl_sync(FULL, isb ? ib : ia, sl);
+                    const RT re = __shfl_sync(FULL, isb ? eb : ea, sl);
                     bool found = false;
-                    for (int i0 = ri; i0 < re && !found; i0 += 32) {
-                        const int i = i0 + (int)lane;
+                    for (RT i0 = ri; i0 < re && !found; i0 += 32) {
+                        const RT i = i0 + (RT)lane;
                         unsigned hit = 0;
                         if (i < re) {
                             const int u = __ldg(bcol + i);
@@ -455,10 +470,14 @@ __device__ __forceinline__ void probe_rows(int &ia, int ea, bool &fa, int &ib, i
 
 // MINB (CTAs per SM the register budget is sized for) only shapes register
 // allocation; the launch decides the actual grid.
-template <int BLOCK, int MINB>
+template <int BLOCK, int MINB, typename RT>
 __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
 {
-    extern __shared__ int smem[];
+    using Sel = RowSel<RT>;
+    using B = BndT<RT>;
+    const RT *const row = Sel::row(a);
+    const RT *const brow = Sel::brow(a);
+    extern __shared__ __align__(16) int smem[];
     __shared__ unsigned long long s_red[32];
     __shared__ unsigned long long s_base;
     __shared__ unsigned long long s_cd;
@@ -468,8 +487,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
     constexpr int NW = BLOCK / 32;
     int *s_q = smem;                           // NW * QCAP warp queues
     int *s_pre = s_q + NW * QCAP;              // SEG degree prefix
-    int *s_beg = s_pre + SEG;                  // SEG row begins
-    int2 *s_def = (int2 *)(s_beg + SEG);       // NW * BU_DEF: queue row bounds (top-down), deferred rows (bottom-up)
+    RT *s_beg = (RT *)(s_pre + SEG);           // SEG row begins
+    B *s_def = (B *)(s_beg + SEG);             // NW * BU_DEF: queue row bounds (top-down), deferred rows (bottom-up)
 
     const int n = a.n;
     const int W = (n + 31) >> 5;
@@ -479,7 +498,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
     const long long gwarp = gtid >> 5;
     const long long nwarps = gthreads >> 5;
     BfsCtrl *ctrl = a.ctrl;
-    WarpQB q{s_q + (threadIdx.x >> 5) * QCAP, s_def + (threadIdx.x >> 5) * BU_DEF, 0};
+    WarpQB<RT> q{s_q + (threadIdx.x >> 5) * QCAP, s_def + (threadIdx.x >> 5) * BU_DEF, 0};
     unsigned epoch = 0;
     if (a.resume) {
         // a continuation: nothing to do when the search has ended or failed,
@@ -511,8 +530,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
         }
         if (root >= 0 && gtid == 0) {
             a.q0[0] = root;
-            a.qb[0][0] = make_int2(__ldg(a.row + root), __ldg(a.row + root + 1));
-            ctrl->cd[0] = cd_pack(1, (unsigned long long)(__ldg(a.row + root + 1) - __ldg(a.row + root)));
+            Sel::qb(a, 0)[0] = Sel::mk(__ldg(row + root), __ldg(row + root + 1));
+            ctrl->cd[0] = cd_pack(1, (unsigned long long)(__ldg(row + root + 1) - __ldg(row + root)));
         }
         if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
         if (root >= 0) {
@@ -523,11 +542,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                     const int r = a.roots[i];
                     if (atomicCAS(&a.level[r], -1, 0) == -1) {
                         atomicOr(&a.visited[r >> 5], 1u << (r & 31));
-                        const int2 be = make_int2(__ldg(a.row + r), __ldg(a.row + r + 1));
+                        const B be = Sel::mk(__ldg(row + r), __ldg(row + r + 1));
                         const unsigned long long pos =
                             cd_count(atomicAdd(&ctrl->cd[0], cd_pack(1, (unsigned long long)(be.y - be.x))));
                         a.q0[pos] = r;
-                        a.qb[0][pos] = be;
+                        Sel::qb(a, 0)[pos] = be;
                     }
                 }
             }
@@ -605,7 +624,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
         edges_c += mf;
         m_u -= (long long)mf;
         bool bu;
-        if (a.direction == GBFS_DIR_TOPDOWN || a.brow == nullptr) bu = false;
+        if (a.direction == GBFS_DIR_TOPDOWN || brow == nullptr) bu = false;
         else if (a.direction == GBFS_DIR_BOTTOMUP) bu = true;
         else if (td) bu = (long long)mf * a.alpha > m_u;
         else bu = !((long long)nf * a.beta < a.n_active && nf < prev_nf);
@@ -623,8 +642,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
 
         int *qc = (L & 1) ? a.q1 : a.q0;
         int *qn = (L & 1) ? a.q0 : a.q1;
-        const int2 *qbc = a.qb[L & 1];      // row bounds beside qc
-        int2 *qbn = a.qb[(L + 1) & 1];      // and beside qn
+        const B *qbc = Sel::qb(a, L & 1);   // row bounds beside qc
+        B *qbn = Sel::qb(a, (L + 1) & 1);   // and beside qn
         unsigned *fc = a.fb[L % 3];
         unsigned *fn = a.fb[(L + 1) % 3];
         unsigned *fz = a.fb[(L + 2) % 3];   // zeroed now: the next level's fn
@@ -653,7 +672,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
         const bool from_bitmap = !bu && !td && mf <= BMTD_EDGES;
         if (!bu && !td && !from_bitmap) {
             // bitmap -> queue
-            bitmap_to_list<BLOCK>(fc, false, n, W, qc, a.qb[L & 1], a.row, &ctrl->fill, s_warp, &s_base);
+            bitmap_to_list<BLOCK, RT>(fc, false, n, W, qc, Sel::qb(a, L & 1), row, &ctrl->fill, s_warp, &s_base);
             if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
         }
         td = !bu;
@@ -672,25 +691,26 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
             // bitmap, so the switch needs no queue -> bitmap pass
             const float growth = fmaxf(1.f, (float)mf / (float)(prev_mf ? prev_mf : 1ull));
             const bool likely_bu = (float)mf * growth * (float)a.alpha > (float)m_u;
-            unsigned *fnw = a.direction == GBFS_DIR_OPTIMIZING && a.brow && likely_bu ? fn : nullptr;
+            unsigned *fnw = a.direction == GBFS_DIR_OPTIMIZING && brow && likely_bu ? fn : nullptr;
             if (from_bitmap) {
                 bitmap_expand(fc, W, (long long)nf, a, nl, q, cnt_next, qn, qbn, my_deg, &ctrl->big[L % 3], gwarp, nwarps,
                               lane, fnw);
             } else if (nf <= (unsigned long long)SEG) {
                 // small frontier: every edge of it balanced over the whole grid
-                grid_expand_list<BLOCK>(qc, qbc, (int)nf, a, nl, q, cnt_next, qn, qbn, my_deg, s_pre, s_beg, s_warp,
-                                        fnw);
+                grid_expand_list<BLOCK, RT>(qc, qbc, (int)nf, a, nl, q, cnt_next, qn, qbn, my_deg, s_pre, s_beg,
+                                            s_warp, fnw);
             } else {
                 // large frontier: 32 rows per warp as one concatenated edge
                 // range, rows of degree >= big_degree deferred to a grid pass
                 for (long long base = gwarp * 32; base < (long long)nf; base += nwarps * 32) {
                     const long long i = base + lane;
-                    int v = 0, b = 0, d = 0;
+                    int v = 0, d = 0;
+                    RT b = 0;
                     if (i < (long long)nf) {
                         v = __ldcg(qc + i);
-                        const int2 be = __ldcg(qbc + i);
+                        const B be = __ldcg(qbc + i);
                         b = be.x;
-                        d = be.y - be.x;
+                        d = (int)(be.y - be.x);
                     }
                     expand_lane_rows(v, b, d, a, nl, q, cnt_next, qn, qbn, my_deg, &ctrl->big[L % 3], lane, fnw);
                 }
@@ -709,8 +729,8 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
             traced_big = nb > 0;
             if (nb > 0) {
                 my_deg = 0;
-                grid_expand_list<BLOCK>(a.bigl, nullptr, nb, a, nl, q, cnt_next, qn, qbn, my_deg, s_pre, s_beg, s_warp,
-                                        fnw, true);
+                grid_expand_list<BLOCK, RT>(a.bigl, (const B *)nullptr, nb, a, nl, q, cnt_next, qn, qbn, my_deg, s_pre,
+                                            s_beg, s_warp, fnw, true);
                 block_flush_bounds(q, cnt_next, qn, qbn, my_deg, s_wq, s_red, &s_base);
                 if (!grid_sync(&ctrl->bar, &ctrl->status, a.timeout_ns, epoch)) return;
             }
@@ -733,7 +753,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
             const int cw = (int)min(32LL, max(1LL, cwl));
             unsigned *my_found = (unsigned *)(s_beg) + (threadIdx.x >> 5) * 32;  // s_beg is free here
             int *def_v = q.buf;  // the warp's queue is idle in bottom-up steps
-            int2 *def_b = s_def + (threadIdx.x >> 5) * BU_DEF;
+            B *def_b = s_def + (threadIdx.x >> 5) * BU_DEF;
             my_found[lane] = 0;
             __syncwarp();
             if (a.bsecond == nullptr) {
@@ -753,10 +773,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                 auto phase_b = [&](int cntb) {
                     const int base = dn - cntb;
                     const int ka = base + (int)lane, kb = base + 32 + (int)lane;
-                    int va = -1, vb = -1, ia = 0, ea = 0, ib = 0, eb = 0;
+                    int va = -1, vb = -1;
+                    RT ia = 0, ea = 0, ib = 0, eb = 0;
                     if (ka < dn) { va = def_v[ka]; ia = def_b[ka].x; ea = def_b[ka].y; }
                     if (kb < dn) { vb = def_v[kb]; ib = def_b[kb].x; eb = def_b[kb].y; }
-                    const int da = ea - ia + skip, db = eb - ib + skip;
+                    const int da = (int)(ea - ia) + skip, db = (int)(eb - ib) + skip;
                     bool fa = false, fb = false;
                     probe_rows(ia, ea, fa, ib, eb, fb, a.bcol, fc, lane);
                     if (fa) {
@@ -764,14 +785,14 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                         atomicOr(fn + (va >> 5), 1u << (va & 31));
                         atomicOr(a.visited + (va >> 5), 1u << (va & 31));
                         ++my_cnt;
-                        my_deg += (unsigned long long)(a.brow == a.row ? da : __ldg(a.row + va + 1) - __ldg(a.row + va));
+                        my_deg += (unsigned long long)(brow == row ? (RT)da : __ldg(row + va + 1) - __ldg(row + va));
                     }
                     if (fb) {
                         a.level[vb] = nl;
                         atomicOr(fn + (vb >> 5), 1u << (vb & 31));
                         atomicOr(a.visited + (vb >> 5), 1u << (vb & 31));
                         ++my_cnt;
-                        my_deg += (unsigned long long)(a.brow == a.row ? db : __ldg(a.row + vb + 1) - __ldg(a.row + vb));
+                        my_deg += (unsigned long long)(brow == row ? (RT)db : __ldg(row + vb + 1) - __ldg(row + vb));
                     }
                     __syncwarp();
                     dn = base;
@@ -817,15 +838,16 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                             }
                             vv[h] = slot < U ? (int)((w0 + owner) * 32 + pos) : -1;
                         }
-                        int pf[4], rb[4], re[4];
+                        int pf[4];
+                        RT rb[4], re[4];
 #pragma unroll
                         for (int h = 0; h < 4; h++) {
                             pf[h] = -1;
                             rb[h] = re[h] = 0;
                             if (vv[h] >= 0) {
                                 pf[h] = __ldg(a.bfirst + vv[h]);
-                                rb[h] = __ldg(a.brow + vv[h]);
-                                re[h] = __ldg(a.brow + vv[h] + 1);
+                                rb[h] = __ldg(brow + vv[h]);
+                                re[h] = __ldg(brow + vv[h] + 1);
                             }
                         }
                         unsigned hit[4];
@@ -842,15 +864,15 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                                 a.level[v] = nl;
                                 atomicOr(&my_found[(v >> 5) - w0], 1u << (v & 31));
                                 ++my_cnt;
-                                my_deg += (unsigned long long)(a.brow == a.row ? re[h] - rb[h]
-                                                                               : __ldg(a.row + v + 1) - __ldg(a.row + v));
+                                my_deg += (unsigned long long)(brow == row ? re[h] - rb[h]
+                                                                           : __ldg(row + v + 1) - __ldg(row + v));
                             }
                             const bool defer = v >= 0 && !f && rb[h] + skip < re[h];
                             const unsigned dm = __ballot_sync(FULL, defer);
                             if (defer) {
                                 const int slotd = dn + __popc(dm & lanemask_lt());
                                 def_v[slotd] = v;
-                                def_b[slotd] = make_int2(rb[h] + skip, re[h]);
+                                def_b[slotd] = Sel::mk(rb[h] + skip, re[h]);
                             }
                             dn += __popc(dm);
                         }
@@ -914,20 +936,21 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                         }
                         const int va = vv[0], vb = vv[1];
                         const bool two = a.bsecond != nullptr;
-                        int ia = 0, ea = 0, ib = 0, eb = 0, pa = -1, pb = -1, qa = -1, qb = -1;
+                        RT ia = 0, ea = 0, ib = 0, eb = 0;
+                        int pa = -1, pb = -1, qa = -1, qb = -1;
                         if (va >= 0) {
                             pa = __ldg(a.bfirst + va);
                             if (two) qa = __ldg(a.bsecond + va);
-                            ia = __ldg(a.brow + va);
-                            ea = __ldg(a.brow + va + 1);
+                            ia = __ldg(brow + va);
+                            ea = __ldg(brow + va + 1);
                         }
                         if (vb >= 0) {
                             pb = __ldg(a.bfirst + vb);
                             if (two) qb = __ldg(a.bsecond + vb);
-                            ib = __ldg(a.brow + vb);
-                            eb = __ldg(a.brow + vb + 1);
+                            ib = __ldg(brow + vb);
+                            eb = __ldg(brow + vb + 1);
                         }
-                        const int da = ea - ia, db = eb - ib;
+                        const int da = (int)(ea - ia), db = (int)(eb - ib);
                         // First step: each row's first entry (hub-first rows: the
                         // highest-degree neighbour, where most vertices find their
                         // parent), with its second on other rows, from the compact
@@ -949,13 +972,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
                             a.level[va] = nl;
                             atomicOr(&my_found[(va >> 5) - w0], 1u << (va & 31));
                             ++my_cnt;
-                            my_deg += (unsigned long long)(a.brow == a.row ? da : __ldg(a.row + va + 1) - __ldg(a.row + va));
+                            my_deg += (unsigned long long)(brow == row ? (RT)da : __ldg(row + va + 1) - __ldg(row + va));
                         }
                         if (fb) {
                             a.level[vb] = nl;
                             atomicOr(&my_found[(vb >> 5) - w0], 1u << (vb & 31));
                             ++my_cnt;
-                            my_deg += (unsigned long long)(a.brow == a.row ? db : __ldg(a.row + vb + 1) - __ldg(a.row + vb));
+                            my_deg += (unsigned long long)(brow == row ? (RT)db : __ldg(row + vb + 1) - __ldg(row + vb));
                         }
                     }
                     __syncwarp();
@@ -1008,22 +1031,25 @@ __global__ void __launch_bounds__(BLOCK, MINB) k_bfs(BfsArgs a)
     grid_exit(&ctrl->bar, &ctrl->t_exit);
 }
 
-template <int BLOCK>
+template <int BLOCK, typename RT = int>
 size_t bfs_smem_bytes()
 {
-    return sizeof(int) * ((size_t)(BLOCK / 32) * QCAP + 2 * (size_t)SEG) + sizeof(int2) * (size_t)(BLOCK / 32) * BU_DEF;
+    return sizeof(int) * ((size_t)(BLOCK / 32) * QCAP + (size_t)SEG) + sizeof(RT) * (size_t)SEG +
+           sizeof(BndT<RT>) * (size_t)(BLOCK / 32) * BU_DEF;
 }
 
-template <int BLOCK, int MINB>
+template <int BLOCK, int MINB, typename RT = int>
 cudaError_t bfs_launch(BfsArgs &args, int blocks_per_sm, cudaStream_t st, int max_ctas)
 {
     static LaunchSetup setup;  // per template instance
-    const size_t smem = bfs_smem_bytes<BLOCK>();
+    const size_t smem = bfs_smem_bytes<BLOCK, RT>();
     int sms = 0, occ = 0;
     cudaError_t e = setup.get(sms, occ, [&](int dev, int &s_out, int &o_out) {
-        cudaError_t r = cudaFuncSetAttribute(k_bfs<BLOCK, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t r =
+            cudaFuncSetAttribute(k_bfs<BLOCK, MINB, RT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (r == cudaSuccess) r = cudaDeviceGetAttribute(&s_out, cudaDevAttrMultiProcessorCount, dev);
-        if (r == cudaSuccess) r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o_out, k_bfs<BLOCK, MINB>, BLOCK, smem);
+        if (r == cudaSuccess)
+            r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o_out, k_bfs<BLOCK, MINB, RT>, BLOCK, smem);
         return r;
     });
     if (e != cudaSuccess) return e;
@@ -1032,11 +1058,14 @@ cudaError_t bfs_launch(BfsArgs &args, int blocks_per_sm, cudaStream_t st, int ma
     int grid = sms * per;
     if (max_ctas > 0) grid = std::max(1, std::min(grid, max_ctas));
     void *kargs[] = {&args};
-    return cudaLaunchCooperativeKernel((const void *)k_bfs<BLOCK, MINB>, dim3(grid), dim3(BLOCK), kargs, smem, st);
+    return cudaLaunchCooperativeKernel((const void *)k_bfs<BLOCK, MINB, RT>, dim3(grid), dim3(BLOCK), kargs, smem,
+                                       st);
 }
 
 cudaError_t bfs_launch_any(BfsArgs &a, int threads, int bps, cudaStream_t st, int max_ctas)
 {
+    // wide graphs: one launch shape (512 threads, up to 2 CTAs per SM)
+    if (a.wide) return bfs_launch<512, 2, long long>(a, std::min(bps, 2), st, max_ctas);
     switch (threads) {
     case 256: return bps <= 4 ? bfs_launch<256, 4>(a, bps, st, max_ctas) : bfs_launch<256, 8>(a, bps, st, max_ctas);
     case 1024:
@@ -1052,12 +1081,12 @@ template <int BLOCK, int MINB>
 int occupancy_ctas(int blocks_per_sm)
 {
     int dev = 0, sms = 0, occ = 0;
-    if (cudaFuncSetAttribute(k_bfs<BLOCK, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(k_bfs<BLOCK, MINB, int>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)bfs_smem_bytes<BLOCK>()) != cudaSuccess)
         return 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bfs<BLOCK, MINB>, BLOCK, bfs_smem_bytes<BLOCK>()) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_bfs<BLOCK, MINB, int>, BLOCK, bfs_smem_bytes<BLOCK>()) !=
         cudaSuccess)
         return 0;
     return sms * std::max(1, std::min(blocks_per_sm, occ));
@@ -1078,9 +1107,9 @@ int bfs_max_ctas(const gbfs_params &p)
     }
 }
 
-int bfs_work_alloc(BfsWork &w, int32_t n, std::string &err)
+int bfs_work_alloc(BfsWork &w, int32_t n, std::string &err, bool wide)
 {
-    if (w.ctrl && w.n == n) return GBFS_OK;
+    if (w.ctrl && w.n == n && w.wide == wide) return GBFS_OK;
     bfs_work_free(w);
     const size_t W = ((size_t)n + 31) / 32;
     const size_t bytes_int = sizeof(int) * (size_t)n;
@@ -1097,7 +1126,7 @@ int bfs_work_alloc(BfsWork &w, int32_t n, std::string &err)
     if (!al((void **)&w.level, bytes_int) || !al((void **)&w.visited, W * 4) ||
         !al((void **)&w.fb0, W * 4) || !al((void **)&w.fb1, W * 4) || !al((void **)&w.fb2, W * 4) ||
         !al((void **)&w.q0, bytes_int) || !al((void **)&w.q1, bytes_int) ||
-        !al((void **)&w.qb0, 2 * bytes_int) || !al((void **)&w.qb1, 2 * bytes_int) ||
+        !al((void **)&w.qb0, (wide ? 4 : 2) * bytes_int) || !al((void **)&w.qb1, (wide ? 4 : 2) * bytes_int) ||
         !al((void **)&w.big, bytes_int) || !al((void **)&w.roots, bytes_int) ||
         !al((void **)&w.ctrl, sizeof(BfsCtrl))) {
         bfs_work_free(w);
@@ -1111,6 +1140,7 @@ int bfs_work_alloc(BfsWork &w, int32_t n, std::string &err)
         return GBFS_ERR_CUDA;
     }
     w.n = n;
+    w.wide = wide;
     return GBFS_OK;
 }
 
@@ -1169,15 +1199,22 @@ BfsArgs make_args(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const in
     a.n = g.n;
     a.n_active = (int)std::max<int64_t>(1, g.nonisolated);
     a.m = g.m;
+    a.wide = g.wide ? 1 : 0;
     a.row = g.row;
+    a.row64 = g.row64;
     a.col = g.col;
     // in-edges for bottom-up steps; null when neither (then every level is
-    // top-down); the transpose is read only when bottom-up may run
+    // top-down); the transpose is read only when bottom-up may run (wide
+    // graphs have none)
     const bool bu_possible = p.direction != GBFS_DIR_TOPDOWN;
     a.brow = symmetric ? g.row : bu_possible ? g.trow : nullptr;
+    a.brow64 = symmetric ? g.row64 : nullptr;
     a.bcol = symmetric ? g.col : bu_possible ? g.tcol : nullptr;
     a.bfirst = symmetric ? g.first : bu_possible ? g.tfirst : nullptr;
-    if (!a.bfirst) a.brow = a.bcol = nullptr;
+    if (!a.bfirst) {
+        a.brow = a.bcol = nullptr;
+        a.brow64 = nullptr;
+    }
     // hub-first rows (the transpose's always are): most vertices find their
     // parent at the first entry, and a second lookup per vertex costs more
     // than it saves; other rows probe their first two entries at once
@@ -1192,6 +1229,8 @@ BfsArgs make_args(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const in
     a.q1 = w.q1;
     a.qb[0] = w.qb0;
     a.qb[1] = w.qb1;
+    a.qb64[0] = reinterpret_cast<longlong2 *>(w.qb0);  // the workspace of a wide graph has 16-byte bounds
+    a.qb64[1] = reinterpret_cast<longlong2 *>(w.qb1);
     a.bigl = w.big;
     a.ctrl = w.ctrl;
     a.out = slot;
@@ -1221,16 +1260,16 @@ cudaError_t bfs_shape(int blocks_per_sm, int max_ctas, const void **func, int *b
     const size_t sm = bfs_smem_bytes<BLOCK>();
     int sms = 0, occ = 0;
     cudaError_t e = setup.get(sms, occ, [&](int dev, int &s_out, int &o_out) {
-        cudaError_t r = cudaFuncSetAttribute(k_bfs<BLOCK, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaError_t r = cudaFuncSetAttribute(k_bfs<BLOCK, MINB, int>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
         if (r == cudaSuccess) r = cudaDeviceGetAttribute(&s_out, cudaDevAttrMultiProcessorCount, dev);
-        if (r == cudaSuccess) r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o_out, k_bfs<BLOCK, MINB>, BLOCK, sm);
+        if (r == cudaSuccess) r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o_out, k_bfs<BLOCK, MINB, int>, BLOCK, sm);
         return r;
     });
     if (e != cudaSuccess) return e;
     if (occ < 1) return cudaErrorInvalidConfiguration;
     int gr = sms * std::max(1, std::min(blocks_per_sm, occ));
     if (max_ctas > 0) gr = std::max(1, std::min(gr, max_ctas));
-    *func = (const void *)k_bfs<BLOCK, MINB>;
+    *func = (const void *)k_bfs<BLOCK, MINB, int>;
     *block = BLOCK;
     *grid = gr;
     *smem = sm;
@@ -1414,6 +1453,10 @@ int bfs_work_reserve_many(BfsWork &w, int k, std::string &err)
 int bfs_run(const DeviceCsr &g, const gbfs_params &p, BfsWork &w, const int *d_roots, int k,
             int single_root, int *d_level, cudaStream_t st, BfsResult &res, std::string &err, bool symmetric)
 {
+    if (g.wide && p.per_level_launch) {
+        err = "per-level launch modes need 32-bit row offsets";
+        return GBFS_ERR_TOO_LARGE;
+    }
     cudaError_t e = cudaSuccess;
     if (p.per_level_launch == 2) {
         // the graph reads its roots from w.roots

@@ -91,7 +91,8 @@ struct BfsWork {
     int *q0 = nullptr;           // n frontier queues
     int *q1 = nullptr;
     int2 *qb0 = nullptr;         // n row bounds (row[v], row[v + 1]) beside q0 / q1
-    int2 *qb1 = nullptr;
+    int2 *qb1 = nullptr;         // (16-byte longlong2 entries when `wide`)
+    bool wide = false;           // sized for a graph with 64-bit row offsets
     int *big = nullptr;          // n deferred rows
     int *roots = nullptr;        // root staging (n)
     BfsCtrl *ctrl = nullptr;
@@ -112,7 +113,7 @@ struct BfsWork {
     // instantiated graph and the launch arguments / shape it was built for
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
-    unsigned char graph_key[256] = {};
+    unsigned char graph_key[320] = {};
     int graph_shape[3] = {0, 0, 0};
     int64_t bytes = 0;
 };
@@ -122,7 +123,7 @@ void bfs_graph_free(BfsWork &w);
 // Allocate the second level buffer, the copy stream and its events.
 int bfs_work_reserve_overlap(BfsWork &w, std::string &err);
 
-int bfs_work_alloc(BfsWork &w, int32_t n, std::string &err);
+int bfs_work_alloc(BfsWork &w, int32_t n, std::string &err, bool wide = false);
 void bfs_work_free(BfsWork &w);
 
 struct BfsResult {

@@ -11,9 +11,12 @@ struct BfsArgs {
     int n;
     int n_active;            // non-isolated vertices (for beta)
     long long m;
+    int wide;                // 64-bit row offsets: row64 / brow64 / qb64 instead of row / brow / qb
     const int *row;
+    const long long *row64;
     const int *col;
     const int *brow, *bcol;  // bottom-up adjacency: in-edges (row/col when symmetric)
+    const long long *brow64;
     const int *bfirst;       // first entry of each brow row (-1: empty row)
     const int *bsecond;      // second entries (-1 past the end); null: probe the first alone
     const unsigned *zmask;   // out-degree-0 bitmap, or NULL (directed graphs:
@@ -23,6 +26,7 @@ struct BfsArgs {
     unsigned *fb[3];         // frontier bitmaps, rotating by level
     int *q0, *q1;            // frontier queues
     int2 *qb[2];             // row bounds beside q0 and q1
+    longlong2 *qb64[2];      // the same for wide graphs
     int *bigl;
     BfsCtrl *ctrl;
     BfsOut *out;
@@ -42,6 +46,29 @@ struct BfsArgs {
     int yield_max_f;
     unsigned long long timeout_ns;
 };
+
+// Row-offset type RT of the kernels (int, or long long on wide graphs): the
+// matching row pointers, row-bound pairs and queue bound arrays.
+template <typename RT>
+struct RowSel;
+template <>
+struct RowSel<int> {
+    using B = int2;
+    __device__ static const int *row(const BfsArgs &a) { return a.row; }
+    __device__ static const int *brow(const BfsArgs &a) { return a.brow; }
+    __device__ static int2 *qb(const BfsArgs &a, int i) { return a.qb[i]; }
+    __host__ __device__ static int2 mk(int x, int y) { return make_int2(x, y); }
+};
+template <>
+struct RowSel<long long> {
+    using B = longlong2;
+    __device__ static const long long *row(const BfsArgs &a) { return a.row64; }
+    __device__ static const long long *brow(const BfsArgs &a) { return a.brow64; }
+    __device__ static longlong2 *qb(const BfsArgs &a, int i) { return a.qb64[i]; }
+    __host__ __device__ static longlong2 mk(long long x, long long y) { return make_longlong2(x, y); }
+};
+template <typename RT>
+using BndT = typename RowSel<RT>::B;
 
 // The label-correcting kernel (bfs_relax.cu), queued after a grid launch
 // with may_yield set: it finishes a search the grid launch parked.

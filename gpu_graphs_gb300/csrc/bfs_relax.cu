@@ -65,10 +65,14 @@ constexpr int RX_ILP_BIG = 4;
 constexpr int RX_HOPS = 64;
 constexpr int RX_BPS = 2;  // CTAs per SM (one: 7000^2 grid 19.6 ms, thin-start expander +30 %)
 
+template <typename RT>
 __global__ void __launch_bounds__(RX_BLOCK, 2) k_bfs_relax(BfsArgs a)
 {
+    using Sel = RowSel<RT>;
+    using B = BndT<RT>;
+    const RT *const row = Sel::row(a);
     __shared__ int s_v[2][RX_CAP];
-    __shared__ int2 s_b[2][RX_CAP];           // row bounds beside s_v
+    __shared__ B s_b[2][RX_CAP];              // row bounds beside s_v
     __shared__ int s_pre[RX_CAP];             // exclusive prefix of the entries' out-degrees
     __shared__ int s_wsum[RX_NW];
     __shared__ int s_tot;
@@ -120,15 +124,15 @@ __global__ void __launch_bounds__(RX_BLOCK, 2) k_bfs_relax(BfsArgs a)
         // the count two rounds back (read by every CTA before the last barrier)
         if (gtid == 0) ctrl->cd[(Lj + 2) % 3] = 0;
         const int *qin = (Lj & 1) ? a.q1 : a.q0;
-        const int2 *qbin = a.qb[Lj & 1];
+        const B *qbin = Sel::qb(a, Lj & 1);
         int *qout = (Lj & 1) ? a.q0 : a.q1;
-        int2 *qbout = a.qb[(Lj + 1) & 1];
+        B *qbout = Sel::qb(a, (Lj + 1) & 1);
         unsigned long long *cnt_out = &ctrl->cd[(Lj + 1) % 3];
         const int mark = j + 1;
 
         // global push of v (with its row bounds) by the lanes with `go`,
         // at most once per vertex and round
-        auto push_global = [&](bool go, int v, int2 vb) {
+        auto push_global = [&](bool go, int v, B vb) {
             if (go) go = atomicMax(stamp + v, mark) < mark;
             const unsigned m = __ballot_sync(FULL, go);
             if (!m) return;
@@ -151,14 +155,14 @@ __global__ void __launch_bounds__(RX_BLOCK, 2) k_bfs_relax(BfsArgs a)
 #pragma unroll
             for (int q = 0; q < Q; q++) nd[q] = w[q] >= 0 ? __ldcg(lvl + u[q]) + 1u : 0u;  // 0: skip
             unsigned old[Q];
-            int2 wb[Q];
+            B wb[Q];
 #pragma unroll
             for (int q = 0; q < Q; q++) {
                 old[q] = 0;
-                wb[q] = make_int2(0, 0);
+                wb[q] = Sel::mk(0, 0);
                 if (nd[q] != 0) {
                     old[q] = atomicMin(lvl + w[q], nd[q]);
-                    wb[q] = make_int2(__ldg(a.row + w[q]), __ldg(a.row + w[q] + 1));
+                    wb[q] = Sel::mk(__ldg(row + w[q]), __ldg(row + w[q] + 1));
                 }
             }
 #pragma unroll
@@ -202,9 +206,9 @@ __global__ void __launch_bounds__(RX_BLOCK, 2) k_bfs_relax(BfsArgs a)
                 // itself, two entries per lane, and finds an edge's entry with
                 // shuffles (no CTA barrier)
                 const int i0 = 2 * (int)lane, i1 = i0 + 1;
-                const int2 b0 = i0 < nc ? s_b[cur][i0] : make_int2(0, 0);
-                const int2 b1 = i1 < nc ? s_b[cur][i1] : make_int2(0, 0);
-                const int d0 = b0.y - b0.x, d1 = b1.y - b1.x;
+                const B b0 = i0 < nc ? s_b[cur][i0] : Sel::mk(0, 0);
+                const B b1 = i1 < nc ? s_b[cur][i1] : Sel::mk(0, 0);
+                const int d0 = (int)(b0.y - b0.x), d1 = (int)(b1.y - b1.x);
                 const int incl = warp_incl_scan(d0 + d1);
                 const int ex0 = incl - d0 - d1, ex1 = ex0 + d0;
                 const int E = __shfl_sync(FULL, incl, 31);
@@ -221,7 +225,7 @@ __global__ void __launch_bounds__(RX_BLOCK, 2) k_bfs_relax(BfsArgs a)
                         for (int st = 16; st > 0; st >>= 1)
                             if (__shfl_sync(FULL, ex0, l + st) <= e) l += st;
                         const int x0 = __shfl_sync(FULL, ex0, l), x1 = __shfl_sync(FULL, ex1, l);
-                        const int bx0 = __shfl_sync(FULL, b0.x, l), bx1 = __shfl_sync(FULL, b1.x, l);
+                        const RT bx0 = __shfl_sync(FULL, b0.x, l), bx1 = __shfl_sync(FULL, b1.x, l);
                         w[q] = -1;
                         u[q] = 0;
                         if (e < E) {
@@ -243,8 +247,8 @@ __global__ void __launch_bounds__(RX_BLOCK, 2) k_bfs_relax(BfsArgs a)
                 const int i = (int)t * RX_PER_T + k;
                 dl[k] = 0;
                 if (i < nc) {
-                    const int2 be = s_b[cur][i];
-                    dl[k] = be.y - be.x;
+                    const B be = s_b[cur][i];
+                    dl[k] = (int)(be.y - be.x);
                 }
                 dsum += dl[k];
             }
@@ -323,7 +327,7 @@ __global__ void __launch_bounds__(RX_BLOCK, 2) k_bfs_relax(BfsArgs a)
                     for (unsigned k0 = 0; k0 < nn; k0 += RX_BLOCK) {
                         const unsigned i = k0 + t;
                         int v = 0;
-                        int2 vb = make_int2(0, 0);
+                        B vb = Sel::mk(0, 0);
                         if (i < nn) {
                             v = s_v[(h + 1) & 1][i];
                             vb = s_b[(h + 1) & 1][i];
@@ -418,7 +422,7 @@ cudaError_t bfs_relax_launch(const BfsArgs &args, cudaStream_t st, int max_ctas)
     int sms = 0, occ = 0;
     cudaError_t e = setup.get(sms, occ, [](int dev, int &s_out, int &o_out) {
         cudaError_t r = cudaDeviceGetAttribute(&s_out, cudaDevAttrMultiProcessorCount, dev);
-        if (r == cudaSuccess) r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o_out, k_bfs_relax, RX_BLOCK, 0);
+        if (r == cudaSuccess) r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o_out, k_bfs_relax<int>, RX_BLOCK, 0);
         return r;
     });
     if (e != cudaSuccess) return e;
@@ -427,7 +431,10 @@ cudaError_t bfs_relax_launch(const BfsArgs &args, cudaStream_t st, int max_ctas)
     if (max_ctas > 0) grid = std::max(1, std::min(grid, max_ctas));
     BfsArgs a = args;
     void *kargs[] = {&a};
-    return cudaLaunchCooperativeKernel((const void *)k_bfs_relax, dim3(grid), dim3(RX_BLOCK), kargs, 0, st);
+    // the wide kernel holds twice the row-bound bytes in shared memory; its
+    // CTAs still fit two per SM
+    const void *fn = a.wide ? (const void *)k_bfs_relax<long long> : (const void *)k_bfs_relax<int>;
+    return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(RX_BLOCK), kargs, 0, st);
 }
 
 }  // namespace gbfs

@@ -45,16 +45,23 @@ constexpr int BIN_THREADS = 1024;
         }                                                                        \
     } while (0)
 
+__device__ __forceinline__ int atomic_add_t(int *p, int v) { return atomicAdd(p, v); }
+__device__ __forceinline__ long long atomic_add_t(long long *p, long long v)
+{
+    return (long long)atomicAdd(reinterpret_cast<unsigned long long *>(p), (unsigned long long)v);
+}
+
 // All 32 lanes call; key < 0 means "no increment".  Returns the old value of
 // arr[key] plus this lane's rank among lanes with the same key.
-__device__ __forceinline__ int agg_atomic_add(int *arr, int key)
+template <typename T>
+__device__ __forceinline__ T agg_atomic_add(T *arr, int key)
 {
     unsigned peers = __match_any_sync(FULL, key);
     int leader = __ffs(peers) - 1;
-    int old = 0;
-    if (key >= 0 && (int)lane_id() == leader) old = atomicAdd(&arr[key], __popc(peers));
+    T old = 0;
+    if (key >= 0 && (int)lane_id() == leader) old = atomic_add_t(&arr[key], (T)__popc(peers));
     old = __shfl_sync(FULL, old, leader);
-    return old + __popc(peers & lanemask_lt());
+    return old + (T)__popc(peers & lanemask_lt());
 }
 
 template <typename T>
@@ -113,10 +120,14 @@ __global__ void k_count(const int *__restrict__ src, const int *__restrict__ dst
                 u = v = -1;
             }
         }
-        agg_atomic_add(deg, u);
+        // (every lane calls agg_atomic_add); a row of 2^30 edges or more
+        // would overflow the int32 degrees
+        const int cu = agg_atomic_add(deg, u);
+        if (u >= 0 && cu >= (1 << 30)) atomicExch(status, DEV_OVERFLOW);
         mine += u >= 0;
         if (sym) {
-            agg_atomic_add(deg, v);
+            const int cv = agg_atomic_add(deg, v);
+            if (v >= 0 && cv >= (1 << 30)) atomicExch(status, DEV_OVERFLOW);
             mine += v >= 0;
         }
     }
@@ -124,8 +135,9 @@ __global__ void k_count(const int *__restrict__ src, const int *__restrict__ dst
     if (threadIdx.x == 0 && t) atomicAdd(total, t);
 }
 
+template <typename RT>
 __global__ void k_scatter(const int *__restrict__ src, const int *__restrict__ dst, int64_t m,
-                          int n, unsigned flags, int *cursor, int *tmp)
+                          int n, unsigned flags, RT *cursor, int *tmp)
 {
     const bool sym = flags & GBFS_SYMMETRIZE, noself = flags & GBFS_DROP_SELF_LOOPS;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -139,10 +151,10 @@ __global__ void k_scatter(const int *__restrict__ src, const int *__restrict__ d
             if ((unsigned)u >= (unsigned)n || (unsigned)v >= (unsigned)n || (noself && u == v))
                 u = v = -1;
         }
-        int p = agg_atomic_add(cursor, u);
+        const RT p = agg_atomic_add(cursor, u);
         if (u >= 0) tmp[p] = v;
         if (sym) {
-            int q = agg_atomic_add(cursor, v);
+            const RT q = agg_atomic_add(cursor, v);
             if (v >= 0) tmp[q] = u;
         }
     }
@@ -151,14 +163,15 @@ __global__ void k_scatter(const int *__restrict__ src, const int *__restrict__ d
 // Rows longer than 32 go to one of four lists by length: up to W4_MAX and
 // up to W16_MAX (warp sorts in registers), up to MED_MAX (CTA sort in shared
 // memory), longer (radix sort).  cnt[0] medium, [1] large, [2] W4, [3] W16.
-__global__ void k_bin(const int *__restrict__ row, int n, int *med, int *large, int *w4, int *w16, unsigned *cnt)
+template <typename RT>
+__global__ void k_bin(const RT *__restrict__ row, int n, int *med, int *large, int *w4, int *w16, unsigned *cnt)
 {
     __shared__ int s_warp[33];
     __shared__ int s_base[4];
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n;
          base += (int64_t)gridDim.x * blockDim.x) {
         int64_t r = base + threadIdx.x;
-        int d = r < n ? row[r + 1] - row[r] : 0;
+        int d = r < n ? (int)(row[r + 1] - row[r]) : 0;
         const int cls = d <= 32 ? -1 : d <= W4_MAX ? 2 : d <= W16_MAX ? 3 : d <= MED_MAX ? 0 : 1;
         int tot[4], off[4];
 #pragma unroll
@@ -191,12 +204,14 @@ __device__ __forceinline__ int warp_bitonic_sort(int x)
 }
 
 // One warp per row of length <= 32: sort in registers, pack distinct values.
-__global__ void k_sort_small(const int *__restrict__ row, int n, int *tmp, int dedup, int *ucnt)
+template <typename RT>
+__global__ void k_sort_small(const RT *__restrict__ row, int n, int *tmp, int dedup, int *ucnt)
 {
     const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const unsigned lane = lane_id();
     for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
-        const int b = row[r], d = row[r + 1] - b;
+        const RT b = row[r];
+        const int d = (int)(row[r + 1] - b);
         if (d > 32) continue;
         if (d <= 1) {
             if (lane == 0) ucnt[r] = d;
@@ -257,8 +272,8 @@ __device__ __forceinline__ void warp_bitonic_sort_regs(int (&v)[E])
 
 // One warp per listed row of length 33..32*E: sort in registers, pack the
 // distinct values (dedup) or all of them back in place, record the count.
-template <int E>
-__global__ void k_sort_warp(const int *__restrict__ row, const int *__restrict__ list, const unsigned *cnt,
+template <int E, typename RT>
+__global__ void k_sort_warp(const RT *__restrict__ row, const int *__restrict__ list, const unsigned *cnt,
                             int *tmp, int dedup, int *ucnt)
 {
     const int count = (int)*cnt;
@@ -266,7 +281,8 @@ __global__ void k_sort_warp(const int *__restrict__ row, const int *__restrict__
     const int lane = (int)lane_id();
     for (int64_t li = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; li < count; li += warps) {
         const int r = list[li];
-        const int b = row[r], d = row[r + 1] - b;
+        const RT b = row[r];
+        const int d = (int)(row[r + 1] - b);
         int v[E];
 #pragma unroll
         for (int k = 0; k < E; k++) {
@@ -293,8 +309,9 @@ __global__ void k_sort_warp(const int *__restrict__ row, const int *__restrict__
 }
 
 // One CTA per row of length W16_MAX+1..MED_MAX: bitonic sort in shared memory.
+template <typename RT>
 __global__ void __launch_bounds__(MED_THREADS)
-k_sort_medium(const int *__restrict__ row, const int *__restrict__ list, const unsigned *cnt,
+k_sort_medium(const RT *__restrict__ row, const int *__restrict__ list, const unsigned *cnt,
               int *tmp, int dedup, int *ucnt)
 {
     __shared__ int s[MED_MAX];
@@ -302,7 +319,8 @@ k_sort_medium(const int *__restrict__ row, const int *__restrict__ list, const u
     const int count = (int)cnt[0];
     for (int li = blockIdx.x; li < count; li += gridDim.x) {
         const int r = list[li];
-        const int b = row[r], d = row[r + 1] - b;
+        const RT b = row[r];
+        const int d = (int)(row[r + 1] - b);
         int P = 64;
         while (P < d) P <<= 1;
         for (int i = threadIdx.x; i < P; i += blockDim.x) s[i] = i < d ? tmp[b + i] : INT_MAX;
@@ -346,8 +364,9 @@ k_sort_medium(const int *__restrict__ row, const int *__restrict__ list, const u
 // distinct values into tmp.  Stability within a 1024-element tile comes
 // from match_any ranks inside each warp and per-digit prefixes across warps
 // in warp order.
+template <typename RT>
 __global__ void __launch_bounds__(LARGE_THREADS)
-k_sort_large(const int *__restrict__ row, const int *__restrict__ list, const unsigned *cnt,
+k_sort_large(const RT *__restrict__ row, const int *__restrict__ list, const unsigned *cnt,
              int *tmp, int *tmp2, int key_bits, int dedup, int *ucnt)
 {
     __shared__ int s_hist[256];
@@ -360,7 +379,8 @@ k_sort_large(const int *__restrict__ row, const int *__restrict__ list, const un
     const int nwarps = blockDim.x >> 5;
     for (int li = blockIdx.x; li < count; li += gridDim.x) {
         const int r = list[li];
-        const int b = row[r], d = row[r + 1] - b;
+        const RT b = row[r];
+        const int d = (int)(row[r + 1] - b);
         int *from = tmp + b, *to = tmp2 + b;
         for (int shift = 0; shift < key_bits; shift += 8) {
             for (int i = threadIdx.x; i < 256; i += blockDim.x) s_hist[i] = 0;
@@ -428,17 +448,20 @@ k_sort_large(const int *__restrict__ row, const int *__restrict__ list, const un
 }
 
 // One warp per row: copy the packed distinct prefix of each row.
-__global__ void k_compact(const int *__restrict__ row, const int *__restrict__ row2, int n,
+template <typename RT>
+__global__ void k_compact(const RT *__restrict__ row, const RT *__restrict__ row2, int n,
                           const int *__restrict__ tmp, int *col)
 {
     const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
-        const int b = row[r], o = row2[r], c = row2[r + 1] - o;
+        const RT b = row[r], o = row2[r];
+        const int c = (int)(row2[r + 1] - o);
         for (int i = lane_id(); i < c; i += 32) col[o + i] = tmp[b + i];
     }
 }
 
-__global__ void k_finalize(const int *__restrict__ row, int n, unsigned *zmask, int *maxdeg,
+template <typename RT>
+__global__ void k_finalize(const RT *__restrict__ row, int n, unsigned *zmask, int *maxdeg,
                            unsigned long long *nonisolated)
 {
     __shared__ unsigned long long s_red[32];
@@ -450,7 +473,7 @@ __global__ void k_finalize(const int *__restrict__ row, int n, unsigned *zmask, 
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < (int64_t)W * 32;
          base += stride) {
         int64_t v = base + lane_id();
-        int d = v < n ? row[v + 1] - row[v] : 0;
+        int d = v < n ? (int)(row[v + 1] - row[v]) : 0;
         unsigned z = __ballot_sync(FULL, d == 0);  // out-of-range bits count as zero-degree
         if (lane_id() == 0) zmask[v >> 5] = z;
         mine += d > 0;
@@ -469,7 +492,8 @@ __global__ void k_finalize(const int *__restrict__ row, int n, unsigned *zmask, 
     }
 }
 
-__global__ void k_heavy_list(const int *__restrict__ row, int n, int *heavy, unsigned *cnt)
+template <typename RT>
+__global__ void k_heavy_list(const RT *__restrict__ row, int n, int *heavy, unsigned *cnt)
 {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
@@ -484,7 +508,8 @@ __global__ void k_heavy_list(const int *__restrict__ row, int n, int *heavy, uns
     }
 }
 
-__global__ void k_validate_csr(const int *__restrict__ row, const int *__restrict__ col, int n,
+template <typename RT>
+__global__ void k_validate_csr(const RT *__restrict__ row, const int *__restrict__ col, int n,
                                int64_t m, int *status)
 {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -495,16 +520,17 @@ __global__ void k_validate_csr(const int *__restrict__ row, const int *__restric
 }
 
 // Symmetry check on sorted rows: every (u,v) has (v,u).
-__global__ void k_check_sym(const int *__restrict__ row, const int *__restrict__ col, int n, int *flags)
+template <typename RT>
+__global__ void k_check_sym(const RT *__restrict__ row, const int *__restrict__ col, int n, int *flags)
 {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += stride) {
-        const int b = row[u], e = row[u + 1];
-        for (int i = b; i < e; i++) {
+        const RT b = row[u], e = row[u + 1];
+        for (RT i = b; i < e; i++) {
             const int v = col[i];
-            int lo = row[v], hi = row[v + 1];
+            RT lo = row[v], hi = row[v + 1];
             while (lo < hi) {
-                const int mid = (lo + hi) >> 1;
+                const RT mid = (lo + hi) >> 1;
                 if (col[mid] < (int)u) lo = mid + 1; else hi = mid;
             }
             if (lo >= row[v + 1] || col[lo] != (int)u) {
@@ -515,12 +541,13 @@ __global__ void k_check_sym(const int *__restrict__ row, const int *__restrict__
     }
 }
 
-__global__ void k_check_sorted(const int *__restrict__ row, const int *__restrict__ col, int n, int *flags)
+template <typename RT>
+__global__ void k_check_sorted(const RT *__restrict__ row, const int *__restrict__ col, int n, int *flags)
 {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += stride) {
-        const int b = row[u], e = row[u + 1];
-        for (int i = b + 1; i < e; i++)
+        const RT b = row[u], e = row[u + 1];
+        for (RT i = b + 1; i < e; i++)
             if (col[i - 1] > col[i]) {
                 flags[0] = 1;
                 break;
@@ -533,17 +560,20 @@ __global__ void k_check_sorted(const int *__restrict__ row, const int *__restric
 // probes first.  One warp per row below HUB_CTA_ROW, one CTA above.
 constexpr int HUB_CTA_ROW = 4096;
 
-__device__ __forceinline__ unsigned long long hub_key(const int *row, int v, int pos)
+template <typename RT>
+__device__ __forceinline__ unsigned long long hub_key(const RT *row, int v, int pos)
 {
     const unsigned d = (unsigned)(row[v + 1] - row[v]);
     return ((unsigned long long)d << 32) | (unsigned)(0x7fffffff - pos);
 }
 
-__global__ void k_hub_first_warp(const int *__restrict__ row, int n, int *col)
+template <typename RT>
+__global__ void k_hub_first_warp(const RT *__restrict__ row, int n, int *col)
 {
     const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
-        const int b = row[r], d = row[r + 1] - b;
+        const RT b = row[r];
+        const int d = (int)(row[r + 1] - b);
         if (d < 2 || d >= HUB_CTA_ROW) continue;
         unsigned long long best = 0;
         for (int i = lane_id(); i < d; i += 32) {
@@ -565,11 +595,13 @@ __global__ void k_hub_first_warp(const int *__restrict__ row, int n, int *col)
     }
 }
 
-__global__ void k_hub_first_cta(const int *__restrict__ row, int n, int *col)
+template <typename RT>
+__global__ void k_hub_first_cta(const RT *__restrict__ row, int n, int *col)
 {
     __shared__ unsigned long long s_best[32];
     for (int64_t r = blockIdx.x; r < n; r += gridDim.x) {
-        const int b = row[r], d = row[r + 1] - b;
+        const RT b = row[r];
+        const int d = (int)(row[r + 1] - b);
         if (d < HUB_CTA_ROW) continue;
         unsigned long long best = 0;
         for (int i = threadIdx.x; i < d; i += blockDim.x) {
@@ -607,7 +639,8 @@ struct Scratch {
     ~Scratch() { if (p) cudaFree(p); }
 };
 
-int finalize(DeviceCsr &out, cudaStream_t st, std::string &err)
+template <typename RT>
+int finalize_t(DeviceCsr &out, const RT *row, cudaStream_t st, std::string &err)
 {
     int rc = GBFS_OK;
     struct Res { unsigned long long nonisolated; int maxdeg; unsigned nheavy; } h{};
@@ -616,8 +649,8 @@ int finalize(DeviceCsr &out, cudaStream_t st, std::string &err)
     CK(cudaMalloc(&out.zmask, sizeof(unsigned) * (size_t)W));
     CK(cudaMalloc(&d_res, sizeof(Res)));
     CK(cudaMemsetAsync(d_res, 0, sizeof(Res), st));
-    k_finalize<<<grid_for((int64_t)W * 32, 256), 256, 0, st>>>(out.row, out.n, out.zmask,
-                                                                &d_res->maxdeg, &d_res->nonisolated);
+    k_finalize<<<grid_for((int64_t)W * 32, 256), 256, 0, st>>>(row, out.n, out.zmask, &d_res->maxdeg,
+                                                                &d_res->nonisolated);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(&h, d_res, sizeof(Res), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -626,7 +659,7 @@ int finalize(DeviceCsr &out, cudaStream_t st, std::string &err)
     {
         // heavy-row list (sized by a first count pass folded into k_heavy_list's atomic)
         CK(cudaMalloc(&out.heavy, sizeof(int) * (size_t)std::max<int64_t>(1, out.n)));
-        k_heavy_list<<<grid_for(out.n, 256), 256, 0, st>>>(out.row, out.n, out.heavy, &d_res->nheavy);
+        k_heavy_list<<<grid_for(out.n, 256), 256, 0, st>>>(row, out.n, out.heavy, &d_res->nheavy);
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(&h, d_res, sizeof(Res), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
@@ -635,6 +668,12 @@ int finalize(DeviceCsr &out, cudaStream_t st, std::string &err)
 done:
     if (d_res) cudaFree(d_res);
     return rc;
+}
+
+int finalize(DeviceCsr &out, cudaStream_t st, std::string &err)
+{
+    return out.wide ? finalize_t(out, (const long long *)out.row64, st, err)
+                    : finalize_t(out, (const int *)out.row, st, err);
 }
 
 // Sort every row of (row, col) in place (no dedup).  Scratch is allocated
@@ -654,18 +693,18 @@ int sort_rows_inplace(const int *row, int *col, int32_t n, int64_t m, cudaStream
     CK(cudaMalloc(&lcnt, 16));
     CK(cudaMalloc(&tmp2, sizeof(int) * (size_t)std::max<int64_t>(m, 1)));
     CK(cudaMemsetAsync(lcnt, 0, 16, st));
-    k_bin<<<grid_for(n, BIN_THREADS, 152 * 4), BIN_THREADS, 0, st>>>(row, n, med, large, w4, w16, lcnt);
+    k_bin<int><<<grid_for(n, BIN_THREADS, 152 * 4), BIN_THREADS, 0, st>>>(row, n, med, large, w4, w16, lcnt);
     CK(cudaGetLastError());
-    k_sort_small<<<grid_for((int64_t)n * 32, thr), thr, 0, st>>>(row, n, col, 0, ucnt);
+    k_sort_small<int><<<grid_for((int64_t)n * 32, thr), thr, 0, st>>>(row, n, col, 0, ucnt);
     CK(cudaGetLastError());
-    k_sort_warp<4><<<152 * 8, 256, 0, st>>>(row, w4, lcnt + 2, col, 0, ucnt);
+    k_sort_warp<4, int><<<152 * 8, 256, 0, st>>>(row, w4, lcnt + 2, col, 0, ucnt);
     CK(cudaGetLastError());
-    k_sort_warp<16><<<152 * 8, 256, 0, st>>>(row, w16, lcnt + 3, col, 0, ucnt);
+    k_sort_warp<16, int><<<152 * 8, 256, 0, st>>>(row, w16, lcnt + 3, col, 0, ucnt);
     CK(cudaGetLastError());
-    k_sort_medium<<<152 * 4, MED_THREADS, 0, st>>>(row, med, lcnt, col, 0, ucnt);
+    k_sort_medium<int><<<152 * 4, MED_THREADS, 0, st>>>(row, med, lcnt, col, 0, ucnt);
     CK(cudaGetLastError());
     while (key_bits < 31 && (1LL << key_bits) < (int64_t)n) key_bits++;
-    k_sort_large<<<152 * 2, LARGE_THREADS, 0, st>>>(row, large, lcnt, col, tmp2, key_bits, 0, ucnt);
+    k_sort_large<int><<<152 * 2, LARGE_THREADS, 0, st>>>(row, large, lcnt, col, tmp2, key_bits, 0, ucnt);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
 done:
@@ -689,12 +728,18 @@ int csr_check_symmetric(const DeviceCsr &c, cudaStream_t st, bool &sym, std::str
     const int grid = grid_for(c.n, 256, 152 * 8);
     CK(cudaMalloc(&flags, 8));
     CK(cudaMemsetAsync(flags, 0, 8, st));
-    k_check_sorted<<<grid, 256, 0, st>>>(c.row, c.col, c.n, flags);
+    if (c.wide) k_check_sorted<<<grid, 256, 0, st>>>((const long long *)c.row64, c.col, c.n, flags);
+    else k_check_sorted<<<grid, 256, 0, st>>>((const int *)c.row, c.col, c.n, flags);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(h, flags, 8, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     {
         const int *col = c.col;
+        if (h[0] && c.wide) {  // wide rows come sorted from the edge-list build
+            err = "unsorted rows of a wide graph";
+            rc = GBFS_ERR_TOO_LARGE;
+            goto done;
+        }
         if (h[0]) {  // unsorted rows: check a sorted copy
             CK(cudaMalloc(&copy, sizeof(int) * (size_t)std::max<int64_t>(c.m, 1)));
             CK(cudaMemcpyAsync(copy, c.col, sizeof(int) * (size_t)c.m, cudaMemcpyDeviceToDevice, st));
@@ -702,7 +747,8 @@ int csr_check_symmetric(const DeviceCsr &c, cudaStream_t st, bool &sym, std::str
             if (rc) goto done;
             col = copy;
         }
-        k_check_sym<<<grid, 256, 0, st>>>(c.row, col, c.n, flags);
+        if (c.wide) k_check_sym<<<grid, 256, 0, st>>>((const long long *)c.row64, col, c.n, flags);
+        else k_check_sym<<<grid, 256, 0, st>>>((const int *)c.row, col, c.n, flags);
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(h, flags, 8, cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
@@ -717,9 +763,15 @@ done:
 int csr_hub_first(DeviceCsr &c, cudaStream_t st, std::string &err)
 {
     int rc = GBFS_OK;
-    k_hub_first_warp<<<grid_for((int64_t)c.n * 32, 256), 256, 0, st>>>(c.row, c.n, c.col);
-    CK(cudaGetLastError());
-    k_hub_first_cta<<<152 * 2, 512, 0, st>>>(c.row, c.n, c.col);
+    if (c.wide) {
+        k_hub_first_warp<<<grid_for((int64_t)c.n * 32, 256), 256, 0, st>>>((const long long *)c.row64, c.n, c.col);
+        CK(cudaGetLastError());
+        k_hub_first_cta<<<152 * 2, 512, 0, st>>>((const long long *)c.row64, c.n, c.col);
+    } else {
+        k_hub_first_warp<<<grid_for((int64_t)c.n * 32, 256), 256, 0, st>>>((const int *)c.row, c.n, c.col);
+        CK(cudaGetLastError());
+        k_hub_first_cta<<<152 * 2, 512, 0, st>>>((const int *)c.row, c.n, c.col);
+    }
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
     c.hub_rows = true;
@@ -737,10 +789,12 @@ __global__ void k_in_count(const int *__restrict__ col, int64_t m, int *indeg)
 
 // first[v] / second[v]: row v's first / second entry, -1 past its end
 // (second may be null).
-__global__ void k_first(const int *__restrict__ row, const int *__restrict__ col, int n, int *first, int *second)
+template <typename RT>
+__global__ void k_first(const RT *__restrict__ row, const int *__restrict__ col, int n, int *first, int *second)
 {
     for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-        const int b = row[v], d = row[v + 1] - b;
+        const RT b = row[v];
+        const int d = (int)(row[v + 1] - b);
         first[v] = d > 0 ? col[b] : -1;
         if (second) second[v] = d > 1 ? col[b + 1] : -1;
     }
@@ -759,6 +813,10 @@ __global__ void k_in_scatter(const int *__restrict__ row, const int *__restrict_
 int csr_build_transpose(DeviceCsr &c, cudaStream_t st, std::string &err)
 {
     if (c.trow) return GBFS_OK;
+    if (c.wide) {
+        err = "no transpose of a graph with 64-bit row offsets (its searches stay top-down)";
+        return GBFS_ERR_TOO_LARGE;
+    }
     int rc = GBFS_OK;
     const int n = c.n;
     const int64_t m = c.m;
@@ -789,15 +847,15 @@ int csr_build_transpose(DeviceCsr &c, cudaStream_t st, std::string &err)
         k_in_scatter<<<grid_for((int64_t)n * 32, 256), 256, 0, st>>>(c.row, c.col, n, cursor, tcol);
         CK(cudaGetLastError());
     }
-    k_heavy_list<<<grid_for(n, 256), 256, 0, st>>>(trow, n, theavy, d_nheavy);
+    k_heavy_list<<<grid_for(n, 256), 256, 0, st>>>((const int *)trow, n, theavy, d_nheavy);
     CK(cudaGetLastError());
     // in-rows hub-first (the in-neighbour of highest in-degree, the likeliest
     // to be reached early, is probed first), then their first entries
-    k_hub_first_warp<<<grid_for((int64_t)n * 32, 256), 256, 0, st>>>(trow, n, tcol);
+    k_hub_first_warp<<<grid_for((int64_t)n * 32, 256), 256, 0, st>>>((const int *)trow, n, tcol);
     CK(cudaGetLastError());
-    k_hub_first_cta<<<152 * 2, 512, 0, st>>>(trow, n, tcol);
+    k_hub_first_cta<<<152 * 2, 512, 0, st>>>((const int *)trow, n, tcol);
     CK(cudaGetLastError());
-    k_first<<<grid_for(n, 256), 256, 0, st>>>(trow, tcol, n, tfirst, nullptr);
+    k_first<<<grid_for(n, 256), 256, 0, st>>>((const int *)trow, (const int *)tcol, n, tfirst, (int *)nullptr);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(&h_nheavy, d_nheavy, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -835,7 +893,12 @@ int csr_build_first(DeviceCsr &c, cudaStream_t st, std::string &err)
     // hub-first rows are probed at their first entry alone: no second array
     if (!c.hub_rows && !c.second) CK(cudaMalloc(&c.second, sizeof(int) * (size_t)std::max(1, c.n)));
     if (c.n > 0) {
-        k_first<<<grid_for(c.n, 256), 256, 0, st>>>(c.row, c.col, c.n, c.first, c.second);
+        if (c.wide)
+            k_first<<<grid_for(c.n, 256), 256, 0, st>>>((const long long *)c.row64, (const int *)c.col, c.n, c.first,
+                                                        c.second);
+        else
+            k_first<<<grid_for(c.n, 256), 256, 0, st>>>((const int *)c.row, (const int *)c.col, c.n, c.first,
+                                                        c.second);
         CK(cudaGetLastError());
     }
     CK(cudaStreamSynchronize(st));
@@ -846,7 +909,7 @@ done:
 int64_t csr_device_bytes(const DeviceCsr &c)
 {
     const int64_t n = c.n, m = c.m;
-    int64_t b = 4 * (n + 1 + m) + 4 * ((n + 31) / 32) + 4 * n;  // row, col, zmask, heavy list
+    int64_t b = (c.wide ? 8 : 4) * (n + 1) + 4 * m + 4 * ((n + 31) / 32) + 4 * n;  // row, col, zmask, heavy list
     if (c.first) b += 4 * n;
     if (c.second) b += 4 * n;
     if (c.pieces) b += 8 * (int64_t)c.npieces;
@@ -868,18 +931,121 @@ void csr_free(DeviceCsr &c)
     if (c.heavy) cudaFree(c.heavy);
     if (c.pieces) cudaFree(c.pieces);
     if (c.row) cudaFree(c.row);
+    if (c.row64) cudaFree(c.row64);
     if (c.col) cudaFree(c.col);
     if (c.zmask) cudaFree(c.zmask);
     c = DeviceCsr{};
 }
 
+namespace {
+
+inline cudaError_t scan_rows(const int *in, int *out, int64_t n, ScanScratch &ss, cudaStream_t st)
+{
+    return scan_exclusive_i32_i32(in, out, n, out + n, ss, st);
+}
+inline cudaError_t scan_rows(const int *in, long long *out, int64_t n, ScanScratch &ss, cudaStream_t st)
+{
+    return scan_exclusive_i32_i64(in, out, n, out + n, ss, st);
+}
+
+// Steps 2-5 with row offsets of type RT (int, or long long for wide
+// graphs): offsets from the degrees, scatter, per-row sort, dedup
+// compaction.  md: edges before deduplication.  On success the offsets and
+// columns move to row_out / col_out.
+template <typename RT>
+int build_rows(int32_t n, int64_t m, int64_t md, const int *d_src, const int *d_dst, unsigned flags,
+               const int *deg, ScanScratch &ss, unsigned *lcnt, cudaStream_t st, RT *&row_out, int *&col_out,
+               int64_t &m_out, std::string &err)
+{
+    int rc = GBFS_OK;
+    const bool dedup = flags & GBFS_DEDUP;
+    RT *row = nullptr, *cursor = nullptr, *row2 = nullptr;
+    int *tmp = nullptr, *tmp2 = nullptr, *ucnt = nullptr, *med = nullptr, *large = nullptr, *w4 = nullptr,
+        *w16 = nullptr, *col = nullptr;
+    int key_bits = 1;
+    const int thr = 256;
+    CK(cudaMalloc(&row, sizeof(RT) * ((size_t)n + 1)));
+    CK(scan_rows(deg, row, n, ss, st));
+    CK(cudaMalloc(&cursor, sizeof(RT) * ((size_t)n + 1)));
+    CK(cudaMemcpyAsync(cursor, row, sizeof(RT) * ((size_t)n + 1), cudaMemcpyDeviceToDevice, st));
+    CK(cudaMalloc(&tmp, sizeof(int) * (size_t)std::max<int64_t>(md, 1)));
+    if (m > 0) {
+        k_scatter<RT><<<grid_for(m, thr), thr, 0, st>>>(d_src, d_dst, m, n, flags, cursor, tmp);
+        CK(cudaGetLastError());
+    }
+    CK(cudaStreamSynchronize(st));
+    cudaFree(cursor);
+    cursor = nullptr;
+
+    // Per-row sort (+ distinct count).
+    CK(cudaMalloc(&ucnt, sizeof(int) * ((size_t)n + 1)));
+    CK(cudaMalloc(&med, sizeof(int) * (size_t)n));
+    CK(cudaMalloc(&large, sizeof(int) * (size_t)n));
+    CK(cudaMalloc(&w4, sizeof(int) * (size_t)n));
+    CK(cudaMalloc(&w16, sizeof(int) * (size_t)n));
+    k_bin<RT><<<grid_for(n, BIN_THREADS, 152 * 4), BIN_THREADS, 0, st>>>(row, n, med, large, w4, w16, lcnt);
+    CK(cudaGetLastError());
+    k_sort_small<RT><<<grid_for((int64_t)n * 32, thr), thr, 0, st>>>(row, n, tmp, dedup, ucnt);
+    CK(cudaGetLastError());
+    k_sort_warp<4, RT><<<152 * 8, 256, 0, st>>>(row, w4, lcnt + 2, tmp, dedup, ucnt);
+    CK(cudaGetLastError());
+    k_sort_warp<16, RT><<<152 * 8, 256, 0, st>>>(row, w16, lcnt + 3, tmp, dedup, ucnt);
+    CK(cudaGetLastError());
+    k_sort_medium<RT><<<152 * 4, MED_THREADS, 0, st>>>(row, med, lcnt, tmp, dedup, ucnt);
+    CK(cudaGetLastError());
+    while (key_bits < 31 && (1LL << key_bits) < (int64_t)n) key_bits++;
+    CK(cudaMalloc(&tmp2, sizeof(int) * (size_t)std::max<int64_t>(md, 1)));
+    k_sort_large<RT><<<152 * 2, LARGE_THREADS, 0, st>>>(row, large, lcnt, tmp, tmp2, key_bits, dedup, ucnt);
+    CK(cudaGetLastError());
+
+    if (dedup) {
+        RT h_m2 = 0;
+        CK(cudaMalloc(&row2, sizeof(RT) * ((size_t)n + 1)));
+        CK(scan_rows(ucnt, row2, n, ss, st));
+        CK(cudaMemcpyAsync(&h_m2, row2 + n, sizeof(RT), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        cudaFree(tmp2);  // the sorts are done; room for the compacted columns
+        tmp2 = nullptr;
+        CK(cudaMalloc(&col, sizeof(int) * (size_t)std::max<int64_t>((int64_t)h_m2, 1)));
+        k_compact<RT><<<grid_for((int64_t)n * 32, thr), thr, 0, st>>>(row, row2, n, tmp, col);
+        CK(cudaGetLastError());
+        CK(cudaStreamSynchronize(st));
+        cudaFree(row);
+        row = row2;
+        row2 = nullptr;
+        m_out = (int64_t)h_m2;
+    } else {
+        CK(cudaStreamSynchronize(st));
+        col = tmp;
+        tmp = nullptr;
+        m_out = md;
+    }
+    row_out = row;
+    col_out = col;
+    row = nullptr;
+    col = nullptr;
+done:
+    if (row) cudaFree(row);
+    if (row2) cudaFree(row2);
+    if (cursor) cudaFree(cursor);
+    if (col) cudaFree(col);
+    if (tmp) cudaFree(tmp);
+    if (tmp2) cudaFree(tmp2);
+    if (ucnt) cudaFree(ucnt);
+    if (med) cudaFree(med);
+    if (large) cudaFree(large);
+    if (w4) cudaFree(w4);
+    if (w16) cudaFree(w16);
+    return rc;
+}
+
+}  // namespace
+
 int csr_build_from_edges(int32_t n, int64_t m, const int *d_src, const int *d_dst, unsigned flags,
                          cudaStream_t st, DeviceCsr &out, std::string &err)
 {
     int rc = GBFS_OK;
-    const bool dedup = flags & GBFS_DEDUP;
-    int *deg = nullptr, *cursor = nullptr, *tmp = nullptr, *tmp2 = nullptr, *ucnt = nullptr;
-    int *med = nullptr, *large = nullptr, *row2 = nullptr, *w4 = nullptr, *w16 = nullptr;
+    int *deg = nullptr;
     unsigned *lcnt = nullptr;
     int *status = nullptr;
     unsigned long long *total = nullptr;
@@ -887,8 +1053,6 @@ int csr_build_from_edges(int32_t n, int64_t m, const int *d_src, const int *d_ds
     ScanScratch ss;
     unsigned long long h_total = 0;
     int h_status = 0;
-    int64_t md = 0;
-    int key_bits = 1;
     const int thr = 256;
     out = DeviceCsr{};
     out.n = n;
@@ -912,73 +1076,24 @@ int csr_build_from_edges(int32_t n, int64_t m, const int *d_src, const int *d_ds
     CK(cudaMemcpyAsync(&h_total, total, 8, cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(&h_status, status, 4, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
+    if (h_status == DEV_OVERFLOW) {
+        err = "a vertex with 2^30 or more edges";
+        rc = GBFS_ERR_TOO_LARGE;
+        goto done;
+    }
     if (h_status != DEV_OK) {
         err = "edge endpoint outside [0, n)";
         rc = GBFS_ERR_INVALID_ARG;
         goto done;
     }
-    if (h_total > (unsigned long long)INT32_MAX) {
-        err = "more than 2^31-1 directed edges";
-        rc = GBFS_ERR_TOO_LARGE;
-        goto done;
-    }
-    md = (int64_t)h_total;
-
-    CK(cudaMalloc(&out.row, sizeof(int) * ((size_t)n + 1)));
-    CK(scan_exclusive_i32_i32(deg, out.row, n, out.row + n, ss, st));
-    CK(cudaMalloc(&cursor, sizeof(int) * ((size_t)n + 1)));
-    CK(cudaMemcpyAsync(cursor, out.row, sizeof(int) * ((size_t)n + 1), cudaMemcpyDeviceToDevice, st));
-    CK(cudaMalloc(&tmp, sizeof(int) * (size_t)std::max<int64_t>(md, 1)));
-    if (m > 0) {
-        k_scatter<<<grid_for(m, thr), thr, 0, st>>>(d_src, d_dst, m, n, flags, cursor, tmp);
-        CK(cudaGetLastError());
-    }
-    cudaFree(cursor);
-    cursor = nullptr;
-    cudaFree(deg);
-    deg = nullptr;
-
-    // Per-row sort (+ distinct count).
-    CK(cudaMalloc(&ucnt, sizeof(int) * ((size_t)n + 1)));
-    CK(cudaMalloc(&med, sizeof(int) * (size_t)n));
-    CK(cudaMalloc(&large, sizeof(int) * (size_t)n));
-    CK(cudaMalloc(&w4, sizeof(int) * (size_t)n));
-    CK(cudaMalloc(&w16, sizeof(int) * (size_t)n));
-    k_bin<<<grid_for(n, BIN_THREADS, 152 * 4), BIN_THREADS, 0, st>>>(out.row, n, med, large, w4, w16, lcnt);
-    CK(cudaGetLastError());
-    k_sort_small<<<grid_for((int64_t)n * 32, thr), thr, 0, st>>>(out.row, n, tmp, dedup, ucnt);
-    CK(cudaGetLastError());
-    k_sort_warp<4><<<152 * 8, 256, 0, st>>>(out.row, w4, lcnt + 2, tmp, dedup, ucnt);
-    CK(cudaGetLastError());
-    k_sort_warp<16><<<152 * 8, 256, 0, st>>>(out.row, w16, lcnt + 3, tmp, dedup, ucnt);
-    CK(cudaGetLastError());
-    k_sort_medium<<<152 * 4, MED_THREADS, 0, st>>>(out.row, med, lcnt, tmp, dedup, ucnt);
-    CK(cudaGetLastError());
-    while (key_bits < 31 && (1LL << key_bits) < (int64_t)n) key_bits++;
-    CK(cudaMalloc(&tmp2, sizeof(int) * (size_t)std::max<int64_t>(md, 1)));
-    k_sort_large<<<152 * 2, LARGE_THREADS, 0, st>>>(out.row, large, lcnt, tmp, tmp2, key_bits, dedup,
-                                                    ucnt);
-    CK(cudaGetLastError());
-
-    if (dedup) {
-        int h_m2 = 0;
-        CK(cudaMalloc(&row2, sizeof(int) * ((size_t)n + 1)));
-        CK(scan_exclusive_i32_i32(ucnt, row2, n, row2 + n, ss, st));
-        CK(cudaMemcpyAsync(&h_m2, row2 + n, 4, cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        CK(cudaMalloc(&out.col, sizeof(int) * (size_t)std::max(h_m2, 1)));
-        k_compact<<<grid_for((int64_t)n * 32, thr), thr, 0, st>>>(out.row, row2, n, tmp, out.col);
-        CK(cudaGetLastError());
-        CK(cudaStreamSynchronize(st));
-        cudaFree(out.row);
-        out.row = row2;
-        row2 = nullptr;
-        out.m = h_m2;
-    } else {
-        out.col = tmp;
-        tmp = nullptr;
-        out.m = md;
-    }
+    out.wide = (flags & GBFS_WIDE_ROWS) || h_total > (unsigned long long)INT32_MAX;
+    if (out.wide)
+        rc = build_rows<long long>(n, m, (int64_t)h_total, d_src, d_dst, flags, deg, ss, lcnt, st, out.row64,
+                                   out.col, out.m, err);
+    else
+        rc = build_rows<int>(n, m, (int64_t)h_total, d_src, d_dst, flags, deg, ss, lcnt, st, out.row, out.col,
+                             out.m, err);
+    if (rc) goto done;
     {
         unsigned h_scan_status[3] = {0, 0, 0};
         CK(cudaMemcpyAsync(h_scan_status, ss.ctl, 12, cudaMemcpyDeviceToHost, st));
@@ -993,39 +1108,27 @@ int csr_build_from_edges(int32_t n, int64_t m, const int *d_src, const int *d_ds
 
 done:
     if (deg) cudaFree(deg);
-    if (cursor) cudaFree(cursor);
-    if (tmp) cudaFree(tmp);
-    if (tmp2) cudaFree(tmp2);
-    if (ucnt) cudaFree(ucnt);
-    if (med) cudaFree(med);
-    if (large) cudaFree(large);
-    if (w4) cudaFree(w4);
-    if (w16) cudaFree(w16);
-    if (row2) cudaFree(row2);
     if (status) cudaFree(status);
     if (scan_mem) cudaFree(scan_mem);
     if (rc != GBFS_OK) csr_free(out);
     return rc;
 }
 
-int csr_adopt(int32_t n, int64_t m, int *d_row, int *d_col, cudaStream_t st, DeviceCsr &out,
-              std::string &err)
+namespace {
+
+template <typename RT>
+int csr_adopt_t(int32_t n, int64_t m, RT *d_row, int *d_col, cudaStream_t st, DeviceCsr &out, std::string &err)
 {
     int rc = GBFS_OK;
     int *status = nullptr;
-    int h[2] = {0, 0};
+    RT h[2] = {0, 0};
     int h_status = 0;
-    out = DeviceCsr{};
-    out.n = n;
-    out.m = m;
-    out.row = d_row;
-    out.col = d_col;
     CK(cudaMalloc(&status, sizeof(int)));
     CK(cudaMemsetAsync(status, 0, sizeof(int), st));
-    k_validate_csr<<<grid_for(std::max<int64_t>(m, n), 256), 256, 0, st>>>(d_row, d_col, n, m, status);
+    k_validate_csr<RT><<<grid_for(std::max<int64_t>(m, n), 256), 256, 0, st>>>(d_row, d_col, n, m, status);
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(&h[0], d_row, 4, cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(&h[1], d_row + n, 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&h[0], d_row, sizeof(RT), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&h[1], d_row + n, sizeof(RT), cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(&h_status, status, 4, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     if (h[0] != 0 || (int64_t)h[1] != m || h_status != DEV_OK) {
@@ -1039,6 +1142,31 @@ done:
     if (status) cudaFree(status);
     if (rc != GBFS_OK) csr_free(out);
     return rc;
+}
+
+}  // namespace
+
+int csr_adopt(int32_t n, int64_t m, int *d_row, int *d_col, cudaStream_t st, DeviceCsr &out,
+              std::string &err)
+{
+    out = DeviceCsr{};
+    out.n = n;
+    out.m = m;
+    out.row = d_row;
+    out.col = d_col;
+    return csr_adopt_t(n, m, d_row, d_col, st, out, err);
+}
+
+int csr_adopt64(int32_t n, int64_t m, long long *d_row, int *d_col, cudaStream_t st, DeviceCsr &out,
+                std::string &err)
+{
+    out = DeviceCsr{};
+    out.n = n;
+    out.m = m;
+    out.row64 = d_row;
+    out.wide = true;
+    out.col = d_col;
+    return csr_adopt_t(n, m, d_row, d_col, st, out, err);
 }
 
 }  // namespace gbfs

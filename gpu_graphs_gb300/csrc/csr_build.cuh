@@ -13,7 +13,9 @@ namespace gbfs {
 struct DeviceCsr {
     int32_t n = 0;
     int64_t m = 0;
-    int *row = nullptr;        // n+1
+    int *row = nullptr;        // n+1 (null when wide)
+    long long *row64 = nullptr;  // n+1, wide graphs only: 64-bit row offsets (more than 2^31-1 edges)
+    bool wide = false;
     int *col = nullptr;        // m
     unsigned *zmask = nullptr; // (n+31)/32
     int32_t max_degree = 0;
@@ -49,7 +51,8 @@ constexpr int HEAVY_DEGREE = 64;
 
 // Build from device edge arrays (m entries each).  Returns a GBFS_* status;
 // on failure `err` says why.  All work is ordered on `st`; the call
-// synchronises `st` before returning.
+// synchronises `st` before returning.  The row offsets are 64-bit (`wide`)
+// when the edges to store could exceed 2^31-1, or with GBFS_WIDE_ROWS.
 int csr_build_from_edges(int32_t n, int64_t m, const int *d_src, const int *d_dst,
                          unsigned flags, cudaStream_t st, DeviceCsr &out, std::string &err);
 
@@ -57,6 +60,9 @@ int csr_build_from_edges(int32_t n, int64_t m, const int *d_src, const int *d_ds
 // validate it and compute zmask / max_degree / nonisolated.
 int csr_adopt(int32_t n, int64_t m, int *d_row, int *d_col, cudaStream_t st, DeviceCsr &out,
               std::string &err);
+// The same with 64-bit row offsets (a wide graph).
+int csr_adopt64(int32_t n, int64_t m, long long *d_row, int *d_col, cudaStream_t st, DeviceCsr &out,
+                std::string &err);
 
 // in-edges == out-edges?  Rows need not be sorted (a sorted copy is checked).
 int csr_check_symmetric(const DeviceCsr &c, cudaStream_t st, bool &sym, std::string &err);
@@ -65,7 +71,8 @@ int csr_check_symmetric(const DeviceCsr &c, cudaStream_t st, bool &sym, std::str
 int csr_hub_first(DeviceCsr &c, cudaStream_t st, std::string &err);
 
 // Build c.trow / c.tcol (the in-edge CSR, rows hub-first) with c.tfirst and
-// c.theavy; a no-op once built.  Synchronises st.
+// c.theavy; a no-op once built.  Synchronises st.  Not for wide graphs
+// (GBFS_ERR_TOO_LARGE: their searches stay top-down).
 int csr_build_transpose(DeviceCsr &c, cudaStream_t st, std::string &err);
 
 // (Re)compute c.first / c.second from the rows as they are now.  Synchronises st.

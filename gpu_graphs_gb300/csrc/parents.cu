@@ -27,17 +27,18 @@ namespace {
 
 constexpr int PT = 256;
 
-__global__ void k_parents_pull_light(const int *__restrict__ row, const int *__restrict__ col, int n,
+template <typename RT>
+__global__ void k_parents_pull_light(const RT *__restrict__ row, const int *__restrict__ col, int n,
                                      const int *__restrict__ level, int *__restrict__ parent)
 {
     for (long long v = (long long)blockIdx.x * PT + threadIdx.x; v < n; v += (long long)gridDim.x * PT) {
         const int lv = level[v];
-        const int b = row[v], e = row[v + 1];
+        const RT b = row[v], e = row[v + 1];
         if (lv > 0 && e - b > HEAVY_DEGREE) continue;  // the heavy kernel's row
         int best = -1;
         if (lv > 0) {
             best = INT_MAX;
-            for (int i = b; i < e; i++) {
+            for (RT i = b; i < e; i++) {
                 const int u = col[i];
                 if (u < best && level[u] == lv - 1) best = u;
             }
@@ -46,7 +47,8 @@ __global__ void k_parents_pull_light(const int *__restrict__ row, const int *__r
     }
 }
 
-__global__ void k_parents_pull_heavy(const int *__restrict__ row, const int *__restrict__ col,
+template <typename RT>
+__global__ void k_parents_pull_heavy(const RT *__restrict__ row, const int *__restrict__ col,
                                      const int *__restrict__ heavy, int nheavy, const int *__restrict__ level,
                                      int *__restrict__ parent)
 {
@@ -58,7 +60,7 @@ __global__ void k_parents_pull_heavy(const int *__restrict__ row, const int *__r
         const int lv = level[v];
         if (lv <= 0) continue;  // written by the light kernel
         int best = INT_MAX;
-        for (int i = row[v] + lane; i < row[v + 1]; i += 32) {
+        for (RT i = row[v] + lane; i < row[v + 1]; i += 32) {
             const int u = col[i];
             if (u < best && level[u] == lv - 1) best = u;
         }
@@ -75,7 +77,8 @@ __global__ void k_parents_init(int n, const int *__restrict__ level, int *__rest
 }
 
 // one warp per vertex u: offer u to the out-neighbours one level further
-__global__ void k_parents_push(const int *__restrict__ row, const int *__restrict__ col, int n,
+template <typename RT>
+__global__ void k_parents_push(const RT *__restrict__ row, const int *__restrict__ col, int n,
                                const int *__restrict__ level, int *parent)
 {
     const long long gw = ((long long)blockIdx.x * PT + threadIdx.x) >> 5;
@@ -84,7 +87,7 @@ __global__ void k_parents_push(const int *__restrict__ row, const int *__restric
     for (long long u = gw; u < n; u += nw) {
         const int lu = level[u];
         if (lu < 0) continue;
-        for (int i = row[u] + lane; i < row[u + 1]; i += 32) {
+        for (RT i = row[u] + lane; i < row[u + 1]; i += 32) {
             const int v = col[i];
             if (level[v] == lu + 1 && parent[v] > (int)u) atomicMin(parent + v, (int)u);
         }
@@ -99,19 +102,31 @@ int grid_of(long long work, int cap)
 
 }  // namespace
 
+namespace {
+
+template <typename RT>
+cudaError_t parents_launch(const DeviceCsr &g, const RT *row, bool symmetric, const int *d_level, int *d_parent,
+                           cudaStream_t st)
+{
+    if (symmetric) {
+        k_parents_pull_light<RT><<<grid_of(g.n, 152 * 16), PT, 0, st>>>(row, g.col, g.n, d_level, d_parent);
+        if (g.nheavy > 0)
+            k_parents_pull_heavy<RT><<<grid_of((long long)g.nheavy * 32, 152 * 16), PT, 0, st>>>(
+                row, g.col, g.heavy, g.nheavy, d_level, d_parent);
+    } else {
+        k_parents_init<<<grid_of(g.n, 152 * 16), PT, 0, st>>>(g.n, d_level, d_parent);
+        k_parents_push<RT><<<grid_of((long long)g.n * 32, 152 * 16), PT, 0, st>>>(row, g.col, g.n, d_level, d_parent);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace
+
 cudaError_t parents_enqueue(const DeviceCsr &g, bool symmetric, const int *d_level, int *d_parent, cudaStream_t st)
 {
     if (g.n == 0) return cudaSuccess;
-    if (symmetric) {
-        k_parents_pull_light<<<grid_of(g.n, 152 * 16), PT, 0, st>>>(g.row, g.col, g.n, d_level, d_parent);
-        if (g.nheavy > 0)
-            k_parents_pull_heavy<<<grid_of((long long)g.nheavy * 32, 152 * 16), PT, 0, st>>>(
-                g.row, g.col, g.heavy, g.nheavy, d_level, d_parent);
-    } else {
-        k_parents_init<<<grid_of(g.n, 152 * 16), PT, 0, st>>>(g.n, d_level, d_parent);
-        k_parents_push<<<grid_of((long long)g.n * 32, 152 * 16), PT, 0, st>>>(g.row, g.col, g.n, d_level, d_parent);
-    }
-    return cudaGetLastError();
+    return g.wide ? parents_launch(g, (const long long *)g.row64, symmetric, d_level, d_parent, st)
+                  : parents_launch(g, (const int *)g.row, symmetric, d_level, d_parent, st);
 }
 
 }  // namespace gbfs

@@ -365,6 +365,7 @@ extern "C" void gbfs_server_destroy(gbfs_server *s)
 extern "C" int gbfs_server_add_graph(gbfs_server *s, gbfs_graph *g, int32_t *graph_id)
 {
     if (!s || !g || !graph_id) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
+    if (g->csr.wide) return fail(GBFS_ERR_TOO_LARGE, "the server's multi-source slots need 32-bit row offsets");
     std::lock_guard<std::mutex> admit(s->admit_mu);
     std::unique_lock<std::mutex> lk(s->mu);
     // a directed graph that may step bottom-up gets its transpose (in-edge

@@ -67,6 +67,9 @@ const char *gbfs_version(void);
  * probe it first, which resolves most unvisited vertices with one probe on
  * power-law graphs.  Levels are unaffected. */
 #define GBFS_HUB_FIRST        8u
+/* Store 64-bit row offsets even when 32-bit ones would do (graphs whose
+ * stored edges can exceed 2^31-1 get them anyway). */
+#define GBFS_WIDE_ROWS       16u
 
 typedef struct gbfs_graph gbfs_graph;
 
@@ -75,8 +78,14 @@ typedef struct gbfs_graph gbfs_graph;
  * scatter, per-row sort, dedup, compaction).  Rows come out sorted
  * ascending (see GBFS_HUB_FIRST for the one exception).  src/dst: m int32 vertex ids in [0, n), host or device.
  * Replaces csr::csr / csc::csc (which parse a file into host CSR; the file
- * parser is gbfs_read_edge_list below).  Limits: n <= 2^31-2, stored
- * directed edges <= 2^31-1 (GBFS_ERR_TOO_LARGE otherwise).
+ * parser is gbfs_read_edge_list below).  Limits: n <= 2^31-2; a graph
+ * whose stored directed edges can exceed 2^31-1 (counted before
+ * deduplication) gets 64-bit row offsets ("wide", also with
+ * GBFS_WIDE_ROWS).  A wide graph supports single-source searches (top-down
+ * and, when built symmetric, direction-optimising), parents, the trace,
+ * gbfs_graph_csr64 and the binary cache; multi-source searches, graph sets,
+ * the server, per-level launch modes and the transpose of a directed wide
+ * graph return GBFS_ERR_TOO_LARGE.
  */
 int gbfs_graph_from_edges(int32_t n, int64_t m, const int32_t *src,
                           const int32_t *dst, uint32_t flags,
@@ -101,13 +110,19 @@ typedef struct gbfs_graph_info {
     int64_t device_bytes;       /* CSR and what is built on it (first-entry
                                    arrays, pull pieces, transpose) + per-graph
                                    search workspace                          */
+    int32_t wide;               /* 1: 64-bit row offsets                     */
+    int32_t reserved;
 } gbfs_graph_info;
 
 int gbfs_graph_get_info(const gbfs_graph *g, gbfs_graph_info *info);
 
-/* Copy the device CSR out: row_offset n+1, col_idx m (host or device). */
+/* Copy the device CSR out: row_offset n+1, col_idx m (host or device).
+ * GBFS_ERR_TOO_LARGE for a wide graph (64-bit row offsets). */
 int gbfs_graph_get_csr(const gbfs_graph *g, int32_t *row_offset,
                        int32_t *col_idx);
+/* The same with 64-bit row offsets, for any graph. */
+int gbfs_graph_get_csr64(const gbfs_graph *g, int64_t *row_offset,
+                         int32_t *col_idx);
 
 /* ---- traversal parameters (autotuned) --------------------------------- */
 /* Bottom-up steps probe in-edges: on a directed graph the first traversal

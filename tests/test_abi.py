@@ -52,7 +52,8 @@ def test_null_and_range_arguments(gb):
     h = C.c_void_p()
     assert lib.gbfs_graph_from_edges(0, 0, None, None, 0, C.byref(h)) == gb._lib.ERR_INVALID_ARG
     assert lib.gbfs_graph_from_edges(5, 3, None, None, 0, C.byref(h)) == gb._lib.ERR_INVALID_ARG
-    assert lib.gbfs_graph_from_edges(5, 0, None, None, 16, C.byref(h)) == gb._lib.ERR_INVALID_ARG
+    assert lib.gbfs_graph_from_edges(5, 0, None, None, 32, C.byref(h)) == gb._lib.ERR_INVALID_ARG  # unknown flag
+    assert lib.gbfs_graph_get_csr64(None, None, None) == gb._lib.ERR_INVALID_ARG
     assert lib.gbfs_bfs(None, 0, None, None) == gb._lib.ERR_INVALID_ARG
     assert lib.gbfs_graph_get_info(None, None) == gb._lib.ERR_INVALID_ARG
     assert lib.gbfs_exclusive_scan_i32(None, None, -1, None) == gb._lib.ERR_INVALID_ARG
