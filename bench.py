@@ -27,8 +27,10 @@ Extra objects on the same line (rank 0, skipped with --no-extra): config1
 the reference binaries' stored output), e2e_from_edge_list (host edge list
 -> CSR build -> 64 searches -> host levels), grid (7000 x 7000, persistent
 vs one launch per level), batched (64-lane multi-source on RMAT-20; 512
-small graphs in one launch), primitives (CSR build, exclusive scan) and
-serving (32 resident graphs, Poisson arrivals; --no-serving skips it).  The
+small graphs in one launch), primitives (CSR build, exclusive scan),
+graph500 (RMAT scales 26 and 27 at edge factor 16, the latter with 64-bit
+row offsets; --no-large skips them) and serving (32 resident graphs,
+Poisson arrivals; --no-serving skips it).  The
 batched and serving objects carry a cpu_parallel throughput: the same
 queries through the oracle's queue BFS, one query per host core at a time.
 
@@ -78,6 +80,8 @@ def parse_args():
                     help="CSR row order: sorted ids, or highest-degree neighbour first")
     ap.add_argument("--no-extra", action="store_true", help="skip the grid and batched measurements")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving sweep (32 resident graphs)")
+    ap.add_argument("--no-large", action="store_true",
+                    help="skip the RMAT scale-26 and scale-27 graphs (the latter with 64-bit row offsets)")
     ap.add_argument("--grid-side", type=int, default=7000)
     ap.add_argument("--grid-only", action="store_true",
                     help="only --steps persistent searches on the --grid-side grid (a profiling workload)")
@@ -518,6 +522,37 @@ def grid_only(side: int, reps: int) -> dict:
             "searches": len(runs), "ms": round(ms, 3), "us_per_level": round(1e3 * ms / max(1, st.levels), 3)}
 
 
+def measure_rmat_large(torch, scale: int, edge_factor: int = 16, nsrc: int = 8) -> dict:
+    """A Graph500-size RMAT graph (the bench's a/b/c and seed): build time
+    from the host edge list and device-timed searches from nsrc sources, one
+    launch each.  From scale 27 on (edge factor 16) the stored edges pass
+    2^31-1 and the CSR gets 64-bit row offsets; bit-exact parity at these
+    sizes is in tests/test_wide_gpu.py and tests/test_fullsize_gpu.py."""
+    import gpu_graphs_gb300 as gb
+    src, dst = gb.gen_rmat(scale, edge_factor, RMAT["a"], RMAT["b"], RMAT["c"], RMAT["seed"])
+    n = 1 << scale
+    pairs = len(src)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g = gb.Graph.from_edges(n, src, dst, gb.UNDIRECTED | gb.HUB_FIRST)
+    build_s = time.perf_counter() - t0
+    del src, dst
+    sources = pick_sources(np.diff(g.row_offsets()), nsrc)
+    out = torch.empty((nsrc, n), dtype=torch.int32, device="cuda")
+    g.bfs_many(sources, out=out)
+    _, sts = g.bfs_many(sources, out=out)
+    ms = float(sum(x.ms for x in sts))
+    ec = sum(x.edges_in_component for x in sts)
+    res = {"workload": f"RMAT scale {scale}, edge factor {edge_factor} ({pairs} pairs), undirected, hub-first rows",
+           "vertices": n, "directed_edges": int(g.m), "row_offset_bits": 64 if g.wide else 32,
+           "build_s_from_host_edges": round(build_s, 3), "sources": nsrc, "search_ms_mean": round(ms / nsrc, 3),
+           "gteps": round(ec / 2 / (ms / 1e3) / 1e9, 2),
+           "levels": [int(x.levels) for x in sts]}
+    del out, g
+    torch.cuda.empty_cache()
+    return res
+
+
 def many_graphs_workload(gen, count: int = 512):
     """The fused-launch configuration: `count` Erdos-Renyi graphs, n
     log-uniform in [2^8, 2^16], 4n sampled pairs each (average degree 8 once
@@ -904,6 +939,9 @@ def main():
         log("batched done")
         extra["primitives"] = measure_primitives(torch)
         log("primitives done")
+        if not args.no_large:
+            extra["graph500"] = {f"scale{sc}": measure_rmat_large(torch, sc) for sc in (26, 27)}
+            log(f"large RMAT done: {extra['graph500']}")
     if rank == 0 and world == 1 and not args.no_serving and not args.no_extra:
         extra["serving"] = measure_serving(torch)
 

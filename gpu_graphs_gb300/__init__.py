@@ -135,6 +135,12 @@ class Graph:
         check(fn(self._h, C.c_void_p(row.ctypes.data), C.c_void_p(col.ctypes.data)), "gbfs_graph_get_csr")
         return row, col[: self.m]
 
+    def row_offsets(self) -> np.ndarray:
+        """The n + 1 row offsets alone, as int64."""
+        row = np.empty(self.n + 1, np.int64)
+        check(lib.gbfs_graph_get_csr64(self._h, C.c_void_p(row.ctypes.data), None), "gbfs_graph_get_csr64")
+        return row
+
     # ---- parameters ----
     @property
     def params(self) -> Params:

@@ -96,7 +96,7 @@ extern "C" const char *gbfs_strerror(int status)
     case GBFS_ERR_OOM: return "out of memory";
     case GBFS_ERR_CUDA: return "CUDA error";
     case GBFS_ERR_TIMEOUT: return "device-side wait timed out";
-    case GBFS_ERR_TOO_LARGE: return "graph too large for int32 CSR";
+    case GBFS_ERR_TOO_LARGE: return "graph too large for this path (size limit, or 64-bit row offsets)";
     case GBFS_ERR_IO: return "file missing or malformed";
     case GBFS_ERR_BUDGET: return "memory budget exceeded";
     case GBFS_ERR_NOT_FOUND: return "unknown graph id or ticket";
@@ -304,7 +304,7 @@ extern "C" int gbfs_graph_get_csr(const gbfs_graph *g, int32_t *row_offset, int3
 
 extern "C" int gbfs_graph_get_csr64(const gbfs_graph *g, int64_t *row_offset, int32_t *col_idx)
 {
-    if (!g || !row_offset || (g->csr.m > 0 && !col_idx)) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
+    if (!g || !row_offset) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
     gbfs_graph *gg = const_cast<gbfs_graph *>(g);
     std::lock_guard<std::mutex> lk(gg->mu);
     const size_t nr = (size_t)g->csr.n + 1;
@@ -326,7 +326,7 @@ extern "C" int gbfs_graph_get_csr64(const gbfs_graph *g, int64_t *row_offset, in
                            dev_row ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost);
         }
     }
-    if (e == cudaSuccess && g->csr.m > 0)
+    if (e == cudaSuccess && g->csr.m > 0 && col_idx)
         e = cudaMemcpyAsync(col_idx, g->csr.col, sizeof(int) * (size_t)g->csr.m, kc, g->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
     if (e != cudaSuccess) return cuda_fail(e, "CSR download");

@@ -42,7 +42,7 @@ extern "C" {
 #define GBFS_ERR_OOM          -2  /* device or host allocation failed       */
 #define GBFS_ERR_CUDA         -3  /* a CUDA runtime call failed / no device */
 #define GBFS_ERR_TIMEOUT      -4  /* a bounded device-side wait ran out     */
-#define GBFS_ERR_TOO_LARGE    -5  /* graph exceeds the int32 CSR limits     */
+#define GBFS_ERR_TOO_LARGE    -5  /* size limit, or a path without 64-bit rows */
 #define GBFS_ERR_IO           -6  /* file missing or malformed              */
 #define GBFS_ERR_BUDGET       -7  /* serving: memory budget refuses it      */
 #define GBFS_ERR_NOT_FOUND    -8  /* serving: unknown graph id or ticket    */
@@ -120,7 +120,8 @@ int gbfs_graph_get_info(const gbfs_graph *g, gbfs_graph_info *info);
  * GBFS_ERR_TOO_LARGE for a wide graph (64-bit row offsets). */
 int gbfs_graph_get_csr(const gbfs_graph *g, int32_t *row_offset,
                        int32_t *col_idx);
-/* The same with 64-bit row offsets, for any graph. */
+/* The same with 64-bit row offsets, for any graph; col_idx may be NULL
+ * (the offsets alone). */
 int gbfs_graph_get_csr64(const gbfs_graph *g, int64_t *row_offset,
                          int32_t *col_idx);
 

@@ -53,6 +53,11 @@ public:
         check(rc, "gbfs_graph_from_edges");
         gbfs_graph_info info;
         check(gbfs_graph_get_info(graph, &info), "gbfs_graph_get_info");
+        if (info.wide) {  // the reference's int members cannot hold it: use the C ABI (gbfs_graph_get_csr64)
+            gbfs_graph_destroy(graph);
+            graph = nullptr;
+            throw error(GBFS_ERR_TOO_LARGE, "csr: more than 2^31-1 edges");
+        }
         num_edges = (int)info.m;
         row_offset = (int *)malloc(sizeof(int) * ((size_t)num_nodes + 1));
         col_idx = (int *)malloc(sizeof(int) * (size_t)(num_edges > 0 ? num_edges : 1));

@@ -37,6 +37,7 @@ def test_wide_csr_equals_narrow(gb):
         col = np.empty(max(g64.m, 1), np.int32)
         rc = gb._lib.lib.gbfs_graph_get_csr(g64.handle, row.ctypes.data, col.ctypes.data)
         assert rc == gb._lib.ERR_TOO_LARGE
+        assert np.array_equal(g64.row_offsets(), r64) and np.array_equal(g32.row_offsets(), r64)
 
 
 @pytest.mark.parametrize("direction", [0, 1, 2])
