@@ -678,7 +678,8 @@ int finalize(DeviceCsr &out, cudaStream_t st, std::string &err)
 
 // Sort every row of (row, col) in place (no dedup).  Scratch is allocated
 // and freed here.  Synchronises st.
-int sort_rows_inplace(const int *row, int *col, int32_t n, int64_t m, cudaStream_t st, std::string &err)
+template <typename RT>
+int sort_rows_inplace(const RT *row, int *col, int32_t n, int64_t m, cudaStream_t st, std::string &err)
 {
     int rc = GBFS_OK;
     int *ucnt = nullptr, *med = nullptr, *large = nullptr, *tmp2 = nullptr, *w4 = nullptr, *w16 = nullptr;
@@ -693,18 +694,18 @@ int sort_rows_inplace(const int *row, int *col, int32_t n, int64_t m, cudaStream
     CK(cudaMalloc(&lcnt, 16));
     CK(cudaMalloc(&tmp2, sizeof(int) * (size_t)std::max<int64_t>(m, 1)));
     CK(cudaMemsetAsync(lcnt, 0, 16, st));
-    k_bin<int><<<grid_for(n, BIN_THREADS, 152 * 4), BIN_THREADS, 0, st>>>(row, n, med, large, w4, w16, lcnt);
+    k_bin<RT><<<grid_for(n, BIN_THREADS, 152 * 4), BIN_THREADS, 0, st>>>(row, n, med, large, w4, w16, lcnt);
     CK(cudaGetLastError());
-    k_sort_small<int><<<grid_for((int64_t)n * 32, thr), thr, 0, st>>>(row, n, col, 0, ucnt);
+    k_sort_small<RT><<<grid_for((int64_t)n * 32, thr), thr, 0, st>>>(row, n, col, 0, ucnt);
     CK(cudaGetLastError());
-    k_sort_warp<4, int><<<152 * 8, 256, 0, st>>>(row, w4, lcnt + 2, col, 0, ucnt);
+    k_sort_warp<4, RT><<<152 * 8, 256, 0, st>>>(row, w4, lcnt + 2, col, 0, ucnt);
     CK(cudaGetLastError());
-    k_sort_warp<16, int><<<152 * 8, 256, 0, st>>>(row, w16, lcnt + 3, col, 0, ucnt);
+    k_sort_warp<16, RT><<<152 * 8, 256, 0, st>>>(row, w16, lcnt + 3, col, 0, ucnt);
     CK(cudaGetLastError());
-    k_sort_medium<int><<<152 * 4, MED_THREADS, 0, st>>>(row, med, lcnt, col, 0, ucnt);
+    k_sort_medium<RT><<<152 * 4, MED_THREADS, 0, st>>>(row, med, lcnt, col, 0, ucnt);
     CK(cudaGetLastError());
     while (key_bits < 31 && (1LL << key_bits) < (int64_t)n) key_bits++;
-    k_sort_large<int><<<152 * 2, LARGE_THREADS, 0, st>>>(row, large, lcnt, col, tmp2, key_bits, 0, ucnt);
+    k_sort_large<RT><<<152 * 2, LARGE_THREADS, 0, st>>>(row, large, lcnt, col, tmp2, key_bits, 0, ucnt);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
 done:
@@ -735,15 +736,11 @@ int csr_check_symmetric(const DeviceCsr &c, cudaStream_t st, bool &sym, std::str
     CK(cudaStreamSynchronize(st));
     {
         const int *col = c.col;
-        if (h[0] && c.wide) {  // wide rows come sorted from the edge-list build
-            err = "unsorted rows of a wide graph";
-            rc = GBFS_ERR_TOO_LARGE;
-            goto done;
-        }
-        if (h[0]) {  // unsorted rows: check a sorted copy
+        if (h[0]) {  // unsorted rows (hub-first ones, for instance): check a sorted copy
             CK(cudaMalloc(&copy, sizeof(int) * (size_t)std::max<int64_t>(c.m, 1)));
             CK(cudaMemcpyAsync(copy, c.col, sizeof(int) * (size_t)c.m, cudaMemcpyDeviceToDevice, st));
-            rc = sort_rows_inplace(c.row, copy, c.n, c.m, st, err);
+            rc = c.wide ? sort_rows_inplace((const long long *)c.row64, copy, c.n, c.m, st, err)
+                        : sort_rows_inplace((const int *)c.row, copy, c.n, c.m, st, err);
             if (rc) goto done;
             col = copy;
         }
