@@ -58,6 +58,10 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
+# The server runs its slots' searches on up to 24 streams at once; CUDA's
+# default of 8 hardware work queues per process lets only about four of
+# them progress together (set before the first CUDA call of the process).
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 RMAT = dict(edge_factor=16, a=0.57, b=0.19, c=0.19, seed=1)
 SOURCE_SEED = 1
@@ -693,7 +697,8 @@ def measure_primitives(torch) -> dict:
     return res
 
 
-def measure_serving(torch, seconds: float = 2.0, fractions=(0.25, 0.5, 0.75, 1.0), max_queries: int = 3000) -> dict:
+def measure_serving(torch, seconds: float = 2.0, fractions=(0.25, 0.5, 0.75, 1.0), max_queries: int = 3000,
+                    num_slots: int = 6) -> dict:
     """32 resident graphs, Poisson arrivals at fractions of the measured capacity."""
     import gpu_graphs_gb300 as gb
     rng = np.random.default_rng(5)
@@ -727,7 +732,7 @@ def measure_serving(torch, seconds: float = 2.0, fractions=(0.25, 0.5, 0.75, 1.0
         g.set_params(direction=0)
     out = {"workload": "32 resident graphs: 16 RMAT scale U{12..22} ef 16, 16 grids side U[64, 4096]; "
                        "queries pick a graph uniformly and a source uniformly among degree>0 vertices; "
-                       "4 slots, batch window max(0.5 ms, 10% of the graph's recent launch time); "
+                       f"{num_slots} slots, batch window max(0.5 ms, 10% of the graph's recent launch time); "
                        "grids (degree <= 16) served as up to 4 concurrent single-source searches per slot; "
                        "results copied into pinned host buffers",
            "plain_one_query_per_launch": {"queries_per_s": round(len(plain_ms) / (sum(plain_ms) / 1e3), 1),
@@ -755,7 +760,7 @@ def measure_serving(torch, seconds: float = 2.0, fractions=(0.25, 0.5, 0.75, 1.0
     pinned = [[torch.empty(g.n, dtype=torch.int32, pin_memory=True) for _ in range(8)] for g in graphs]
     pools = [[t.numpy() for t in ts] for ts in pinned]
     counters = [0] * 32
-    cfg = dict(mem_budget_bytes=150 << 30, num_slots=4, max_lanes=64, batch_window_us=500, window_pct=10)
+    cfg = dict(mem_budget_bytes=150 << 30, num_slots=num_slots, max_lanes=64, batch_window_us=500, window_pct=10)
 
     def submitter(srv, gids):
         def submit():

@@ -15,10 +15,16 @@ Two layers:
 from __future__ import annotations
 
 import ctypes as C
+import os
 import sys
 from typing import Iterable, Sequence
 
 import numpy as np
+
+# The server runs its slots' searches on many streams at once; CUDA's
+# default of 8 hardware work queues per process serialises most of them.
+# Effective only when this import comes before the process's first CUDA call.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 from . import _lib
 from ._lib import (DEDUP, DIR_BOTTOMUP, DIR_OPTIMIZING, DIR_TOPDOWN, DROP_SELF_LOOPS, HUB_FIRST, SYMMETRIZE,

@@ -73,10 +73,14 @@ struct SrvGraph {
 };
 
 // Single-source searches a slot runs at once on a graph of small degree.
-// Four slots on a 4000 x 4000 grid, 64 queries at once: 224 ms with four
-// searches per slot, 283 ms with two slots of four; batching a graph's
-// queries into multi-source launches from 16 pending on instead cut the
-// serving mix's capacity from 1,377 to 1,249 queries/s.
+// A 4000 x 4000 grid search takes 12.7 ms on the whole GPU and 18.8 ms
+// capped to 19 CTAs; 16 such searches at once finish in 21.5 ms each (677
+// queries/s against 76 one after another), given enough hardware work
+// queues (CUDA_DEVICE_MAX_CONNECTIONS: with CUDA's default of 8, about four
+// searches progress at a time).  On the 32-graph serving mix, 6 slots of 4
+// searches: capacity 3,358 queries/s (4 slots 2,713, 8 slots 2,999; 8
+// searches per slot 2,816); batching such a graph's queries into
+// multi-source launches from 16 pending on was slower.
 #ifndef SRV_SUB_DEF
 #define SRV_SUB_DEF 4
 #endif

@@ -386,7 +386,10 @@ int64_t gbfs_gen_grid_capacity(int32_t side, double extra);
  * out-degree <= 16 (meshes, grids, road networks: long searches of small
  * frontiers) a slot instead runs up to 4 of its queries at once as
  * single-source searches on its own streams, each with a share of the
- * slot's CTAs (batch_lanes then counts the searches run together). */
+ * slot's CTAs (batch_lanes then counts the searches run together).
+ * These run concurrently only with enough hardware work queues: start the
+ * process with CUDA_DEVICE_MAX_CONNECTIONS of at least 4 * num_slots + 2
+ * (CUDA's default of 8 lets about four searches progress at a time). */
 typedef struct gbfs_server gbfs_server;
 
 typedef struct gbfs_server_config {

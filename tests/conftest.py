@@ -1,8 +1,13 @@
 """Shared test setup: repo root on sys.path, the `gpu` marker, golden data."""
 from __future__ import annotations
 
+import os
 import sys
 from pathlib import Path
+
+# the server's concurrent searches need more than CUDA's default 8 hardware
+# work queues; set before any test makes the first CUDA call
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 import numpy as np
 import pytest
