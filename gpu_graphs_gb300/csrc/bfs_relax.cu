@@ -51,7 +51,6 @@ namespace {
 constexpr int RX_BLOCK = 512;
 constexpr int RX_NW = RX_BLOCK / 32;
 constexpr int RX_CAP = 1024;                 // entries of a CTA's local frontier (two held)
-constexpr int RX_PER_T = RX_CAP / RX_BLOCK;  // entries per thread in the degree scan
 // Edges per thread in flight: local frontiers of up to 64 entries (a few
 // hundred edges per CTA), and larger ones (searches capped to a few CTAs,
 // e.g. the server's concurrent searches: 64 queries on a 4000 x 4000 grid,
@@ -73,9 +72,6 @@ __global__ void __launch_bounds__(RX_BLOCK, 2) k_bfs_relax(BfsArgs a)
     const RT *const row = Sel::row(a);
     __shared__ int s_v[2][RX_CAP];
     __shared__ B s_b[2][RX_CAP];              // row bounds beside s_v
-    __shared__ int s_pre[RX_CAP];             // exclusive prefix of the entries' out-degrees
-    __shared__ int s_wsum[RX_NW];
-    __shared__ int s_tot;
     __shared__ unsigned s_cnt[3];
     __shared__ unsigned long long s_cd;
     __shared__ unsigned long long s_red[2][RX_NW];
@@ -239,57 +235,46 @@ __global__ void __launch_bounds__(RX_BLOCK, 2) k_bfs_relax(BfsArgs a)
                 }
                 return;
             }
-            // a larger frontier: a CTA-wide exclusive scan of the out-degrees
-            int dl[RX_PER_T];
-            int dsum = 0;
+            {
+                // a larger frontier: warp w expands its own slice of at most
+                // 64 entries, [w C, (w + 1) C), two per lane, with a warp scan
+                // and shuffles, RX_ILP_BIG edges per lane in flight (no CTA
+                // barrier; grid-like rows have similar degrees).  Against one
+                // CTA-wide scan of the whole frontier: a 4000 x 4000 grid
+                // search capped to 12 CTAs 22.0 -> 19.3 ms, 16 concurrent
+                // searches of 19 CTAs 662 -> 726 queries/s
+                const int C = (nc + RX_NW - 1) / RX_NW;
+                const int base = (int)warp * C;
+                const int cnt = max(0, min(C, nc - base));
+                const int j0 = 2 * (int)lane, j1 = j0 + 1;
+                const B b0 = j0 < cnt ? s_b[cur][base + j0] : Sel::mk(0, 0);
+                const B b1 = j1 < cnt ? s_b[cur][base + j1] : Sel::mk(0, 0);
+                const int d0 = (int)(b0.y - b0.x), d1 = (int)(b1.y - b1.x);
+                const int incl = warp_incl_scan(d0 + d1);
+                const int ex0 = incl - d0 - d1, ex1 = ex0 + d0;
+                const int Ew = __shfl_sync(FULL, incl, 31);
+                for (int e0 = 0; e0 < Ew; e0 += 32 * RX_ILP_BIG) {
+                    int w[RX_ILP_BIG], u[RX_ILP_BIG];
 #pragma unroll
-            for (int k = 0; k < RX_PER_T; k++) {
-                const int i = (int)t * RX_PER_T + k;
-                dl[k] = 0;
-                if (i < nc) {
-                    const B be = s_b[cur][i];
-                    dl[k] = (int)(be.y - be.x);
-                }
-                dsum += dl[k];
-            }
-            const int incl = warp_incl_scan(dsum);
-            if (lane == 31) s_wsum[warp] = incl;
-            __syncthreads();
-            if (warp == 0) {
-                const int x = lane < RX_NW ? s_wsum[lane] : 0;
-                const int xi = warp_incl_scan(x);
-                if (lane < RX_NW) s_wsum[lane] = xi - x;
-                if (lane == 31) s_tot = xi;
-            }
-            __syncthreads();
-            int run = s_wsum[warp] + incl - dsum;
+                    for (int q = 0; q < RX_ILP_BIG; q++) {
+                        const int e = e0 + q * 32 + (int)lane;
+                        int l = 0;
 #pragma unroll
-            for (int k = 0; k < RX_PER_T; k++) {
-                const int i = (int)t * RX_PER_T + k;
-                if (i < nc) s_pre[i] = run;
-                run += dl[k];
-            }
-            __syncthreads();
-            const int E = s_tot;
-            for (int e0 = 0; e0 < E; e0 += RX_BLOCK * RX_ILP_BIG) {
-                if (e0 + (int)(warp * 32) >= E) break;  // no edge left for this warp
-                int w[RX_ILP_BIG], u[RX_ILP_BIG];
-#pragma unroll
-                for (int q = 0; q < RX_ILP_BIG; q++) {
-                    const int e = e0 + q * RX_BLOCK + (int)t;
-                    w[q] = -1;
-                    u[q] = 0;
-                    if (e < E) {
-                        // the entry holding edge e: the last i with s_pre[i] <= e
-                        int i = 0;
-#pragma unroll
-                        for (int st = RX_CAP / 2; st > 0; st >>= 1)
-                            if (i + st < nc && s_pre[i + st] <= e) i += st;
-                        w[q] = __ldg(a.col + s_b[cur][i].x + (e - s_pre[i]));
-                        u[q] = s_v[cur][i];
+                        for (int st = 16; st > 0; st >>= 1)
+                            if (__shfl_sync(FULL, ex0, l + st) <= e) l += st;
+                        const int x0 = __shfl_sync(FULL, ex0, l), x1 = __shfl_sync(FULL, ex1, l);
+                        const RT bx0 = __shfl_sync(FULL, b0.x, l), bx1 = __shfl_sync(FULL, b1.x, l);
+                        w[q] = -1;
+                        u[q] = 0;
+                        if (e < Ew) {
+                            const bool second = e >= x1;
+                            w[q] = __ldg(a.col + (second ? bx1 + (e - x1) : bx0 + (e - x0)));
+                            u[q] = s_v[cur][base + 2 * l + (second ? 1 : 0)];
+                        }
                     }
+                    relax(std::integral_constant<int, RX_ILP_BIG>{}, w, u, last, nb, cnt_nb);
                 }
-                relax(std::integral_constant<int, RX_ILP_BIG>{}, w, u, last, nb, cnt_nb);
+                return;
             }
         };
 
