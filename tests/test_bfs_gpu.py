@@ -494,3 +494,57 @@ def test_relaxed_phase_shapes(gb, orc):
             assert st.edges_in_component == orc.component_edges(o, want), (name, s0)
             assert st.levels == int(want.max()) + 1, (name, s0)
             assert st.launches == 2
+
+
+def _random_small_degree_graph(kind: str, n: int, rng):
+    """Seeded graphs whose out-degree stays at most 16 (the label-correcting
+    phase's domain): shuffled binary trees, paths with short and long chords,
+    unions of random perfect matchings, and grids with random holes."""
+    perm = rng.permutation(n).astype(np.int32)
+    if kind == "tree":
+        i = np.arange(1, n)
+        src, dst = perm[i], perm[(i - 1) // 2]
+    elif kind == "chords":
+        i = np.arange(n - 1)
+        c = rng.integers(0, n - 40, n // 50)
+        far = rng.integers(0, n, n // 2000)
+        src = np.concatenate([perm[i], perm[c], perm[far]])
+        dst = np.concatenate([perm[i + 1], perm[c + rng.integers(2, 40, c.size)], perm[rng.integers(0, n, far.size)]])
+    elif kind == "matchings":
+        m = n - n % 2
+        parts = [rng.permutation(m) for _ in range(3)]
+        src = np.concatenate([p[0::2] for p in parts]).astype(np.int32)
+        dst = np.concatenate([p[1::2] for p in parts]).astype(np.int32)
+    else:  # holes
+        side = int(np.sqrt(n))
+        n = side * side
+        v = np.arange(n).reshape(side, side)
+        keep = rng.random((side, side)) > 0.15
+        h = (keep[:, :-1] & keep[:, 1:])
+        w = (keep[:-1, :] & keep[1:, :])
+        src = np.concatenate([v[:, :-1][h], v[:-1, :][w]])
+        dst = np.concatenate([v[:, 1:][h], v[1:, :][w]])
+    return n, np.ascontiguousarray(src, np.int32), np.ascontiguousarray(dst, np.int32)
+
+
+@pytest.mark.parametrize("wide", [False, True])
+def test_relaxed_phase_random_sweep(gb, orc, wide):
+    """Twenty seeded graphs of four small-degree families, five sources each
+    (the hops, overflowing local frontiers and racing pieces of the
+    label-correcting phase at random), int32 and int64 row offsets: levels
+    and counts against the oracle."""
+    rng = np.random.default_rng(2024)
+    for t in range(20):
+        kind = ("tree", "chords", "matchings", "holes")[t % 4]
+        n, src, dst = _random_small_degree_graph(kind, int(rng.integers(20_000, 200_000)), rng)
+        g = gb.Graph.from_edges(n, src, dst, gb.UNDIRECTED | (gb.WIDE_ROWS if wide else 0))
+        assert g.max_degree <= 16 and g.wide == wide
+        o = orc.csr_build(n, src, dst, orc.UNDIRECTED)
+        deg = np.diff(g.row_offsets())
+        for s0 in rng.choice(np.flatnonzero(deg > 0), 5, replace=False):
+            got, st = g.bfs(int(s0), stats=True)
+            want = orc.bfs_queue(o, int(s0))
+            assert np.array_equal(got, want), (kind, t, int(s0))
+            assert st.vertices_reached == int((want >= 0).sum())
+            assert st.edges_in_component == orc.component_edges(o, want)
+            assert st.levels == int(want.max()) + 1
