@@ -203,31 +203,42 @@ __device__ __forceinline__ int warp_bitonic_sort(int x)
     return x;
 }
 
-// One warp per row of length <= 32: sort in registers, pack distinct values.
+// Rows of length <= 32, one warp per row: sort in registers, pack distinct
+// values.  A warp loads the offsets of 32 consecutive rows at once, then
+// sorts those of them that are short, one after another.
 template <typename RT>
 __global__ void k_sort_small(const RT *__restrict__ row, int n, int *tmp, int dedup, int *ucnt)
 {
     const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const unsigned lane = lane_id();
-    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
-        const RT b = row[r];
-        const int d = (int)(row[r + 1] - b);
-        if (d > 32) continue;
-        if (d <= 1) {
-            if (lane == 0) ucnt[r] = d;
-            continue;
+    for (int64_t r0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; r0 < n; r0 += warps * 32) {
+        RT bl = 0;
+        int dl = 33;  // rows past n are skipped as long ones
+        if (r0 + lane < n) {
+            bl = row[r0 + lane];
+            dl = (int)(row[r0 + lane + 1] - bl);
         }
-        int x = (int)lane < d ? tmp[b + lane] : INT_MAX;
-        x = warp_bitonic_sort(x);
-        if (dedup) {
-            int prev = __shfl_up_sync(FULL, x, 1);
-            bool uniq = (int)lane < d && (lane == 0 || x != prev);
-            unsigned mask = __ballot_sync(FULL, uniq);
-            if (uniq) tmp[b + __popc(mask & lanemask_lt())] = x;
-            if (lane == 0) ucnt[r] = __popc(mask);
-        } else {
-            if ((int)lane < d) tmp[b + lane] = x;
-            if (lane == 0) ucnt[r] = d;
+        for (int j = 0; j < 32; j++) {
+            const int64_t r = r0 + j;
+            const RT b = __shfl_sync(FULL, bl, j);
+            const int d = __shfl_sync(FULL, dl, j);
+            if (d > 32) continue;
+            if (d <= 1) {
+                if (lane == 0) ucnt[r] = d;
+                continue;
+            }
+            int x = (int)lane < d ? tmp[b + lane] : INT_MAX;
+            x = warp_bitonic_sort(x);
+            if (dedup) {
+                int prev = __shfl_up_sync(FULL, x, 1);
+                bool uniq = (int)lane < d && (lane == 0 || x != prev);
+                unsigned mask = __ballot_sync(FULL, uniq);
+                if (uniq) tmp[b + __popc(mask & lanemask_lt())] = x;
+                if (lane == 0) ucnt[r] = __popc(mask);
+            } else {
+                if ((int)lane < d) tmp[b + lane] = x;
+                if (lane == 0) ucnt[r] = d;
+            }
         }
     }
 }
@@ -447,16 +458,30 @@ k_sort_large(const RT *__restrict__ row, const int *__restrict__ list, const uns
     }
 }
 
-// One warp per row: copy the packed distinct prefix of each row.
+// Copy the packed distinct prefix of each row.  A warp loads the offsets
+// of 32 consecutive rows at once (one coalesced load per array instead of
+// a dependent pair per row), then copies the 32 rows one after another.
 template <typename RT>
 __global__ void k_compact(const RT *__restrict__ row, const RT *__restrict__ row2, int n,
                           const int *__restrict__ tmp, int *col)
 {
     const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += warps) {
-        const RT b = row[r], o = row2[r];
-        const int c = (int)(row2[r + 1] - o);
-        for (int i = lane_id(); i < c; i += 32) col[o + i] = tmp[b + i];
+    const int lane = (int)lane_id();
+    for (int64_t r0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; r0 < n; r0 += warps * 32) {
+        const int64_t r = r0 + lane;
+        RT b = 0, o = 0;
+        int c = 0;
+        if (r < n) {
+            b = row[r];
+            o = row2[r];
+            c = (int)(row2[r + 1] - o);
+        }
+#pragma unroll 4
+        for (int j = 0; j < 32; j++) {
+            const RT bj = __shfl_sync(FULL, b, j), oj = __shfl_sync(FULL, o, j);
+            const int cj = __shfl_sync(FULL, c, j);
+            for (int i = lane; i < cj; i += 32) col[oj + i] = tmp[bj + i];
+        }
     }
 }
 
