@@ -471,7 +471,8 @@ __global__ void k_compact(const RT *__restrict__ row, const RT *__restrict__ row
         const int64_t r = r0 + lane;
         RT b = 0, o = 0;
         int c = 0;
-        if (r < n) {
+        // rows longer than MED_MAX before deduplication: k_compact_long
+        if (r < n && row[r + 1] - row[r] <= MED_MAX) {
             b = row[r];
             o = row2[r];
             c = (int)(row2[r + 1] - o);
@@ -482,6 +483,23 @@ __global__ void k_compact(const RT *__restrict__ row, const RT *__restrict__ row
             const int cj = __shfl_sync(FULL, c, j);
             for (int i = lane; i < cj; i += 32) col[oj + i] = tmp[bj + i];
         }
+    }
+}
+
+// The rows of list[0, cnt[1]) (longer than MED_MAX before deduplication),
+// one CTA per row: a long hub row copied by one warp would set the whole
+// pass's time.
+template <typename RT>
+__global__ void k_compact_long(const RT *__restrict__ row, const RT *__restrict__ row2, const int *__restrict__ list,
+                               const unsigned *cnt, const int *__restrict__ tmp, int *col)
+{
+    const int count = (int)cnt[1];
+    for (int li = blockIdx.x; li < count; li += gridDim.x) {
+        const int r = list[li];
+        const RT b = row[r], o = row2[r];
+        const int c = (int)(row2[r + 1] - o);
+#pragma unroll 4
+        for (int i = threadIdx.x; i < c; i += blockDim.x) col[o + i] = tmp[b + i];
     }
 }
 
@@ -620,14 +638,40 @@ __global__ void k_hub_first_warp(const RT *__restrict__ row, int n, int *col)
     }
 }
 
+// Rows of HUB_GIANT_ROW entries or more: the whole grid splits each one.
+constexpr int HUB_GIANT_ROW = 65536;
+
+// Appends the rows of length in [lo, hi) to list (count in *cnt).
 template <typename RT>
-__global__ void k_hub_first_cta(const RT *__restrict__ row, int n, int *col)
+__global__ void k_rows_by_len(const RT *__restrict__ row, int n, int lo, int hi, int *list, unsigned *cnt)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
+        const int64_t r = base + lane_id();
+        bool in = false;
+        if (r < n) {
+            const int64_t d = (int64_t)(row[r + 1] - row[r]);
+            in = d >= lo && d < hi;
+        }
+        const unsigned m = __ballot_sync(FULL, in);
+        if (!m) continue;
+        unsigned pos = 0;
+        if (lane_id() == 0) pos = atomicAdd(cnt, (unsigned)__popc(m));
+        pos = __shfl_sync(FULL, pos, 0);
+        if (in) list[pos + __popc(m & lanemask_lt())] = (int)r;
+    }
+}
+
+// One CTA per listed row (list[0, *cnt)).
+template <typename RT>
+__global__ void k_hub_first_cta(const RT *__restrict__ row, const int *__restrict__ list, const unsigned *cnt, int *col)
 {
     __shared__ unsigned long long s_best[32];
-    for (int64_t r = blockIdx.x; r < n; r += gridDim.x) {
+    const int count = (int)*cnt;
+    for (int li = blockIdx.x; li < count; li += gridDim.x) {
+        const int r = list[li];
         const RT b = row[r];
         const int d = (int)(row[r + 1] - b);
-        if (d < HUB_CTA_ROW) continue;
         unsigned long long best = 0;
         for (int i = threadIdx.x; i < d; i += blockDim.x) {
             const unsigned long long k = hub_key(row, col[b + i], i);
@@ -650,6 +694,50 @@ __global__ void k_hub_first_cta(const RT *__restrict__ row, int n, int *col)
             }
         }
         __syncthreads();
+    }
+}
+
+// The listed giant rows one after another, each split over the whole grid:
+// every warp folds its entries' keys and takes the row's maximum with one
+// atomicMax (best[g], zeroed by the caller); k_hub_giant_swap then moves it.
+template <typename RT>
+__global__ void k_hub_giant_max(const RT *__restrict__ row, const int *__restrict__ list, const unsigned *cnt,
+                                const int *__restrict__ col, unsigned long long *best)
+{
+    const int count = (int)*cnt;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int g = 0; g < count; g++) {
+        const int r = list[g];
+        const RT b = row[r];
+        const int d = (int)(row[r + 1] - b);
+        unsigned long long mine = 0;
+        for (int64_t i = tid; i < d; i += stride) {
+            const unsigned long long k = hub_key(row, col[b + i], (int)i);
+            mine = k > mine ? k : mine;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long y = __shfl_xor_sync(FULL, mine, o);
+            mine = y > mine ? y : mine;
+        }
+        if (lane_id() == 0 && mine) atomicMax(best + g, mine);
+    }
+}
+
+template <typename RT>
+__global__ void k_hub_giant_swap(const RT *__restrict__ row, const int *__restrict__ list, const unsigned *cnt,
+                                 const unsigned long long *best, int *col)
+{
+    const int count = (int)*cnt;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < count; g += gridDim.x * blockDim.x) {
+        const RT b = row[list[g]];
+        const int pos = 0x7fffffff - (int)(best[g] & 0xffffffffu);
+        if (best[g] && pos > 0) {
+            const int t = col[b];
+            col[b] = col[b + pos];
+            col[b + pos] = t;
+        }
     }
 }
 
@@ -744,6 +832,52 @@ done:
     return rc;
 }
 
+// Hub-first order for every row of (row, col), m entries: one warp per row
+// below HUB_CTA_ROW entries, one CTA per listed row up to HUB_GIANT_ROW,
+// the whole grid per longer row (the few longest rows of a power-law
+// graph would otherwise each hold one CTA for most of the pass).
+// Synchronises st.
+template <typename RT>
+int hub_first_rows(const RT *row, int n, int64_t m, int *col, cudaStream_t st, std::string &err)
+{
+    int rc = GBFS_OK;
+    int *lists = nullptr;
+    unsigned *cnts = nullptr;
+    unsigned long long *best = nullptr;
+    unsigned h[2] = {0, 0};
+    const int64_t cap_long = std::min<int64_t>(n, m / HUB_CTA_ROW + 1);
+    const int64_t cap_giant = std::min<int64_t>(n, m / HUB_GIANT_ROW + 1);
+    CK(cudaMalloc(&lists, sizeof(int) * (size_t)(cap_long + cap_giant)));
+    CK(cudaMalloc(&cnts, 2 * sizeof(unsigned)));
+    CK(cudaMemsetAsync(cnts, 0, 2 * sizeof(unsigned), st));
+    k_hub_first_warp<RT><<<grid_for((int64_t)n * 32, 256), 256, 0, st>>>(row, n, col);
+    CK(cudaGetLastError());
+    k_rows_by_len<RT><<<grid_for(n, 256), 256, 0, st>>>(row, n, HUB_CTA_ROW, HUB_GIANT_ROW, lists, cnts);
+    CK(cudaGetLastError());
+    k_rows_by_len<RT><<<grid_for(n, 256), 256, 0, st>>>(row, n, HUB_GIANT_ROW, INT_MAX, lists + cap_long, cnts + 1);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(h, cnts, sizeof(h), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (h[0]) {
+        k_hub_first_cta<RT><<<152 * 2, 512, 0, st>>>(row, lists, cnts, col);
+        CK(cudaGetLastError());
+    }
+    if (h[1]) {
+        CK(cudaMalloc(&best, sizeof(unsigned long long) * h[1]));
+        CK(cudaMemsetAsync(best, 0, sizeof(unsigned long long) * h[1], st));
+        k_hub_giant_max<RT><<<152 * 4, 512, 0, st>>>(row, lists + cap_long, cnts + 1, col, best);
+        CK(cudaGetLastError());
+        k_hub_giant_swap<RT><<<1, 256, 0, st>>>(row, lists + cap_long, cnts + 1, best, col);
+        CK(cudaGetLastError());
+    }
+    CK(cudaStreamSynchronize(st));
+done:
+    if (lists) cudaFree(lists);
+    if (cnts) cudaFree(cnts);
+    if (best) cudaFree(best);
+    return rc;
+}
+
 }  // namespace
 
 int csr_check_symmetric(const DeviceCsr &c, cudaStream_t st, bool &sym, std::string &err)
@@ -785,17 +919,9 @@ done:
 int csr_hub_first(DeviceCsr &c, cudaStream_t st, std::string &err)
 {
     int rc = GBFS_OK;
-    if (c.wide) {
-        k_hub_first_warp<<<grid_for((int64_t)c.n * 32, 256), 256, 0, st>>>((const long long *)c.row64, c.n, c.col);
-        CK(cudaGetLastError());
-        k_hub_first_cta<<<152 * 2, 512, 0, st>>>((const long long *)c.row64, c.n, c.col);
-    } else {
-        k_hub_first_warp<<<grid_for((int64_t)c.n * 32, 256), 256, 0, st>>>((const int *)c.row, c.n, c.col);
-        CK(cudaGetLastError());
-        k_hub_first_cta<<<152 * 2, 512, 0, st>>>((const int *)c.row, c.n, c.col);
-    }
-    CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(st));
+    rc = c.wide ? hub_first_rows((const long long *)c.row64, c.n, c.m, c.col, st, err)
+                : hub_first_rows((const int *)c.row, c.n, c.m, c.col, st, err);
+    if (rc) goto done;
     c.hub_rows = true;
 done:
     return rc;
@@ -873,10 +999,8 @@ int csr_build_transpose(DeviceCsr &c, cudaStream_t st, std::string &err)
     CK(cudaGetLastError());
     // in-rows hub-first (the in-neighbour of highest in-degree, the likeliest
     // to be reached early, is probed first), then their first entries
-    k_hub_first_warp<<<grid_for((int64_t)n * 32, 256), 256, 0, st>>>((const int *)trow, n, tcol);
-    CK(cudaGetLastError());
-    k_hub_first_cta<<<152 * 2, 512, 0, st>>>((const int *)trow, n, tcol);
-    CK(cudaGetLastError());
+    rc = hub_first_rows((const int *)trow, n, m, tcol, st, err);
+    if (rc) goto done;
     k_first<<<grid_for(n, 256), 256, 0, st>>>((const int *)trow, (const int *)tcol, n, tfirst, (int *)nullptr);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(&h_nheavy, d_nheavy, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
@@ -1030,6 +1154,8 @@ int build_rows(int32_t n, int64_t m, int64_t md, const int *d_src, const int *d_
         tmp2 = nullptr;
         CK(cudaMalloc(&col, sizeof(int) * (size_t)std::max<int64_t>((int64_t)h_m2, 1)));
         k_compact<RT><<<grid_for((int64_t)n * 32, thr), thr, 0, st>>>(row, row2, n, tmp, col);
+        CK(cudaGetLastError());
+        k_compact_long<RT><<<152 * 2, 1024, 0, st>>>(row, row2, large, lcnt, tmp, col);
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(st));
         cudaFree(row);
