@@ -733,7 +733,8 @@ def measure_serving(torch, seconds: float = 2.0, fractions=(0.25, 0.5, 0.75, 1.0
     out = {"workload": "32 resident graphs: 16 RMAT scale U{12..22} ef 16, 16 grids side U[64, 4096]; "
                        "queries pick a graph uniformly and a source uniformly among degree>0 vertices; "
                        f"{num_slots} slots, batch window max(0.5 ms, 10% of the graph's recent launch time); "
-                       "grids (degree <= 16) served as up to 4 concurrent single-source searches per slot; "
+                       "grids (degree <= 16) served as up to 4 concurrent single-source searches per slot, "
+                       "each unit refilled as its search ends; "
                        "results copied into pinned host buffers",
            "plain_one_query_per_launch": {"queries_per_s": round(len(plain_ms) / (sum(plain_ms) / 1e3), 1),
                                           "p50_ms": round(plain_ms[len(plain_ms) // 2], 3),

@@ -4,30 +4,35 @@
 // Here a server keeps graphs resident, admits them against an HBM budget and
 // answers queries as they arrive:
 //   * every query joins its graph's FIFO;
-//   * `num_slots` worker threads, each owning CUDA streams, a 64-lane
-//     multi-source workspace and SRV_SUB single-source workspaces sized for
-//     the largest admitted graph, take the ready graph whose oldest query
-//     has waited longest:
-//       - on most graphs they pack up to `max_lanes` of its queries into one
-//         multi-source launch.  Such a graph is ready with a full batch or
-//         once its oldest query has waited `batch_window_us`, or
-//         `window_pct` percent of the graph's recent launch time if longer:
-//         a launch costs about the same for one source as for 64, so slow
-//         graphs gather bigger batches, while other graphs' queries keep the
-//         slots busy meanwhile;
+//   * `num_slots` slots, each a worker thread with SRV_SUB units (a CUDA
+//     stream and a single-source workspace each) and a 64-lane multi-source
+//     workspace, all sized for the largest admitted graph.  A slot's
+//     launches together use at most 1/num_slots of the GPU's CTAs, so every
+//     slot's launches fit on the GPU at once (each launch waits on all of
+//     its own CTAs);
+//   * whenever a unit is free, its worker serves the ready graphs in the
+//     order of their oldest query:
 //       - on a graph of small degree (meshes, grids, road networks) a
 //         search is a long chain of latency-bound levels that the
-//         label-correcting kernel runs at about the same speed on a quarter
-//         of the GPU, while a multi-source launch is bound by its lanes'
-//         combined frontiers; such a graph is ready as soon as it has a
-//         query, and a slot runs up to SRV_SUB of its queries as that many
-//         single-source searches at once, on its own streams, each capped
-//         to its share of the slot's CTAs;
-//   * slots run concurrently on their streams, each launch capped to
-//     1/num_slots of the GPU's CTAs so all of them fit on the GPU together
-//     (every launch waits on all of its own CTAs);
-//   * results are copied to the caller's buffer before the ticket completes;
-//     latency = submit -> result in place.
+//         label-correcting kernel runs at nearly the same speed on a
+//         fraction of the GPU, while a multi-source launch is bound by its
+//         lanes' combined frontiers: each free unit takes one query as a
+//         single-source search capped to 1/SRV_SUB of the slot's CTAs (the
+//         slot's whole share when it is the only query waiting).  Units
+//         refill one by one as their searches end, so a long search holds
+//         only its own unit;
+//       - on other graphs a launch packs up to `max_lanes` queries into one
+//         multi-source search on the whole slot.  Such a graph is ready
+//         with a full batch or once its oldest query has waited
+//         `batch_window_us`, or `window_pct` percent of the graph's recent
+//         launch time if longer: a launch costs about the same for one
+//         source as for 64, so slow graphs gather bigger batches.  When the
+//         slot is partly busy it stops filling units until they are free
+//         (one slot per waiting batch graph; the others keep filling behind
+//         it), so the batch is not overtaken by later queries;
+//   * a stream callback tells the worker when a launch's search, and then
+//     its result copies, are done; results are in the caller's buffer
+//     before the ticket completes (latency = submit -> result in place).
 #include <algorithm>
 #include <cstddef>
 #include <chrono>
@@ -68,18 +73,19 @@ struct SrvGraph {
     int64_t bytes = 0;
     std::deque<std::shared_ptr<SrvQuery>> pending;
     int inflight = 0;
-    double est_us = 0;   // recent launch time (moving average), 0 before the first
-    bool singles = false;  // small degree: served as concurrent single-source searches
+    double est_us = 0;     // recent launch time (moving average), 0 before the first
+    bool singles = false;  // small degree: served as single-source searches
+    int drainer = -1;      // the slot that stops filling units for this graph's next batch
 };
 
-// Single-source searches a slot runs at once on a graph of small degree.
-// A 4000 x 4000 grid search takes 12.7 ms on the whole GPU and 18.8 ms
-// capped to 19 CTAs; 16 such searches at once finish in 21.5 ms each (677
-// queries/s against 76 one after another), given enough hardware work
-// queues (CUDA_DEVICE_MAX_CONNECTIONS: with CUDA's default of 8, about four
+// Units (concurrent single-source searches) per slot.  A 4000 x 4000 grid
+// search takes 12.7 ms on the whole GPU and 18.8 ms capped to 19 CTAs; 16
+// such searches at once finish in 21.5 ms each (677 queries/s against 76 one
+// after another), given enough hardware work queues
+// (CUDA_DEVICE_MAX_CONNECTIONS: with CUDA's default of 8, about four
 // searches progress at a time).  On the 32-graph serving mix, 6 slots of 4
-// searches: capacity 3,358 queries/s (4 slots 2,713, 8 slots 2,999; 8
-// searches per slot 2,816); batching such a graph's queries into
+// searches run together: capacity 3,358 queries/s (4 slots 2,713, 8 slots
+// 2,999; 8 searches per slot 2,816); batching such a graph's queries into
 // multi-source launches from 16 pending on was slower.
 #ifndef SRV_SUB_DEF
 #define SRV_SUB_DEF 4
@@ -100,6 +106,26 @@ double ms_between(Clock::time_point a, Clock::time_point b)
     return std::chrono::duration<double, std::milli>(b - a).count();
 }
 
+// One launch on a slot: a single-source search on unit j's stream and
+// workspace, or (the slot taken whole) a multi-source batch or a search with
+// all of the slot's CTAs on unit 0.  busy and the queries are read and
+// written under the server's mutex, signalled under the slot's signal mutex,
+// phase only by the slot's worker.
+struct SrvJob {
+    gbfs_server *srv = nullptr;
+    int slot = 0;
+    bool busy = false;       // the unit holds a launch (planned or in flight)
+    bool signalled = false;  // the stream passed the launch's callback
+    int phase = 0;           // 1: search and status copy in flight, 2: result copies in flight
+    bool batch = false;      // a multi-source launch on the slot's 64-lane workspace
+    int cap = 0;             // CTA cap of a single-source search
+    int32_t gid = 0;
+    SrvGraph *sg = nullptr;  // stays valid: a graph with queries in flight is not removed
+    std::vector<std::shared_ptr<SrvQuery>> qs;
+    std::vector<int32_t> srcs;
+    Clock::time_point t_launch;
+};
+
 }  // namespace
 
 struct gbfs_server {
@@ -111,7 +137,7 @@ struct gbfs_server {
     // workspaces against a stale capacity (workers never take it)
     std::mutex admit_mu;
     std::mutex mu;
-    std::condition_variable cv_work, cv_done;
+    std::condition_variable cv_done;
     std::map<int32_t, SrvGraph> graphs;
     int32_t next_gid = 1;
     std::unordered_map<int64_t, std::shared_ptr<SrvQuery>> queries;
@@ -119,7 +145,7 @@ struct gbfs_server {
     int64_t n_cap = 0;            // slot workspaces cover graphs up to n_cap vertices
     int64_t resident = 0;         // graph bytes admitted
     int64_t peak = 0;
-    int busy_slots = 0;
+    int busy_jobs = 0;            // launches planned or in flight
     bool resizing = false;
     bool stop = false;
     // stats
@@ -133,170 +159,317 @@ struct gbfs_server {
     double lanes_sum = 0;
     // slots
     struct Slot {
-        cudaStream_t st[SRV_SUB] = {};  // st[0]: multi-source batches and the first search of a group
+        cudaStream_t st[SRV_SUB] = {};  // unit j's stream; unit 0 also carries whole-slot launches
         MsWork w;                       // 64-lane workspace (multi-source batches)
-        BfsWork bw[SRV_SUB];            // single-source workspaces (one per concurrent search)
+        BfsWork bw[SRV_SUB];            // unit j's single-source workspace
+        SrvJob job[SRV_SUB];            // unit j's launch
+        // stream callbacks and wake-ups reach the worker through sig_mu alone,
+        // never through the server's mutex (which admission holds across CUDA
+        // calls that may wait for those callbacks)
+        std::mutex sig_mu;
+        std::condition_variable cv;     // the worker waits here, with sig_mu
+        bool kick = false;              // new queries, admissions or shutdown (under sig_mu)
+        bool whole = false;             // job[0] holds every unit
+        int32_t drain_for = 0;          // a batch graph taken once every unit is free
         int64_t cap = 0;
     };
-    int bfs_ctas = 0;   // CTA cap of a single-source launch in a slot
-    std::vector<Slot> slots;
+    int bfs_ctas = 0;   // CTA cap of a single-source search holding a whole slot
+    std::vector<std::unique_ptr<Slot>> slots;
     std::vector<std::thread> workers;
 
     int64_t slots_total(int64_t cap) const { return slot_bytes(cap) * (int64_t)slots.size(); }
+    void wake_all()
+    {
+        for (auto &sl : slots) {
+            std::lock_guard<std::mutex> lk(sl->sig_mu);
+            sl->kick = true;
+            sl->cv.notify_all();
+        }
+    }
     void worker(int idx);
+    void plan(int idx, std::vector<int> &units, Clock::time_point &next_ready);
+    void take(Slot &sl, int j, int32_t gid, SrvGraph &c, int k, int cap, int lanes, std::vector<int> &units);
+    void launch(Slot &sl, int j);
+    void advance(Slot &sl, int j);
+    void finish(Slot &sl, int j, int status);
 };
+
+namespace {
+
+// Stream callback after a launch's work: marks the job for its worker (no
+// CUDA calls here).  The notification is made under the signal mutex, so the
+// worker cannot see the mark, finish and leave before it.
+void CUDART_CB job_signal(void *p)
+{
+    SrvJob *jb = static_cast<SrvJob *>(p);
+    auto &sl = *jb->srv->slots[jb->slot];
+    std::lock_guard<std::mutex> lk(sl.sig_mu);
+    jb->signalled = true;
+    sl.cv.notify_all();
+}
+
+}  // namespace
+
+// Under mu: unit j of `sl` takes k of graph c's oldest queries.
+void gbfs_server::take(Slot &sl, int j, int32_t gid, SrvGraph &c, int k, int cap, int lanes, std::vector<int> &units)
+{
+    SrvJob &jb = sl.job[j];
+    const auto now = Clock::now();
+    jb.busy = true;
+    jb.batch = k > 1;
+    jb.cap = cap;
+    jb.gid = gid;
+    jb.sg = &c;
+    jb.t_launch = now;
+    jb.qs.clear();
+    jb.srcs.clear();
+    for (int i = 0; i < k; i++) {
+        auto q = c.pending.front();
+        c.pending.pop_front();
+        q->t_launch = now;
+        q->lanes = lanes;
+        jb.qs.push_back(q);
+        jb.srcs.push_back(q->source);
+    }
+    c.inflight += k;
+    ++busy_jobs;
+    ++launches;
+    lanes_sum += lanes;
+    units.push_back(j);
+}
+
+// Under mu: the next launches of slot idx's free units, oldest waiting query
+// first.  A graph served by single-source searches gives each free unit one
+// query (the slot's whole CTA share when it is the only query waiting); a
+// batch graph needs the whole slot: when the slot is not free, it stops
+// filling units until it is (one slot per batch graph; the other slots keep
+// filling behind it).  next_ready: when the earliest batch graph not yet
+// ready (batch window) becomes ready.
+void gbfs_server::plan(int idx, std::vector<int> &units, Clock::time_point &next_ready)
+{
+    Slot &sl = *slots[idx];
+    if (sl.whole) return;
+    int nfree = 0;
+    for (auto &jb : sl.job) nfree += !jb.busy;
+    if (nfree == 0) return;
+    auto first_free = [&] {
+        int j = 0;
+        while (sl.job[j].busy) ++j;
+        return j;
+    };
+    if (sl.drain_for) {
+        auto it = graphs.find(sl.drain_for);
+        if (it == graphs.end() || it->second.pending.empty()) {
+            if (it != graphs.end() && it->second.drainer == idx) it->second.drainer = -1;
+            sl.drain_for = 0;
+        } else if (nfree < SRV_SUB) {
+            return;
+        } else if (it->second.csr.n <= sl.cap) {
+            SrvGraph &c = it->second;
+            c.drainer = -1;
+            sl.drain_for = 0;
+            const int k = std::min<int>((int)c.pending.size(), c.singles ? 1 : cfg.max_lanes);
+            sl.whole = true;
+            take(sl, 0, it->first, c, k, bfs_ctas, k, units);
+            return;
+        }
+    }
+    const auto now = Clock::now();
+    std::vector<std::pair<Clock::time_point, int32_t>> ready;
+    size_t ready_queries = 0;
+    for (auto &kv : graphs) {
+        SrvGraph &c = kv.second;
+        if (c.pending.empty() || c.csr.n > sl.cap) continue;
+        const auto t0 = c.pending.front()->t_submit;
+        if (!c.singles && !stop && (int)c.pending.size() < cfg.max_lanes) {
+            // a batch graph is ready with a full batch or once its oldest
+            // query has waited out the graph's window
+            const double window_us =
+                std::min(1e6, std::max<double>(cfg.batch_window_us, 0.01 * cfg.window_pct * c.est_us));
+            const auto ready_at = t0 + std::chrono::microseconds((int64_t)window_us);
+            if (now < ready_at) {
+                next_ready = std::min(next_ready, ready_at);
+                continue;
+            }
+        }
+        ready.emplace_back(t0, kv.first);
+        ready_queries += c.pending.size();
+    }
+    std::sort(ready.begin(), ready.end());
+    for (auto &r : ready) {
+        SrvGraph &c = graphs.find(r.second)->second;
+        if (c.singles) {
+            if (nfree == SRV_SUB && ready_queries == 1) {
+                // the only query waiting: one search with the slot's CTAs
+                sl.whole = true;
+                take(sl, 0, r.second, c, 1, bfs_ctas, 1, units);
+                return;
+            }
+            while (nfree > 0 && !c.pending.empty()) {
+                take(sl, first_free(), r.second, c, 1, std::max(1, bfs_ctas / SRV_SUB), SRV_SUB - nfree + 1, units);
+                --nfree;
+            }
+            if (nfree == 0) return;
+        } else if (nfree == SRV_SUB) {
+            const int k = std::min<int>((int)c.pending.size(), cfg.max_lanes);
+            sl.whole = true;
+            take(sl, 0, r.second, c, k, bfs_ctas, k, units);
+            return;
+        } else if (c.drainer < 0) {
+            c.drainer = idx;
+            sl.drain_for = r.second;
+            return;
+        }
+    }
+}
+
+// Outside mu: enqueue unit j's launch, its status read-back and its callback.
+void gbfs_server::launch(Slot &sl, int j)
+{
+    SrvJob &jb = sl.job[j];
+    gbfs_graph *g = jb.sg->g;
+    const DeviceCsr &csr = jb.sg->csr;
+    gbfs_params p = graph_params(g);
+    p.timeout_ms = cfg.timeout_ms;
+    if (!g->symmetric && !csr.trow) p.direction = GBFS_DIR_TOPDOWN;  // bottom-up needs in-edges
+    cudaStream_t st = sl.st[j];
+    cudaError_t e;
+    if (jb.batch) {
+        const int k = (int)jb.srcs.size();
+        e = cudaMemcpyAsync(sl.w.src, jb.srcs.data(), sizeof(int32_t) * k, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = msbfs_enqueue(csr, p, g->symmetric, sl.w, sl.w.src, k, sl.w.out, st, max_ctas);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(sl.w.h_ctrl, sl.w.ctrl, offsetof(MsCtrl, t_entry), cudaMemcpyDeviceToHost, st);
+    } else {
+        BfsWork &bw = sl.bw[j];
+        e = bfs_enqueue(csr, p, bw, nullptr, 1, jb.srcs[0], bw.level, &bw.ctrl->out, st, g->symmetric, 0, 0, jb.cap);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(&bw.h_ctrl->status, &bw.ctrl->status, sizeof(int), cudaMemcpyDeviceToHost, st);
+    }
+    // phase is set before the worker can next look at the signal
+    jb.phase = 1;
+    if (e == cudaSuccess) e = cudaLaunchHostFunc(st, job_signal, &jb);
+    if (e != cudaSuccess) {
+        cudaStreamSynchronize(st);
+        finish(sl, j, GBFS_ERR_CUDA);
+    }
+}
+
+// Outside mu, after unit j's callback: check the search's status and copy
+// the levels out (phase 1), or complete the queries (phase 2).
+void gbfs_server::advance(Slot &sl, int j)
+{
+    SrvJob &jb = sl.job[j];
+    if (jb.phase == 2) {
+        finish(sl, j, GBFS_OK);
+        return;
+    }
+    cudaStream_t st = sl.st[j];
+    const int dev_status = jb.batch ? sl.w.h_ctrl->status : sl.bw[j].h_ctrl->status;
+    if (dev_status != DEV_OK) {
+        // a bounded wait ran out: clear the control block for the unit's
+        // next launch (ordered before it on the same stream)
+        if (jb.batch) cudaMemsetAsync(sl.w.ctrl, 0, sizeof(MsCtrl), st);
+        else cudaMemsetAsync(sl.bw[j].ctrl, 0, sizeof(BfsCtrl), st);
+        finish(sl, j, GBFS_ERR_TIMEOUT);
+        return;
+    }
+    const size_t n = (size_t)jb.sg->csr.n;
+    cudaError_t e = cudaSuccess;
+    if (jb.batch) {
+        for (size_t i = 0; i < jb.qs.size() && e == cudaSuccess; i++)
+            e = cudaMemcpyAsync(jb.qs[i]->out, sl.w.out + n * i, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st);
+    } else {
+        e = cudaMemcpyAsync(jb.qs[0]->out, sl.bw[j].level, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st);
+    }
+    jb.phase = 2;
+    if (e == cudaSuccess) e = cudaLaunchHostFunc(st, job_signal, &jb);
+    if (e != cudaSuccess) {
+        cudaStreamSynchronize(st);
+        finish(sl, j, GBFS_ERR_CUDA);
+    }
+}
+
+// Complete unit j's queries with `status` and free the unit.
+void gbfs_server::finish(Slot &sl, int j, int status)
+{
+    SrvJob &jb = sl.job[j];
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        const auto now = Clock::now();
+        for (auto &q : jb.qs) {
+            q->status = status;
+            q->done = true;
+            q->latency_ms = ms_between(q->t_submit, now);
+            q->queue_ms = ms_between(q->t_submit, q->t_launch);
+            if (status == GBFS_OK) {
+                if (lat.size() < LAT_WINDOW) lat.push_back(q->latency_ms);
+                else lat[lat_next] = q->latency_ms;
+                lat_next = (lat_next + 1) % LAT_WINDOW;
+                ++completed;
+            }
+        }
+        SrvGraph &c = *jb.sg;
+        c.inflight -= (int)jb.qs.size();
+        const double us = std::chrono::duration<double, std::micro>(now - jb.t_launch).count();
+        c.est_us = c.est_us > 0 ? 0.7 * c.est_us + 0.3 * us : us;
+        jb.qs.clear();
+        jb.srcs.clear();
+        jb.sg = nullptr;
+        jb.phase = 0;
+        jb.busy = false;
+        if (j == 0) sl.whole = false;
+        --busy_jobs;
+    }
+    cv_done.notify_all();
+}
 
 void gbfs_server::worker(int idx)
 {
     cudaSetDevice(device);
-    Slot &slot = slots[idx];
-    std::vector<std::shared_ptr<SrvQuery>> batch;
-    std::vector<int32_t> srcs;
+    Slot &sl = *slots[idx];
+    std::vector<int> start, done;
+    Clock::time_point next_ready = Clock::time_point::max();
     for (;;) {
-        SrvGraph *sg = nullptr;
-        int32_t gid = 0;
+        // launches whose callbacks ran: the next phase
+        done.clear();
         {
-            std::unique_lock<std::mutex> lk(mu);
-            for (;;) {
-                Clock::time_point next_ready = Clock::time_point::max();
-                if (!resizing) {
-                    // among the graphs that are ready (a full batch, or their
-                    // oldest query has waited out the graph's window), the one
-                    // whose oldest query has waited longest
-                    const auto now = Clock::now();
-                    Clock::time_point oldest = Clock::time_point::max();
-                    for (auto &kv : graphs) {
-                        SrvGraph &c = kv.second;
-                        if (c.pending.empty()) continue;
-                        const auto t0 = c.pending.front()->t_submit;
-                        const double window_us =
-                            std::min(1e6, std::max<double>(cfg.batch_window_us, 0.01 * cfg.window_pct * c.est_us));
-                        const auto ready_at = t0 + std::chrono::microseconds((int64_t)window_us);
-                        if (c.singles || (int)c.pending.size() >= cfg.max_lanes || now >= ready_at || stop) {
-                            if (t0 < oldest) {
-                                oldest = t0;
-                                sg = &c;
-                                gid = kv.first;
-                            }
-                        } else {
-                            next_ready = std::min(next_ready, ready_at);
-                        }
-                    }
-                    if (sg) break;
+            std::lock_guard<std::mutex> lk(sl.sig_mu);
+            sl.kick = false;
+            for (int j = 0; j < SRV_SUB; j++)
+                if (sl.job[j].signalled) {
+                    sl.job[j].signalled = false;
+                    done.push_back(j);
                 }
-                if (stop && next_ready == Clock::time_point::max()) return;
-                if (next_ready != Clock::time_point::max()) cv_work.wait_until(lk, next_ready);
-                else cv_work.wait(lk);
-            }
-            const int k = std::min<int>((int)sg->pending.size(), sg->singles ? SRV_SUB : cfg.max_lanes);
-            batch.clear();
-            srcs.clear();
-            const auto now = Clock::now();
-            for (int i = 0; i < k; i++) {
-                auto q = sg->pending.front();
-                sg->pending.pop_front();
-                q->t_launch = now;
-                q->lanes = k;
-                batch.push_back(q);
-                srcs.push_back(q->source);
-            }
-            sg->inflight += k;
-            ++busy_slots;
-            ++launches;
-            lanes_sum += k;
         }
-        gbfs_graph *g = sg->g;
-        const int k = (int)batch.size();
-        const auto t_launch = Clock::now();
-        const DeviceCsr &csr = sg->csr;
-        const size_t n = (size_t)csr.n;
-        gbfs_params p = graph_params(g);
-        p.timeout_ms = cfg.timeout_ms;
-        if (!g->symmetric && !csr.trow) p.direction = GBFS_DIR_TOPDOWN;  // bottom-up needs in-edges
-        // per query: 0, or a status
-        int qstatus[MS_LANES];
-        for (int i = 0; i < k; i++) qstatus[i] = GBFS_OK;
-        if (k == 1 || (k <= SRV_SUB && bfs_relax_tail(csr, p))) {
-            // one query, or up to SRV_SUB on a graph of small degree: that
-            // many single-source searches at once, each on its own stream
-            // and workspace, sharing the slot's CTAs
-            const int cap = k == 1 ? bfs_ctas : std::max(1, bfs_ctas / k);
-            cudaError_t es[SRV_SUB];
-            for (int j = 0; j < k; j++) {
-                BfsWork &bw = slot.bw[j];
-                es[j] = bfs_enqueue(csr, p, bw, nullptr, 1, srcs[j], bw.level, &bw.ctrl->out, slot.st[j],
-                                    g->symmetric, 0, 0, cap);
-                if (es[j] == cudaSuccess)
-                    es[j] = cudaMemcpyAsync(&bw.h_ctrl->status, &bw.ctrl->status, sizeof(int), cudaMemcpyDeviceToHost,
-                                            slot.st[j]);
-            }
-            for (int j = 0; j < k; j++) {
-                BfsWork &bw = slot.bw[j];
-                if (es[j] == cudaSuccess) es[j] = cudaStreamSynchronize(slot.st[j]);
-                const int dev_status = es[j] == cudaSuccess ? bw.h_ctrl->status : DEV_OK;
-                if (es[j] == cudaSuccess && dev_status == DEV_OK)
-                    es[j] = cudaMemcpyAsync(batch[j]->out, bw.level, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
-                                            slot.st[j]);
-                if (es[j] == cudaSuccess && dev_status != DEV_OK) {
-                    cudaMemsetAsync(bw.ctrl, 0, sizeof(BfsCtrl), slot.st[j]);
-                    qstatus[j] = GBFS_ERR_TIMEOUT;
-                }
-            }
-            for (int j = 0; j < k; j++) {
-                if (es[j] == cudaSuccess) es[j] = cudaStreamSynchronize(slot.st[j]);
-                if (es[j] != cudaSuccess) qstatus[j] = GBFS_ERR_CUDA;
-            }
-        } else {
-            cudaError_t e = cudaMemcpyAsync(slot.w.src, srcs.data(), sizeof(int32_t) * k, cudaMemcpyHostToDevice,
-                                            slot.st[0]);
-            int dev_status = DEV_OK;
-            if (e == cudaSuccess)
-                e = msbfs_enqueue(csr, p, g->symmetric, slot.w, slot.w.src, k, slot.w.out, slot.st[0], max_ctas);
-            if (e == cudaSuccess)
-                e = cudaMemcpyAsync(slot.w.h_ctrl, slot.w.ctrl, offsetof(MsCtrl, t_entry), cudaMemcpyDeviceToHost,
-                                    slot.st[0]);
-            if (e == cudaSuccess) e = cudaStreamSynchronize(slot.st[0]);
-            if (e == cudaSuccess) dev_status = slot.w.h_ctrl->status;
-            if (e == cudaSuccess && dev_status != DEV_OK) {
-                cudaMemsetAsync(slot.w.ctrl, 0, sizeof(MsCtrl), slot.st[0]);
-                cudaStreamSynchronize(slot.st[0]);
-            } else if (e == cudaSuccess) {
-                for (int i = 0; i < k && e == cudaSuccess; i++)
-                    e = cudaMemcpyAsync(batch[i]->out, slot.w.out + n * i, sizeof(int32_t) * n,
-                                        cudaMemcpyDeviceToHost, slot.st[0]);
-                if (e == cudaSuccess) e = cudaStreamSynchronize(slot.st[0]);
-            }
-            const int status = e != cudaSuccess ? GBFS_ERR_CUDA : dev_status != DEV_OK ? GBFS_ERR_TIMEOUT : GBFS_OK;
-            for (int i = 0; i < k; i++) qstatus[i] = status;
-        }
+        for (int j : done) advance(sl, j);
+        if (!done.empty()) continue;
+        // free units: new launches
+        start.clear();
+        next_ready = Clock::time_point::max();
         {
             std::lock_guard<std::mutex> lk(mu);
-            const auto now = Clock::now();
-            for (int i = 0; i < k; i++) {
-                auto &q = batch[i];
-                const int status = qstatus[i];
-                q->status = status;
-                q->done = true;
-                q->latency_ms = ms_between(q->t_submit, now);
-                q->queue_ms = ms_between(q->t_submit, q->t_launch);
-                if (status == GBFS_OK) {
-                    if (lat.size() < LAT_WINDOW) lat.push_back(q->latency_ms);
-                    else lat[lat_next] = q->latency_ms;
-                    lat_next = (lat_next + 1) % LAT_WINDOW;
-                    ++completed;
-                }
+            if (!resizing) plan(idx, start, next_ready);
+            if (start.empty() && stop) {
+                bool idle = true, pending = false;
+                for (auto &jb : sl.job) idle = idle && !jb.busy;
+                for (auto &kv : graphs)
+                    pending = pending || (!kv.second.pending.empty() && kv.second.csr.n <= sl.cap);
+                if (idle && !pending) return;
             }
-            auto it = graphs.find(gid);
-            if (it != graphs.end()) {
-                SrvGraph &c = it->second;
-                c.inflight -= k;
-                const double us = std::chrono::duration<double, std::micro>(now - t_launch).count();
-                c.est_us = c.est_us > 0 ? 0.7 * c.est_us + 0.3 * us : us;
-            }
-            --busy_slots;
         }
-        cv_done.notify_all();
-        cv_work.notify_all();
+        for (int j : start) launch(sl, j);
+        if (!start.empty()) continue;
+        // nothing to do: wait for a callback, a wake-up or a batch window
+        std::unique_lock<std::mutex> lk(sl.sig_mu);
+        auto woken = [&] {
+            if (sl.kick) return true;
+            for (auto &jb : sl.job)
+                if (jb.signalled) return true;
+            return false;
+        };
+        if (next_ready != Clock::time_point::max()) sl.cv.wait_until(lk, next_ready, woken);
+        else sl.cv.wait(lk, woken);
     }
 }
 
@@ -333,9 +506,20 @@ extern "C" int gbfs_server_create(const gbfs_server_config *cfg, gbfs_server **o
         }
         s->bfs_ctas = std::max(1, tb / cfg->num_slots);
     }
-    s->slots.resize(cfg->num_slots);
+    for (int i = 0; i < cfg->num_slots; i++) {
+        s->slots.emplace_back(new (std::nothrow) gbfs_server::Slot());
+        if (!s->slots.back()) {
+            s->slots.pop_back();
+            gbfs_server_destroy(s);
+            return fail(GBFS_ERR_OOM, "host allocation failed");
+        }
+        for (int j = 0; j < SRV_SUB; j++) {
+            s->slots.back()->job[j].srv = s;
+            s->slots.back()->job[j].slot = i;
+        }
+    }
     for (auto &sl : s->slots)
-        for (auto &st : sl.st)
+        for (auto &st : sl->st)
             if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
                 gbfs_server_destroy(s);
                 return fail(GBFS_ERR_CUDA, "cudaStreamCreate");
@@ -351,16 +535,17 @@ extern "C" void gbfs_server_destroy(gbfs_server *s)
     {
         std::lock_guard<std::mutex> lk(s->mu);
         s->stop = true;
+        s->wake_all();
     }
-    s->cv_work.notify_all();
     for (auto &t : s->workers)
         if (t.joinable()) t.join();
+    // the synchronisation also waits for the last callbacks to return
     for (auto &sl : s->slots) {
-        for (auto st : sl.st)
+        for (auto st : sl->st)
             if (st) cudaStreamSynchronize(st);
-        ms_work_free(sl.w);
-        for (auto &bw : sl.bw) bfs_work_free(bw);
-        for (auto st : sl.st)
+        ms_work_free(sl->w);
+        for (auto &bw : sl->bw) bfs_work_free(bw);
+        for (auto st : sl->st)
             if (st) cudaStreamDestroy(st);
     }
     delete s;
@@ -390,7 +575,7 @@ extern "C" int gbfs_server_add_graph(gbfs_server *s, gbfs_graph *g, int32_t *gra
     if (new_cap > s->n_cap) {
         // grow every slot's workspace once the slots are idle
         s->resizing = true;
-        s->cv_done.wait(lk, [&] { return s->busy_slots == 0; });
+        s->cv_done.wait(lk, [&] { return s->busy_jobs == 0; });
         std::string err;
         int rc = GBFS_OK;
         auto slot_free = [](gbfs_server::Slot &sl) {
@@ -406,24 +591,26 @@ extern "C" int gbfs_server_add_graph(gbfs_server *s, gbfs_graph *g, int32_t *gra
             return r;
         };
         for (auto &sl : s->slots) {
-            slot_free(sl);
-            rc = slot_alloc(sl, new_cap, err);
+            slot_free(*sl);
+            rc = slot_alloc(*sl, new_cap, err);
             if (rc) break;
         }
         s->resizing = false;
         if (rc) {
-            for (auto &sl : s->slots) slot_free(sl);
+            for (auto &sl : s->slots) slot_free(*sl);
             const int64_t old = s->n_cap;
             s->n_cap = 0;
             // restore the previous capacity if possible
             std::string err2;
+            // (a slot left without a workspace takes no queries: its cap is 0)
             for (auto &sl : s->slots)
-                if (old > 0 && slot_alloc(sl, old, err2) != GBFS_OK) slot_free(sl);
+                if (old > 0 && slot_alloc(*sl, old, err2) != GBFS_OK) slot_free(*sl);
             s->n_cap = old;
-            s->cv_work.notify_all();
+            s->wake_all();
             return fail(rc, "slot workspace: " + err);
         }
         s->n_cap = new_cap;
+        s->wake_all();
     }
     {
         std::lock_guard<std::mutex> glk(g->mu);
@@ -443,7 +630,7 @@ extern "C" int gbfs_server_add_graph(gbfs_server *s, gbfs_graph *g, int32_t *gra
     s->resident += gbytes;
     s->peak = std::max(s->peak, s->resident + s->slots_total(s->n_cap));
     *graph_id = gid;
-    s->cv_work.notify_all();
+    s->wake_all();
     return GBFS_OK;
 }
 
@@ -480,7 +667,7 @@ extern "C" int gbfs_server_submit(gbfs_server *s, int32_t graph_id, int32_t sour
         s->queries.emplace(q->ticket, q);
         *ticket = q->ticket;
     }
-    s->cv_work.notify_one();
+    s->wake_all();
     return GBFS_OK;
 }
 

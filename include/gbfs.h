@@ -384,9 +384,11 @@ int64_t gbfs_gen_grid_capacity(int32_t side, double extra);
  * arrive while others run are packed into 64-lane multi-source launches as
  * slots (streams with their own workspace) free up.  On a graph of
  * out-degree <= 16 (meshes, grids, road networks: long searches of small
- * frontiers) a slot instead runs up to 4 of its queries at once as
- * single-source searches on its own streams, each with a share of the
- * slot's CTAs (batch_lanes then counts the searches run together).
+ * frontiers) each slot instead runs up to 4 queries at once as
+ * single-source searches on its own streams, each with a quarter of the
+ * slot's CTAs, and starts the next waiting query as soon as any of them
+ * ends (batch_lanes then counts the slot's searches running at its start;
+ * a query alone in the server gets the slot's whole CTA share).
  * These run concurrently only with enough hardware work queues: start the
  * process with CUDA_DEVICE_MAX_CONNECTIONS of at least 4 * num_slots + 2
  * (CUDA's default of 8 lets about four searches progress at a time). */
