@@ -26,10 +26,12 @@
 //         with a full batch or once its oldest query has waited
 //         `batch_window_us`, or `window_pct` percent of the graph's recent
 //         launch time if longer: a launch costs about the same for one
-//         source as for 64, so slow graphs gather bigger batches.  When the
-//         slot is partly busy it stops filling units until they are free
-//         (one slot per waiting batch graph; the others keep filling behind
-//         it), so the batch is not overtaken by later queries;
+//         source as for 64, so slow graphs gather bigger batches.  A batch
+//         of one query runs on one free unit (the whole slot if all its
+//         units are free).  For a larger batch a partly busy slot stops
+//         filling units until they are free (one slot per waiting batch
+//         graph; the others keep filling behind it), so the batch is not
+//         overtaken by later queries;
 //   * a stream callback tells the worker when a launch's search, and then
 //     its result copies, are done; results are in the caller's buffer
 //     before the ticket completes (latency = submit -> result in place).
@@ -83,10 +85,11 @@ struct SrvGraph {
 // such searches at once finish in 21.5 ms each (677 queries/s against 76 one
 // after another), given enough hardware work queues
 // (CUDA_DEVICE_MAX_CONNECTIONS: with CUDA's default of 8, about four
-// searches progress at a time).  On the 32-graph serving mix, 6 slots of 4
-// searches run together: capacity 3,358 queries/s (4 slots 2,713, 8 slots
-// 2,999; 8 searches per slot 2,816); batching such a graph's queries into
-// multi-source launches from 16 pending on was slower.
+// searches progress at a time).  On the 32-graph serving mix, with a slot's
+// units refilled as a group: 6 slots of 4 units, capacity up to 3,358
+// queries/s (4 slots 2,713, 8 slots 2,999; 8 units per slot 2,816);
+// batching such a graph's queries into multi-source launches from 16
+// pending on was slower.
 #ifndef SRV_SUB_DEF
 #define SRV_SUB_DEF 4
 #endif
@@ -240,10 +243,10 @@ void gbfs_server::take(Slot &sl, int j, int32_t gid, SrvGraph &c, int k, int cap
 
 // Under mu: the next launches of slot idx's free units, oldest waiting query
 // first.  A graph served by single-source searches gives each free unit one
-// query (the slot's whole CTA share when it is the only query waiting); a
-// batch graph needs the whole slot: when the slot is not free, it stops
-// filling units until it is (one slot per batch graph; the other slots keep
-// filling behind it).  next_ready: when the earliest batch graph not yet
+// query (the slot's whole CTA share when it is the only query waiting); so
+// does a batch graph with one query waiting.  A larger batch needs the whole
+// slot: when the slot is not free, it stops filling units until it is (one
+// slot per batch graph; the other slots keep filling behind it).  next_ready: when the earliest batch graph not yet
 // ready (batch window) becomes ready.
 void gbfs_server::plan(int idx, std::vector<int> &units, Clock::time_point &next_ready)
 {
@@ -315,6 +318,10 @@ void gbfs_server::plan(int idx, std::vector<int> &units, Clock::time_point &next
             sl.whole = true;
             take(sl, 0, r.second, c, k, bfs_ctas, k, units);
             return;
+        } else if (c.pending.size() == 1) {
+            // a batch of one: a single-source search on one unit, no drain
+            take(sl, first_free(), r.second, c, 1, std::max(1, bfs_ctas / SRV_SUB), SRV_SUB - nfree + 1, units);
+            if (--nfree == 0) return;
         } else if (c.drainer < 0) {
             c.drainer = idx;
             sl.drain_for = r.second;
