@@ -172,6 +172,7 @@ struct gbfs_server {
         std::mutex sig_mu;
         std::condition_variable cv;     // the worker waits here, with sig_mu
         bool kick = false;              // new queries, admissions or shutdown (under sig_mu)
+        std::vector<std::pair<Clock::time_point, int32_t>> ready;  // plan's scratch (under mu)
         bool whole = false;             // job[0] holds every unit
         int32_t drain_for = 0;          // a batch graph taken once every unit is free
         int64_t cap = 0;
@@ -181,13 +182,15 @@ struct gbfs_server {
     std::vector<std::thread> workers;
 
     int64_t slots_total(int64_t cap) const { return slot_bytes(cap) * (int64_t)slots.size(); }
+    static void kick(Slot &sl)
+    {
+        std::lock_guard<std::mutex> lk(sl.sig_mu);
+        sl.kick = true;
+        sl.cv.notify_all();
+    }
     void wake_all()
     {
-        for (auto &sl : slots) {
-            std::lock_guard<std::mutex> lk(sl->sig_mu);
-            sl->kick = true;
-            sl->cv.notify_all();
-        }
+        for (auto &sl : slots) kick(*sl);
     }
     void worker(int idx);
     void plan(int idx, std::vector<int> &units, Clock::time_point &next_ready);
@@ -278,7 +281,8 @@ void gbfs_server::plan(int idx, std::vector<int> &units, Clock::time_point &next
         }
     }
     const auto now = Clock::now();
-    std::vector<std::pair<Clock::time_point, int32_t>> ready;
+    auto &ready = sl.ready;
+    ready.clear();
     size_t ready_queries = 0;
     for (auto &kv : graphs) {
         SrvGraph &c = kv.second;
@@ -673,8 +677,14 @@ extern "C" int gbfs_server_submit(gbfs_server *s, int32_t graph_id, int32_t sour
         it->second.pending.push_back(q);
         s->queries.emplace(q->ticket, q);
         *ticket = q->ticket;
+        // wake the slots with a free unit; the others plan again when one of
+        // their launches ends
+        for (auto &sl : s->slots) {
+            bool free_unit = false;
+            for (auto &jb : sl->job) free_unit = free_unit || !jb.busy;
+            if (free_unit && !sl->whole) gbfs_server::kick(*sl);
+        }
     }
-    s->wake_all();
     return GBFS_OK;
 }
 
