@@ -13,11 +13,14 @@ class Server:
     """Continuous-batching BFS server.
 
     Graphs are admitted against an HBM budget; queries are queued per graph
-    and packed (up to ``max_lanes`` sources) into multi-source launches as
-    slots free up, on ``num_slots`` concurrent streams.  A graph's queries
-    wait up to ``batch_window_us``, or ``window_pct`` percent of its recent
-    launch time if that is longer, for a fuller batch.  Result copies are
-    fastest into pinned host buffers.
+    and served by ``num_slots`` slots of four units (streams) each.  On most
+    graphs a slot packs up to ``max_lanes`` queued sources into one
+    multi-source launch; a graph's queries wait up to ``batch_window_us``,
+    or ``window_pct`` percent of its recent launch time if that is longer,
+    for a fuller batch.  On graphs of out-degree <= 16 (grids, meshes, road
+    networks) every free unit runs one query as a single-source search and
+    takes the next as soon as it ends.  Result copies are fastest into
+    pinned host buffers.
     """
 
     def __init__(self, mem_budget_bytes: int, num_slots: int = 4, max_lanes: int = 64,
