@@ -45,7 +45,7 @@ def _stale(lib: Path, deps: list[Path]) -> bool:
 def build(verbose: bool = False, force: bool = False) -> Path:
     """Compile csrc/ into libgbfs.so if anything changed; return its path."""
     srcs = sources()
-    deps = srcs + list(CSRC.glob("*.cuh")) + list((HERE.parent / "include").glob("*.h")) + [Path(__file__)]
+    deps = srcs + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list((HERE.parent / "include").glob("*.h")) + [Path(__file__)]
     if not force and not _stale(LIB, deps):
         return LIB
     BUILD.mkdir(exist_ok=True)

@@ -49,6 +49,7 @@
 #include <vector>
 
 #include "graph.cuh"
+#include "server_plan.h"
 
 using namespace gbfs;
 using Clock = std::chrono::steady_clock;
@@ -192,6 +193,19 @@ struct gbfs_server {
     {
         for (auto &sl : slots) kick(*sl);
     }
+    // under mu: wake the slots other than idx that have a free unit
+    void kick_others(int idx)
+    {
+        for (int o = 0; o < (int)slots.size(); o++) {
+            Slot &sl = *slots[o];
+            if (o == idx || sl.whole) continue;
+            for (auto &jb : sl.job)
+                if (!jb.busy) {
+                    kick(sl);
+                    break;
+                }
+        }
+    }
     void worker(int idx);
     void plan(int idx, std::vector<int> &units, Clock::time_point &next_ready);
     void take(Slot &sl, int j, int32_t gid, SrvGraph &c, int k, int cap, int lanes, std::vector<int> &units);
@@ -244,94 +258,11 @@ void gbfs_server::take(Slot &sl, int j, int32_t gid, SrvGraph &c, int k, int cap
     units.push_back(j);
 }
 
-// Under mu: the next launches of slot idx's free units, oldest waiting query
-// first.  A graph served by single-source searches gives each free unit one
-// query (the slot's whole CTA share when it is the only query waiting); so
-// does a batch graph with one query waiting.  A larger batch needs the whole
-// slot: when the slot is not free, it stops filling units until it is (one
-// slot per batch graph; the other slots keep filling behind it).  next_ready: when the earliest batch graph not yet
-// ready (batch window) becomes ready.
+// Under mu: the next launches of slot idx's free units (the rule is in
+// server_plan.h).
 void gbfs_server::plan(int idx, std::vector<int> &units, Clock::time_point &next_ready)
 {
-    Slot &sl = *slots[idx];
-    if (sl.whole) return;
-    int nfree = 0;
-    for (auto &jb : sl.job) nfree += !jb.busy;
-    if (nfree == 0) return;
-    auto first_free = [&] {
-        int j = 0;
-        while (sl.job[j].busy) ++j;
-        return j;
-    };
-    if (sl.drain_for) {
-        auto it = graphs.find(sl.drain_for);
-        if (it == graphs.end() || it->second.pending.empty()) {
-            if (it != graphs.end() && it->second.drainer == idx) it->second.drainer = -1;
-            sl.drain_for = 0;
-        } else if (nfree < SRV_SUB) {
-            return;
-        } else if (it->second.csr.n <= sl.cap) {
-            SrvGraph &c = it->second;
-            c.drainer = -1;
-            sl.drain_for = 0;
-            const int k = std::min<int>((int)c.pending.size(), c.singles ? 1 : cfg.max_lanes);
-            sl.whole = true;
-            take(sl, 0, it->first, c, k, bfs_ctas, k, units);
-            return;
-        }
-    }
-    const auto now = Clock::now();
-    auto &ready = sl.ready;
-    ready.clear();
-    size_t ready_queries = 0;
-    for (auto &kv : graphs) {
-        SrvGraph &c = kv.second;
-        if (c.pending.empty() || c.csr.n > sl.cap) continue;
-        const auto t0 = c.pending.front()->t_submit;
-        if (!c.singles && !stop && (int)c.pending.size() < cfg.max_lanes) {
-            // a batch graph is ready with a full batch or once its oldest
-            // query has waited out the graph's window
-            const double window_us =
-                std::min(1e6, std::max<double>(cfg.batch_window_us, 0.01 * cfg.window_pct * c.est_us));
-            const auto ready_at = t0 + std::chrono::microseconds((int64_t)window_us);
-            if (now < ready_at) {
-                next_ready = std::min(next_ready, ready_at);
-                continue;
-            }
-        }
-        ready.emplace_back(t0, kv.first);
-        ready_queries += c.pending.size();
-    }
-    std::sort(ready.begin(), ready.end());
-    for (auto &r : ready) {
-        SrvGraph &c = graphs.find(r.second)->second;
-        if (c.singles) {
-            if (nfree == SRV_SUB && ready_queries == 1) {
-                // the only query waiting: one search with the slot's CTAs
-                sl.whole = true;
-                take(sl, 0, r.second, c, 1, bfs_ctas, 1, units);
-                return;
-            }
-            while (nfree > 0 && !c.pending.empty()) {
-                take(sl, first_free(), r.second, c, 1, std::max(1, bfs_ctas / SRV_SUB), SRV_SUB - nfree + 1, units);
-                --nfree;
-            }
-            if (nfree == 0) return;
-        } else if (nfree == SRV_SUB) {
-            const int k = std::min<int>((int)c.pending.size(), cfg.max_lanes);
-            sl.whole = true;
-            take(sl, 0, r.second, c, k, bfs_ctas, k, units);
-            return;
-        } else if (c.pending.size() == 1) {
-            // a batch of one: a single-source search on one unit, no drain
-            take(sl, first_free(), r.second, c, 1, std::max(1, bfs_ctas / SRV_SUB), SRV_SUB - nfree + 1, units);
-            if (--nfree == 0) return;
-        } else if (c.drainer < 0) {
-            c.drainer = idx;
-            sl.drain_for = r.second;
-            return;
-        }
-    }
+    plan_slot<SRV_SUB>(*this, idx, Clock::now(), units, next_ready);
 }
 
 // Outside mu: enqueue unit j's launch, its status read-back and its callback.
