@@ -172,7 +172,7 @@ struct gbfs_server {
         // calls that may wait for those callbacks)
         std::mutex sig_mu;
         std::condition_variable cv;     // the worker waits here, with sig_mu
-        bool kick = false;              // new queries, admissions or shutdown (under sig_mu)
+        bool kick = false;              // queries to look at, admission or shutdown (under sig_mu)
         std::vector<std::pair<Clock::time_point, int32_t>> ready;  // plan's scratch (under mu)
         bool whole = false;             // job[0] holds every unit
         int32_t drain_for = 0;          // a batch graph taken once every unit is free
