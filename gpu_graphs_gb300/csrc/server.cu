@@ -355,6 +355,9 @@ void gbfs_server::finish(Slot &sl, int j, int status)
         c.inflight -= (int)jb.qs.size();
         const double us = std::chrono::duration<double, std::micro>(now - jb.t_launch).count();
         c.est_us = c.est_us > 0 ? 0.7 * c.est_us + 0.3 * us : us;
+        // the graph's batch window moved with its launch time: slots timed
+        // on the old one look again (this slot plans next anyway)
+        if (!c.pending.empty()) kick_others(jb.slot);
         jb.qs.clear();
         jb.srcs.clear();
         jb.sg = nullptr;

@@ -2,9 +2,11 @@
 // the code server.cu runs) with simulated launches and arrivals on the CPU.
 //
 // A slot plans when the server would wake its worker: a submitted query wakes
-// the slots with a free unit, a finished launch wakes its own slot, a batch
-// window wakes the slots waiting on it; a woken worker plans until it starts
-// nothing.  After every event the simulation checks:
+// the slots with a free unit, a finished launch wakes its own slot (and the
+// others with a free unit when its graph still has queries waiting), a
+// launch that leaves queries behind wakes the others with a free unit, a
+// batch window wakes the slots waiting on it; a woken worker plans until it
+// starts nothing.  After every event the simulation checks:
 //   * a unit never takes a second launch, a slot's launches never hold more
 //     than its CTA share, a batch of two or more queries runs only on a whole
 //     free slot;
@@ -124,6 +126,7 @@ struct Sim {
             CHECK(cap == std::max(1, bfs_ctas / SUB), "a unit's CTA cap");
         }
         if (k > 1) CHECK(!c.singles, "a batch on a single-source graph");
+        CHECK(c.csr.n <= sl.cap, "a slot took a graph larger than its workspace");
         sl.job[j].busy = true;
         Launch L;
         L.slot = idx;
@@ -221,6 +224,9 @@ struct Sim {
         Graph &c = graphs[L.gid];
         const double d = (double)(L.end - L.start).count();
         c.est_us = c.est_us > 0 ? 0.7 * c.est_us + 0.3 * d : d;
+        // the server's finish(): the graph's batch window moved, so the other
+        // slots with a free unit look again
+        if (!c.pending.empty()) kick_others(L.slot);
         for (Query *q : L.qs) q->done = true;
     }
 
@@ -233,15 +239,15 @@ struct Sim {
             if (sl.whole || nfree(idx) == 0 || sl.drain_for != 0) continue;
             for (auto &kv : graphs) {
                 const Graph &c = kv.second;
-                if (c.pending.empty()) continue;
+                if (c.pending.empty() || c.csr.n > sl.cap) continue;
                 if (c.singles) fail("slot " + std::to_string(idx) + " idles beside a waiting single-source query");
-                const bool ready_batch = (int)c.pending.size() >= cfg.max_lanes ||
+                const bool ready_batch = stop || (int)c.pending.size() >= cfg.max_lanes ||
                                          now >= c.pending.front()->t_submit + us((int64_t)std::min(
                                                     1e6, std::max<double>(cfg.batch_window_us,
                                                                           0.01 * cfg.window_pct * c.est_us)));
                 if (!ready_batch) continue;
                 if (c.pending.size() == 1) fail("slot " + std::to_string(idx) + " idles beside a ready batch of one");
-                if (nfree(idx) == SUB) fail("a free slot idles beside a ready batch");
+                if (nfree(idx) == SUB) fail("free slot " + std::to_string(idx) + " idles beside a ready batch");
                 if (c.drainer < 0) fail("a ready batch has no slot draining for it");
             }
         }
@@ -255,27 +261,31 @@ struct Stats {
 
 // One run: `n_slots` slots, `n_single` single-source graphs and `n_batch`
 // batch graphs, `n_queries` Poisson arrivals at `rate` queries per ms
-// (rate 0: all at time 0, a closed loop).
-Stats run(uint64_t seed, int n_slots, int n_single, int n_batch, int n_queries, double rate, int max_lanes)
+// (rate 0: all at time 0, a closed loop).  mixed_caps: slot 0 holds every
+// graph, the others only some (workspaces of two sizes, as after a failed
+// resize); shutdown: the server stops once half the queries have arrived
+// (the rest still arrive and every pending batch is ready at once).
+Stats run(uint64_t seed, int n_slots, int n_single, int n_batch, int n_queries, double rate, int max_lanes,
+          bool mixed_caps, bool shutdown)
 {
     Sim s(seed);
     s.cfg.max_lanes = max_lanes;
-    for (int i = 0; i < n_slots; i++) s.slots.push_back(std::make_unique<Slot>());
+    s.cfg.window_pct = (int)(seed % 3) * 50;
+    for (int i = 0; i < n_slots; i++) {
+        s.slots.push_back(std::make_unique<Slot>());
+        if (mixed_caps && i > 0) s.slots.back()->cap = (s.rng() & 1) ? 2000 : 1000;
+    }
     s.next_ready.assign(n_slots, Time::max());
     int gid = 1;
-    double mean_us = 0;
     for (int i = 0; i < n_single + n_batch; i++) {
         Graph g;
         g.singles = i < n_single;
-        g.csr.n = 1000;
+        g.csr.n = mixed_caps && (s.rng() & 1) ? 1500 : 1000;
         g.base_us = g.singles ? s.uni(200, 20000) : s.uni(50, 3000);
-        mean_us += g.base_us;
         s.graphs[gid++] = g;
     }
-    mean_us /= (n_single + n_batch);
     const int ngraphs = n_single + n_batch;
     std::vector<std::unique_ptr<Query>> qs;
-    std::vector<Time> arrivals;
     double t = 0;
     for (int i = 0; i < n_queries; i++) {
         auto q = std::make_unique<Query>();
@@ -310,6 +320,11 @@ Stats run(uint64_t seed, int n_slots, int n_single, int n_batch, int n_queries, 
         // batch windows that ran out wake the slots waiting on them
         for (int idx = 0; idx < n_slots; idx++)
             if (s.next_ready[idx] <= s.now) s.wake(idx);
+        // shutdown: every slot's worker wakes
+        if (shutdown && !s.stop && next_arrival >= qs.size() / 2) {
+            s.stop = true;
+            for (int idx = 0; idx < n_slots; idx++) s.wake(idx);
+        }
         // arrivals: each wakes the slots with a free unit (not whole)
         while (next_arrival < qs.size() && qs[next_arrival]->t_submit <= s.now) {
             Query *q = qs[next_arrival++].get();
@@ -325,7 +340,6 @@ Stats run(uint64_t seed, int n_slots, int n_single, int n_batch, int n_queries, 
     // no query waits longer than the whole run takes one query at a time on
     // one unit of the slowest graph per query ahead of it
     CHECK(s.max_wait_us <= (double)n_queries * 25000.0 * 2.0, "a query waited too long");
-    (void)mean_us;
     Stats st;
     st.queries = n_queries;
     st.launches = s.launches;
@@ -449,13 +463,14 @@ int main()
     cases();
     Stats tot;
     int runs = 0;
-    for (uint64_t seed = 1; seed <= 40; seed++) {
+    for (uint64_t seed = 1; seed <= 60; seed++) {
         const int n_slots = 1 + (int)(seed % 6);
         const int n_single = (int)(seed % 5);
         const int n_batch = 1 + (int)((seed / 5) % 4);
         const double rate = seed % 4 == 0 ? 0.0 : 0.05 * (double)(1 + seed % 7) * n_slots;
         const int max_lanes = seed % 3 == 0 ? 4 : 64;
-        const Stats st = run(seed, n_slots, n_single, n_batch, 600, rate, max_lanes);
+        const Stats st = run(seed, n_slots, n_single, n_batch, 600, rate, max_lanes, seed % 5 == 1 && n_slots > 1,
+                             seed % 7 == 3);
         tot.queries += st.queries;
         tot.launches += st.launches;
         tot.batches += st.batches;

@@ -2,10 +2,12 @@
 
 tests/cpp/srv_plan_sim.cpp includes gpu_graphs_gb300/csrc/server_plan.h (the
 rule server.cu runs) and drives it with simulated launches and Poisson or
-closed-loop arrivals over single-source and batch graphs, 1-6 slots: no unit
-double-booked, no slot over its CTA share, batches only on whole slots,
-per-graph FIFO, no single-source query left waiting beside a free unit, and
-every query served.
+closed-loop arrivals over single-source and batch graphs, 1-6 slots, fixed
+and launch-time-scaled batch windows, slots whose workspaces hold only some
+graphs, and a shutdown part-way: no unit double-booked, no slot over its CTA
+share or taking a graph larger than its workspace, batches only on whole
+slots, per-graph FIFO, no query left waiting beside a slot that could take
+it, and every query served.
 """
 from __future__ import annotations
 
