@@ -6,7 +6,9 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <memory>
 #include <mutex>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -727,35 +729,40 @@ extern "C" int gbfs_exclusive_scan_i32(const int32_t *d_in, int64_t *d_out, int6
 
 // ---- file format ------------------------------------------------------------------
 
+namespace {
+using FileHandle = std::unique_ptr<FILE, int (*)(FILE *)>;
+FileHandle open_file(const char *path, const char *mode) { return FileHandle(fopen(path, mode), fclose); }
+}  // namespace
+
 extern "C" int gbfs_read_edge_list(const char *path, int32_t one_based, int32_t *n, int64_t *m, int32_t **src,
                                    int32_t **dst)
 {
     if (!path || !n || !m || !src || !dst) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
     *src = *dst = nullptr;
-    FILE *f = fopen(path, "rb");
+    FileHandle f = open_file(path, "rb");
     if (!f) return fail(GBFS_ERR_IO, std::string("Unable to open file ") + path);
     long long hn = 0, hm = 0;
-    if (fscanf(f, "%lld %lld", &hn, &hm) != 2 || hn < 1 || hn > INT32_MAX - 1 || hm < 0) {
-        fclose(f);
+    if (fscanf(f.get(), "%lld %lld", &hn, &hm) != 2 || hn < 1 || hn > INT32_MAX - 1 || hm < 0)
         return fail(GBFS_ERR_IO, "bad header (expected vertex and edge counts)");
-    }
     std::vector<int32_t> s, d;
-    s.reserve((size_t)std::min<long long>(hm, 1LL << 26));
-    d.reserve(s.capacity());
-    long long a, b;
-    const long long off = one_based ? 1 : 0;
-    // Pairs until end of file, like `while (infile >> from >> to)`.
-    while (fscanf(f, "%lld %lld", &a, &b) == 2) {
-        a -= off;
-        b -= off;
-        if (a < 0 || a >= hn || b < 0 || b >= hn) {
-            fclose(f);
-            return fail(GBFS_ERR_IO, "edge endpoint outside the declared vertex range");
+    try {
+        s.reserve((size_t)std::min<long long>(hm, 1LL << 26));
+        d.reserve(s.capacity());
+        long long a, b;
+        const long long off = one_based ? 1 : 0;
+        // Pairs until end of file, like `while (infile >> from >> to)`.
+        while (fscanf(f.get(), "%lld %lld", &a, &b) == 2) {
+            a -= off;
+            b -= off;
+            if (a < 0 || a >= hn || b < 0 || b >= hn)
+                return fail(GBFS_ERR_IO, "edge endpoint outside the declared vertex range");
+            s.push_back((int32_t)a);
+            d.push_back((int32_t)b);
         }
-        s.push_back((int32_t)a);
-        d.push_back((int32_t)b);
+    } catch (const std::bad_alloc &) {
+        return fail(GBFS_ERR_OOM, "host allocation failed while reading the edge list");
     }
-    fclose(f);
+    f.reset();
     const size_t cnt = s.size();
     *src = (int32_t *)malloc(sizeof(int32_t) * std::max<size_t>(cnt, 1));
     *dst = (int32_t *)malloc(sizeof(int32_t) * std::max<size_t>(cnt, 1));
@@ -781,8 +788,15 @@ extern "C" int gbfs_graph_save(const gbfs_graph *g, const char *path)
 {
     if (!g || !path) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
     const bool wide = g->csr.wide;
-    std::vector<int32_t> row32(wide ? 0 : (size_t)g->csr.n + 1), col((size_t)std::max<int64_t>(g->csr.m, 1));
-    std::vector<int64_t> row64(wide ? (size_t)g->csr.n + 1 : 0);
+    std::vector<int32_t> row32, col;
+    std::vector<int64_t> row64;
+    try {
+        row32.resize(wide ? 0 : (size_t)g->csr.n + 1);
+        col.resize((size_t)std::max<int64_t>(g->csr.m, 1));
+        row64.resize(wide ? (size_t)g->csr.n + 1 : 0);
+    } catch (const std::bad_alloc &) {
+        return fail(GBFS_ERR_OOM, "host allocation failed for the CSR copy");
+    }
     int rc = wide ? gbfs_graph_get_csr64(g, row64.data(), col.data()) : gbfs_graph_get_csr(g, row32.data(), col.data());
     if (rc) return rc;
     FILE *f = fopen(path, "wb");
@@ -811,12 +825,27 @@ extern "C" int gbfs_graph_load(const char *path, gbfs_graph **out)
     }
     const bool wide = n < 0;
     if (wide) n = n == INT32_MIN ? 0 : -n;
-    if (n < 1 || n > INT32_MAX - 1 || m < 0 || (!wide && m > INT32_MAX)) {
+    if (n < 1 || n > INT32_MAX - 1 || m < 0 || (!wide && m > INT32_MAX) || m > (int64_t)1 << 40) {
         fclose(f);
         return fail(GBFS_ERR_IO, "bad CSR header");
     }
-    std::vector<int32_t> row32(wide ? 0 : (size_t)n + 1), col((size_t)std::max<int64_t>(m, 1));
-    std::vector<int64_t> row64(wide ? (size_t)n + 1 : 0);
+    // the file must hold exactly what its header announces: a corrupt or
+    // foreign header is refused before anything is allocated for it
+    const int64_t want = 12 + ((int64_t)n + 1) * (wide ? 8 : 4) + 4 * m;
+    if (fseeko(f, 0, SEEK_END) != 0 || ftello(f) != (off_t)want || fseeko(f, 12, SEEK_SET) != 0) {
+        fclose(f);
+        return fail(GBFS_ERR_IO, "CSR file size does not match its header (" + std::to_string(want) + " bytes expected)");
+    }
+    std::vector<int32_t> row32, col;
+    std::vector<int64_t> row64;
+    try {
+        row32.resize(wide ? 0 : (size_t)n + 1);
+        col.resize((size_t)std::max<int64_t>(m, 1));
+        row64.resize(wide ? (size_t)n + 1 : 0);
+    } catch (const std::bad_alloc &) {
+        fclose(f);
+        return fail(GBFS_ERR_OOM, "host allocation failed for the CSR file");
+    }
     bool ok = (wide ? fread(row64.data(), 8, row64.size(), f) == row64.size()
                     : fread(row32.data(), 4, row32.size(), f) == row32.size()) &&
               (m == 0 || fread(col.data(), 4, (size_t)m, f) == (size_t)m);

@@ -106,6 +106,49 @@ def test_read_edge_list(gb, tmp_path):
     assert e.value.code == gb._lib.ERR_IO
 
 
+def test_csr_cache_refuses_bad_files_before_allocating(gb, tmp_path):
+    """gbfs_graph_load checks the file size against its header before it
+    allocates or touches the device (so these run without a GPU)."""
+    import struct
+
+    def write(name, n, m, payload_bytes):
+        p = tmp_path / name
+        p.write_bytes(struct.pack("<iq", n, m) + b"\0" * payload_bytes)
+        return str(p)
+
+    cases = [
+        write("truncated.bin", 5, 3, 4 * 6 + 4 * 2),         # one col entry short
+        write("longer.bin", 5, 3, 4 * 6 + 4 * 3 + 4),        # trailing bytes
+        write("huge.bin", 1_000_000_000, 1_000_000_000, 64),  # a header announcing ~12 GB
+        write("huge_wide.bin", -2_000_000_000, 1 << 36, 64),
+        write("zero.bin", 0, 0, 4),
+        write("negm.bin", 5, -1, 24),
+    ]
+    (tmp_path / "short.bin").write_bytes(b"\1\0")
+    cases.append(str(tmp_path / "short.bin"))
+    for path in cases:
+        with pytest.raises(gb.GbfsError) as e:
+            gb.Graph.load(path)
+        assert e.value.code == gb._lib.ERR_IO, (path, e.value)
+    with pytest.raises(gb.GbfsError) as e:
+        gb.Graph.load(str(tmp_path / "missing.bin"))
+    assert e.value.code == gb._lib.ERR_IO
+    # files of exactly the announced size pass the check (and then need a
+    # device: without one the upload fails with a CUDA error, not an I/O one)
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("the size check's acceptance is covered by the GPU round trips")
+    rows, cols = [0, 1, 2, 3, 3, 3], [1, 2, 0]
+    ok32 = tmp_path / "ok32.bin"
+    ok32.write_bytes(struct.pack("<iq", 5, 3) + struct.pack("<6i", *rows) + struct.pack("<3i", *cols))
+    ok64 = tmp_path / "ok64.bin"
+    ok64.write_bytes(struct.pack("<iq", -5, 3) + struct.pack("<6q", *rows) + struct.pack("<3i", *cols))
+    for path in (ok32, ok64):
+        with pytest.raises(gb.GbfsError) as e:
+            gb.Graph.load(str(path))
+        assert e.value.code != gb._lib.ERR_IO, (path, e.value)
+
+
 def test_csr_mirror_reports_missing_file(gb, tmp_path, capsys):
     with pytest.raises(gb.GbfsError):
         gb.csr(str(tmp_path / "nope.txt"))
