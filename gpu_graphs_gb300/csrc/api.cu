@@ -318,8 +318,14 @@ extern "C" int gbfs_graph_get_csr64(const gbfs_graph *g, int64_t *row_offset, in
                             dev_row ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, g->stream);
     } else {
         // 32-bit offsets widened on the host
-        std::vector<int32_t> r32(nr);
-        std::vector<int64_t> r64(nr);
+        std::vector<int32_t> r32;
+        std::vector<int64_t> r64;
+        try {
+            r32.resize(nr);
+            r64.resize(nr);
+        } catch (const std::bad_alloc &) {
+            return fail(GBFS_ERR_OOM, "host allocation failed for the row offsets");
+        }
         e = cudaMemcpyAsync(r32.data(), g->csr.row, sizeof(int32_t) * nr, cudaMemcpyDeviceToHost, g->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
         if (e == cudaSuccess) {

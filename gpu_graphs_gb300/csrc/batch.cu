@@ -9,6 +9,7 @@
 // load-balances graphs of uneven size across the whole GPU for free.
 #include <algorithm>
 #include <cstring>
+#include <new>
 #include <thread>
 #include <vector>
 
@@ -57,7 +58,13 @@ extern "C" int gbfs_graphset_from_edges(int32_t count, const int32_t *n, const i
     }
     if (voff[count] > INT32_MAX - 1) return fail(GBFS_ERR_TOO_LARGE, "union has more than 2^31-2 vertices");
     // Union edge list on the host (device member arrays are fetched first).
-    std::vector<int32_t> us((size_t)eoff[count]), ud((size_t)eoff[count]);
+    std::vector<int32_t> us, ud;
+    try {
+        us.resize((size_t)eoff[count]);
+        ud.resize((size_t)eoff[count]);
+    } catch (const std::bad_alloc &) {
+        return fail(GBFS_ERR_OOM, "host allocation failed for the union edge list");
+    }
     for (int32_t i = 0; i < count; i++) {
         const int64_t mi = m[i];
         if (mi == 0) continue;

@@ -41,9 +41,11 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <exception>
 #include <map>
 #include <memory>
 #include <mutex>
+#include <new>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -469,7 +471,14 @@ extern "C" int gbfs_server_create(const gbfs_server_config *cfg, gbfs_server **o
                 gbfs_server_destroy(s);
                 return fail(GBFS_ERR_CUDA, "cudaStreamCreate");
             }
-    for (int i = 0; i < cfg->num_slots; i++) s->workers.emplace_back(&gbfs_server::worker, s, i);
+    try {
+        s->workers.reserve(cfg->num_slots);
+        for (int i = 0; i < cfg->num_slots; i++) s->workers.emplace_back(&gbfs_server::worker, s, i);
+    } catch (const std::exception &) {
+        // stops and joins the workers already started
+        gbfs_server_destroy(s);
+        return fail(GBFS_ERR_OOM, "cannot start the server's worker threads");
+    }
     *out = s;
     return GBFS_OK;
 }
@@ -596,7 +605,12 @@ extern "C" int gbfs_server_submit(gbfs_server *s, int32_t graph_id, int32_t sour
                                   int64_t *ticket)
 {
     if (!s || !levels_out || !ticket) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
-    auto q = std::make_shared<SrvQuery>();
+    std::shared_ptr<SrvQuery> q;
+    try {
+        q = std::make_shared<SrvQuery>();
+    } catch (const std::bad_alloc &) {
+        return fail(GBFS_ERR_OOM, "host allocation failed");
+    }
     {
         std::lock_guard<std::mutex> lk(s->mu);
         if (s->stop) return fail(GBFS_ERR_SHUTDOWN, "server is shutting down");
@@ -608,8 +622,17 @@ extern "C" int gbfs_server_submit(gbfs_server *s, int32_t graph_id, int32_t sour
         q->source = source;
         q->out = levels_out;
         q->t_submit = Clock::now();
-        it->second.pending.push_back(q);
-        s->queries.emplace(q->ticket, q);
+        try {
+            s->queries.emplace(q->ticket, q);
+            try {
+                it->second.pending.push_back(q);
+            } catch (...) {
+                s->queries.erase(q->ticket);
+                throw;
+            }
+        } catch (const std::bad_alloc &) {
+            return fail(GBFS_ERR_OOM, "host allocation failed");
+        }
         *ticket = q->ticket;
         // wake the slots with a free unit; the others plan again when one of
         // their launches ends
