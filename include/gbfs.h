@@ -83,7 +83,7 @@ typedef struct gbfs_graph gbfs_graph;
  * deduplication) gets 64-bit row offsets ("wide", also with
  * GBFS_WIDE_ROWS).  A wide graph supports single-source searches (top-down
  * and, when built symmetric, direction-optimising), parents, the trace,
- * gbfs_graph_csr64 and the binary cache; multi-source searches, graph sets,
+ * gbfs_graph_get_csr64 and the binary cache; multi-source searches, graph sets,
  * the server, per-level launch modes and the transpose of a directed wide
  * graph return GBFS_ERR_TOO_LARGE.
  */
@@ -351,7 +351,10 @@ int gbfs_read_edge_list(const char *path, int32_t one_based, int32_t *n,
                         int64_t *m, int32_t **src, int32_t **dst);
 void gbfs_free(void *p);
 
-/* Binary CSR cache: int32 n, int64 m, int32 row_offset[n+1], int32 col[m]. */
+/* Binary CSR cache: int32 n, int64 m, int32 row_offset[n+1], int32 col[m]
+ * (a wide graph: int32 -n, int64 m, int64 row_offset[n+1], int32 col[m]).
+ * Loading refuses (GBFS_ERR_IO) a file whose size is not exactly what its
+ * header announces, before allocating anything for it. */
 int gbfs_graph_save(const gbfs_graph *g, const char *path);
 int gbfs_graph_load(const char *path, gbfs_graph **out);
 
