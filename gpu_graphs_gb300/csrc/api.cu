@@ -735,56 +735,18 @@ extern "C" int gbfs_exclusive_scan_i32(const int32_t *d_in, int64_t *d_out, int6
 
 // ---- file format ------------------------------------------------------------------
 
-namespace {
-using FileHandle = std::unique_ptr<FILE, int (*)(FILE *)>;
-FileHandle open_file(const char *path, const char *mode) { return FileHandle(fopen(path, mode), fclose); }
-}  // namespace
+namespace gbfs {
+// edge_list.cpp: mapped, parsed in parallel, with the semantics of the
+// reference's `while (infile >> from >> to)` loop
+int read_edge_list_text(const char *path, int32_t one_based, int32_t *n, int64_t *m, int32_t **src, int32_t **dst);
+}  // namespace gbfs
 
 extern "C" int gbfs_read_edge_list(const char *path, int32_t one_based, int32_t *n, int64_t *m, int32_t **src,
                                    int32_t **dst)
 {
     if (!path || !n || !m || !src || !dst) return fail(GBFS_ERR_INVALID_ARG, "NULL argument");
     *src = *dst = nullptr;
-    FileHandle f = open_file(path, "rb");
-    if (!f) return fail(GBFS_ERR_IO, std::string("Unable to open file ") + path);
-    long long hn = 0, hm = 0;
-    if (fscanf(f.get(), "%lld %lld", &hn, &hm) != 2 || hn < 1 || hn > INT32_MAX - 1 || hm < 0)
-        return fail(GBFS_ERR_IO, "bad header (expected vertex and edge counts)");
-    std::vector<int32_t> s, d;
-    try {
-        s.reserve((size_t)std::min<long long>(hm, 1LL << 26));
-        d.reserve(s.capacity());
-        long long a, b;
-        const long long off = one_based ? 1 : 0;
-        // Pairs until end of file, like `while (infile >> from >> to)`.
-        while (fscanf(f.get(), "%lld %lld", &a, &b) == 2) {
-            a -= off;
-            b -= off;
-            if (a < 0 || a >= hn || b < 0 || b >= hn)
-                return fail(GBFS_ERR_IO, "edge endpoint outside the declared vertex range");
-            s.push_back((int32_t)a);
-            d.push_back((int32_t)b);
-        }
-    } catch (const std::bad_alloc &) {
-        return fail(GBFS_ERR_OOM, "host allocation failed while reading the edge list");
-    }
-    f.reset();
-    const size_t cnt = s.size();
-    *src = (int32_t *)malloc(sizeof(int32_t) * std::max<size_t>(cnt, 1));
-    *dst = (int32_t *)malloc(sizeof(int32_t) * std::max<size_t>(cnt, 1));
-    if (!*src || !*dst) {
-        free(*src);
-        free(*dst);
-        *src = *dst = nullptr;
-        return fail(GBFS_ERR_OOM, "host allocation failed");
-    }
-    if (cnt) {
-        memcpy(*src, s.data(), sizeof(int32_t) * cnt);
-        memcpy(*dst, d.data(), sizeof(int32_t) * cnt);
-    }
-    *n = (int32_t)hn;
-    *m = (int64_t)cnt;
-    return GBFS_OK;
+    return gbfs::read_edge_list_text(path, one_based, n, m, src, dst);
 }
 
 // File layout: int32 n, int64 m, row offsets (n + 1), int32 col (m).  The

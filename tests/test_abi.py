@@ -106,6 +106,101 @@ def test_read_edge_list(gb, tmp_path):
     assert e.value.code == gb._lib.ERR_IO
 
 
+def _reference_scan(text: str, one_based: bool):
+    """The reference loader's `infile >> n >> m; while (infile >> a >> b)`
+    on a string: integers (optional sign) separated by whitespace, stopping at
+    the first token that does not start an integer; (n, pairs) or an error
+    string for an endpoint outside [0, n) in a pair that is read."""
+    import re
+    pos, vals = 0, []
+    num = re.compile(r"[ \t\n\v\f\r]*([+-]?[0-9]+)")
+    while True:
+        mt = num.match(text, pos)
+        if not mt:
+            break
+        vals.append(int(mt.group(1)))
+        pos = mt.end()
+    if len(vals) < 2 or vals[0] < 1 or vals[1] < 0:
+        return "header"
+    n, body = vals[0], vals[2:]
+    off = 1 if one_based else 0
+    pairs = []
+    for i in range(0, len(body) - 1, 2):
+        a, b = body[i] - off, body[i + 1] - off
+        if not (0 <= a < n and 0 <= b < n):
+            return "range"
+        pairs.append((a, b))
+    return n, pairs
+
+
+def test_edge_list_reader_semantics(gb, tmp_path):
+    """The parallel reader against the reference loop's semantics on edge
+    cases: separators, signs, a trailing unpaired integer, a token that is
+    not an integer (reading stops there, endpoints after it are not
+    checked), out-of-range endpoints before it (an error)."""
+    cases = {
+        "plain": "4 3\n1 2\n2 3\n3 4\n",
+        "crlf_tabs": "4\t3\r\n1\t2\r\n2   3\r\n\r\n3 4",
+        "signs": "4 3\n+1 +2\n2 3\n",
+        "odd_tail": "4 3\n1 2\n3",
+        "odd_tail_out_of_range": "4 3\n1 2\n99",
+        "stop_at_word": "4 3\n1 2\n# comment 3 4\n",
+        "stop_then_out_of_range": "4 3\n1 2\nx 99 99\n",
+        "glued_word": "4 3\n1 2x 3 4\n",
+        "glued_minus": "4 3\n2-3\n",
+        "out_of_range": "4 3\n1 2\n5 1\n",
+        "zero_in_one_based": "4 3\n0 1\n",
+        "header_only": "4 0\n",
+        "header_glued": "4 3x\n1 2\n",
+        "empty": "",
+        "bad_header": "four 3\n1 2\n",
+    }
+    for name, text in cases.items():
+        p = tmp_path / f"{name}.txt"
+        p.write_text(text)
+        for one_based in (True, False):
+            want = _reference_scan(text, one_based)
+            if isinstance(want, str):
+                with pytest.raises(gb.GbfsError) as e:
+                    gb.read_edge_list(str(p), one_based=one_based)
+                assert e.value.code == gb._lib.ERR_IO, (name, one_based)
+                continue
+            n, s, t = gb.read_edge_list(str(p), one_based=one_based)
+            assert n == want[0], (name, one_based)
+            assert list(zip(s.tolist(), t.tolist())) == want[1], (name, one_based)
+
+
+def test_edge_list_reader_large_file_in_chunks(gb, tmp_path):
+    """A file of several chunks: every pair in order; a non-integer token in
+    a later chunk cuts the list there, and an out-of-range endpoint after it
+    is not an error."""
+    rng = np.random.default_rng(3)
+    n, m = 1 << 20, 3_000_000
+    a = rng.integers(1, n + 1, m)
+    b = rng.integers(1, n + 1, m)
+    lines = np.char.add(np.char.add(a.astype(str), "\t" if m % 2 else " "), b.astype(str))
+    body = "\n".join(lines.tolist())
+    p = tmp_path / "big.txt"
+    p.write_text(f"{n} {m}\n" + body + "\n")
+    got_n, s, t = gb.read_edge_list(str(p))
+    assert got_n == n and np.array_equal(s, a - 1) and np.array_equal(t, b - 1)
+    cut = 2_345_678
+    lines2 = lines.copy()
+    lines2[cut] = "oops 5"
+    lines2[cut + 1] = f"{n + 7} 1"
+    p2 = tmp_path / "big_cut.txt"
+    p2.write_text(f"{n} {m}\n" + "\n".join(lines2.tolist()) + "\n")
+    _, s2, t2 = gb.read_edge_list(str(p2))
+    assert np.array_equal(s2, a[:cut] - 1) and np.array_equal(t2, b[:cut] - 1)
+    lines3 = lines.copy()
+    lines3[cut] = f"{n + 7} 1"
+    p3 = tmp_path / "big_range.txt"
+    p3.write_text(f"{n} {m}\n" + "\n".join(lines3.tolist()) + "\n")
+    with pytest.raises(gb.GbfsError) as e:
+        gb.read_edge_list(str(p3))
+    assert e.value.code == gb._lib.ERR_IO
+
+
 def test_csr_cache_refuses_bad_files_before_allocating(gb, tmp_path):
     """gbfs_graph_load checks the file size against its header before it
     allocates or touches the device (so these run without a GPU)."""
